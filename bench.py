@@ -1,0 +1,386 @@
+"""Benchmark: spin-slice updates/s of path-integral quantum annealing on the 80x80, P=20 workload.
+
+Workload (per GPU): 80x80 periodic lattice, couplings iid N(0,1) rounded to FP32
+(seeded synthetic instance), P = 20 Trotter slices, T = 0.05, transverse field
+linear 3.0 -> 1e-8 over 2000 steps, 1 local sweep per step, 1024 replicas
+started from random +-1 spins tiled over the slices.  One step = one complete
+anneal of all replicas (2.62e11 spin-slice updates).
+
+Arms:
+  (default)          the packed CUDA kernel (libpiqmc_gb300.so).
+                     value: device-timed throughput, inputs resident in HBM;
+                     e2e: the same through piqmc.fast.anneal_replicas with host
+                     buffers (H2D of the int8 configurations, D2H of the final
+                     configurations and the FP64 energies inside the timed region).
+  --impl reference   the reference's own Cython QuantumAnneal (compiled in
+                     oracle/_ref; else the oracle's C port), one process per host
+                     core, each annealing its own replica through a bounded sample
+                     of the schedule (every 20th field value).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "pathintegral-qmc_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+L_SIDE, P_SLICES, TEMP, NSCHED, REPLICAS = 80, 20, 0.05, 2000, 1024
+FLOP_PER_UPDATE = 14   # 2(z+2)+2 FP32 flop per update at z = 4 (z coupling adds, 2 Trotter, x 1/T, exp)
+METRIC = "spin-slice updates/s"
+
+
+def schedule(nsched=NSCHED):
+    return np.linspace(3.0, 1e-8, nsched)
+
+
+def instance_arrays(seed=2026):
+    """Seeded 80x80 periodic N(0,1) instance: DOK keys in insertion order (right, down per spin)."""
+    g = np.random.default_rng(seed)
+    L = L_SIDE
+    rows, cols, vals = [], [], []
+    for y in range(L):
+        for x in range(L):
+            i = y * L + x
+            rows += [i, i]
+            cols += [y * L + (x + 1) % L, ((y + 1) % L) * L + x]
+            vals += [float(np.float32(g.normal())), float(np.float32(g.normal()))]
+    return np.array(rows), np.array(cols), np.array(vals)
+
+
+def neighbors_from_keys(n, rows, cols, vals, maxnb):
+    """The (n, maxnb, 2) neighbour table in DOK key order, one pass over the keys (setup only)."""
+    nbs = np.zeros((n, maxnb, 2))
+    fill = np.zeros(n, dtype=np.int64)
+    for a, b, v in zip(rows, cols, vals):
+        nbs[a, fill[a]] = (b, v)
+        fill[a] += 1
+        if b != a:
+            nbs[b, fill[b]] = (a, v)
+            fill[b] += 1
+    return nbs
+
+
+# ------------------------------------------------------------------------------------------
+# CPU baseline: the reference's QuantumAnneal, one process per core
+# ------------------------------------------------------------------------------------------
+
+def _ref_worker_init(use_ref):
+    global _REF_QA, _NBS
+    if use_ref:
+        sys.path.insert(0, os.path.join(ROOT, "oracle", "_ref"))
+        from piqmc_ref import qmc
+        _REF_QA = ("reference", qmc.QuantumAnneal)
+    else:
+        import oracle
+        _REF_QA = ("port", oracle)
+    r, c, v = instance_arrays()
+    _NBS = neighbors_from_keys(L_SIDE * L_SIDE, r, c, v, 4)
+
+
+def _ref_worker_run(args):
+    seed, sched = args
+    n, P = L_SIDE * L_SIDE, P_SLICES
+    g = np.random.default_rng(seed)
+    conf0 = np.where(g.random(n) < 0.5, -1.0, 1.0)
+    kind, fn = _REF_QA
+    t0 = time.perf_counter()
+    if kind == "reference":
+        confs = np.tile(conf0, (P, 1)).T   # Fortran-ordered, as the reference's examples build it
+        fn(sched, 1, P, TEMP, n, confs, _NBS, np.random.RandomState(seed))
+    else:
+        import oracle
+        perms = oracle.reference_perms(np.random.RandomState(seed), n, len(sched))
+        rands = g.integers(0, 2 ** 31 - 1, size=n * P * len(sched), dtype=np.int64).astype(np.int32)
+        sp = np.ascontiguousarray(np.tile(conf0, (P, 1)).T.astype(np.int8))
+        t0 = time.perf_counter()
+        oracle.qa_sparse(sp, _NBS, sched, 1, TEMP, perms, rands)
+    return time.perf_counter() - t0
+
+
+def ref_available():
+    import sysconfig
+    d = os.path.join(ROOT, "oracle", "_ref", "piqmc_ref")
+    return os.path.exists(os.path.join(d, "qmc" + sysconfig.get_config_var("EXT_SUFFIX")))
+
+
+def cpu_baseline(steps, warmup, stride=20, cores=None):
+    """Aggregate updates/s of the reference QuantumAnneal on all host cores (bounded sample)."""
+    use_ref = ref_available()
+    cores = cores or len(os.sched_getaffinity(0))
+    sched = schedule()[::stride]
+    ctx = mp.get_context("spawn")
+    per = L_SIDE * L_SIDE * P_SLICES * len(sched)
+    rates = []
+    with ctx.Pool(cores, initializer=_ref_worker_init, initargs=(use_ref,)) as pool:
+        for it in range(warmup + steps):
+            t0 = time.perf_counter()
+            pool.map(_ref_worker_run, [(1000 * it + c, sched) for c in range(cores)], chunksize=1)
+            dt = time.perf_counter() - t0
+            if it >= warmup:
+                rates.append(per * cores / dt)
+    return {"value": float(np.median(rates)), "unit": METRIC, "cores": cores,
+            "kind": "reference" if use_ref else "port",
+            "sample": "%d processes x 1 replica x 80x80x20 x %d field steps (every %dth of the 2000-step "
+                      "schedule) per step; %s" % (cores, len(sched), stride,
+                                                  "compiled reference Cython QuantumAnneal" if use_ref
+                                                  else "oracle C port of QuantumAnneal")}
+
+
+# ------------------------------------------------------------------------------------------
+# clocks
+# ------------------------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(statistics.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------------
+
+def measured_fp32_peak(lib, torch):
+    """FP32 FMA throughput of this GPU in TFLOP/s (in-run probe kernel, best of 5)."""
+    from piqmc import _device
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks, threads, iters = sms * 8, 256, 4096
+    out = torch.empty(blocks, device="cuda")
+    best = 0.0
+    for _ in range(6):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        lib.pq_fp32_fma_probe(_device.ptr(out), iters, blocks, threads, _device.stream_handle())
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, blocks * threads * iters * 8 * 2 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    return best
+
+
+def gpu_arm(args):
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    cpu_base = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        # spawn the CPU pool before any CUDA work
+        cpu_base = cpu_baseline(steps=2, warmup=1)
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from piqmc import _native, fast
+
+    lib = _native.lib()
+    n, P, R = L_SIDE * L_SIDE, P_SLICES, args.replicas
+    rows, cols, vals = instance_arrays()
+    from piqmc import tools
+    import scipy.sparse as sps
+    J = sps.dok_matrix((n, n))
+    for a, b, v in zip(rows, cols, vals):
+        J[int(a), int(b)] = v
+    nbs = tools.GenerateNeighbors(n, J, 4)
+    prob = fast.Problem(nbs)
+    sched = schedule(args.nsched)
+    g = np.random.default_rng(1234 + rank)
+    conf0 = np.where(g.random((R, n)) < 0.5, -1, 1).astype(np.int8)
+    confs = np.ascontiguousarray(np.repeat(conf0[:, :, None], P, axis=2))
+    words0 = prob.pack(torch.from_numpy(confs))
+    words = words0.clone()
+    jp = torch.from_numpy(fast.jperp_schedule(sched, P, TEMP)).cuda()
+    status = fast._device.Status()
+    l2_flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    seed0 = 7 + 1000 * rank
+    updates = float(n) * P * R * len(sched)
+
+    def one_step(it):
+        fast.anneal(prob, words, sched, P, TEMP, seed=seed0 + it, jperp=jp, status=status, check=False,
+                    threads=args.threads, replicas_per_cta=args.rpc, replica_base=rank * R)
+
+    for it in range(args.warmup):
+        words.copy_(words0)
+        one_step(it)
+    status.raise_if_set("warmup")
+    times = []
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        wall0 = time.perf_counter()
+        for it in range(args.steps):
+            words.copy_(words0)
+            l2_flush.fill_(float(it))          # write > L2 between timed iterations
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            one_step(args.warmup + it)
+            e1.record()
+            times.append((e0, e1))
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    status.raise_if_set("timed steps")
+    step_ms = [a.elapsed_time(b) for a, b in times]
+    total_s = sum(step_ms) * 1e-3
+    if world > 1:
+        t = torch.tensor([total_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = updates * args.steps * world / total_s
+    # energies of the last anneal: residual-energy summary (per spin, best slice)
+    E = prob.energies(words, P).cpu().numpy()
+    best = E.min(axis=1) / n
+
+    # e2e through the host-buffer API
+    pinned_in = torch.from_numpy(confs).pin_memory()
+    out_c = torch.empty((R, n, P), dtype=torch.int8, pin_memory=True)
+    out_e = torch.empty((R, P), dtype=torch.float64, pin_memory=True)
+    fast.anneal_replicas(prob, pinned_in, sched, P, TEMP, seed=seed0, out=out_c, energies_out=out_e)
+    e2e_ms = []
+    for it in range(max(1, min(args.steps, 3))):
+        l2_flush.fill_(float(it))
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fast.anneal_replicas(prob, pinned_in, sched, P, TEMP, seed=seed0 + 100 + it, out=out_c, energies_out=out_e)
+        e1.record()
+        torch.cuda.synchronize()
+        e2e_ms.append(e0.elapsed_time(e1))
+    e2e_s = sum(e2e_ms) * 1e-3
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = updates * len(e2e_ms) * world / e2e_s
+
+    peak = measured_fp32_peak(lib, torch)
+    achieved_tflops = value / world * FLOP_PER_UPDATE / 1e12
+    ms_per_step = total_s / args.steps * 1e3
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "qa_fast_kernel_80x80_P20.traffic.json")
+    if os.path.exists(prof):
+        try:
+            with open(prof) as f:
+                traffic = json.load(f).get("dram_bytes_per_launch")
+        except (OSError, ValueError):
+            traffic = None
+    line = {
+        "metric": METRIC, "value": value, "unit": "updates/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+        "config": {"workload": "80x80 periodic lattice, J~N(0,1) fp32, P=20, T=0.05, G linear 3.0->1e-8 over "
+                               "%d steps, %d replicas/GPU, 1 local sweep/step, packed kernel, random class order"
+                               % (len(sched), R),
+                   "replicas_per_gpu": R, "spins": n, "slices": P, "field_steps": len(sched),
+                   "updates_per_step": updates * world, "parallelism": "replicas%d" % world,
+                   "l2": "256 MB buffer written between timed steps"},
+        "e2e": {"value": e2e_value, "unit": "updates/s", "h2d_bytes_per_step": int(confs.nbytes),
+                "d2h_bytes_per_step": int(out_c.numel() + out_e.numel() * 8)},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved_tflops / peak, "traffic": traffic,
+                     "note": "achieved = %d FP32 flop per spin-slice update x updates/s of the packed sweep "
+                             "(qa_fast_kernel, one launch per step, CUDA events); peak = in-run FP32 FMA probe "
+                             "(no FP32 figure in the measured-peaks file)" % FLOP_PER_UPDATE},
+        "clocks": clk.summary(),
+        "residual": {"best_slice_energy_per_spin_median": float(np.median(best)),
+                     "best_slice_energy_per_spin_min": float(best.min())},
+        "wall_s_timed": wall,
+    }
+    if cpu_base is not None:
+        line["cpu_baseline"] = cpu_base
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    base = cpu_baseline(steps=args.steps, warmup=args.warmup)
+    line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": "updates/s", "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32/fp64", "data": "synthetic",
+            "config": {"workload": "80x80 periodic lattice, J~N(0,1) fp32, P=20, T=0.05, G linear 3.0->1e-8 "
+                                   "(every 20th of 2000 steps), one replica per host core",
+                       "parallelism": "%d host processes" % base["cores"]},
+            "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": "updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--replicas", type=int, default=REPLICAS)
+    ap.add_argument("--nsched", type=int, default=NSCHED)
+    ap.add_argument("--threads", type=int, default=0)
+    ap.add_argument("--rpc", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,236 @@
+/*
+ * piqmc_gb300 -- C ABI of the GB300-native path-integral quantum-annealing library.
+ *
+ * Plain C types only: device pointers are passed as typed pointers, streams as
+ * `void*` (a cudaStream_t; NULL = the legacy default stream).  Every entry
+ * point returns an int status: 0 = PQ_OK, > 0 = a validation error detected on
+ * the host or by a kernel, < 0 = minus a cudaError_t.  Kernels that can fail
+ * on data they read (an out-of-range neighbour index, an exhausted random
+ * stream, a wait that timed out) record the first such error in a device
+ * status word that the caller passes; the entry point does NOT synchronise, so
+ * read that word after the stream has been synchronised (the Python layer
+ * does this and raises).
+ *
+ * Spin layouts
+ *   int8 layout  : spins[(r*n + i)*P + k] = +1/-1, replica r, spin i, slice k.
+ *   packed layout: words[r*n + i] holds the world-line of spin i of replica r,
+ *                  bit k = 1 means spin -1 in slice k (tools.spins2bits
+ *                  convention, reference piqmc/tools.pyx:24-26); 32-bit words
+ *                  for P <= 32, 64-bit words for P <= 64.
+ */
+#ifndef PIQMC_GB300_H
+#define PIQMC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PQ_OK 0
+#define PQ_ERR_INVALID_ARG 1      /* bad size, null pointer, unsupported combination */
+#define PQ_ERR_BAD_INDEX 2        /* a neighbour / permutation index outside [0, n) */
+#define PQ_ERR_RAND_EXHAUSTED 3   /* the supplied uniform stream was too short */
+#define PQ_ERR_UNSUPPORTED 4      /* e.g. P > 64 for the packed kernels */
+#define PQ_ERR_TOO_LARGE 5        /* does not fit the kernel's on-chip tiles */
+#define PQ_ERR_TIMEOUT 6          /* a bounded device-side wait gave up */
+#define PQ_ERR_LIBC_STATE 7       /* libc rand() state has an unsupported layout */
+#define PQ_ERR_NO_DEVICE 8
+
+/* Semantics flags of the reference-order sweeps. 0 = the reference as shipped. */
+#define PQ_FIX_Q2 1 /* reset the energy difference per spin (reference resets it per slice) */
+#define PQ_FIX_Q1 2 /* couple slice k to k-1, k+1 (reference couples every slice to P-1 and 1) */
+
+/* Library identification. */
+int pq_version(void);
+const char* pq_strerror(int status);
+
+/* ---------------------------------------------------------------------------
+ * Reference-order sweeps: the reference's exact update order and arithmetic.
+ * One thread walks one replica; R replicas run concurrently, each with its own
+ * spin orders (perms) and uniform stream (rands).
+ *   perms     int32 [R][nsweeps][n], nsweeps = nsched*mcsteps: the spin order of
+ *             each sweep (the successive rng.permutation results).
+ *   rands     int32 [R][rand_stride]: successive libc rand() values.
+ *   rand_used int64 [R] out: values consumed (the kernel starts at 0).
+ *   jperp     float [nsched]: J-perp per schedule step (pq_jperp_schedule).
+ *   status    int32 [1] device error word (0 = ok), first error wins.
+ * ------------------------------------------------------------------------- */
+
+/* Replaces qmc.QuantumAnneal (reference piqmc/qmc.pyx:30-136).  n = rows of the
+ * spin array and of the neighbour table (int32 [n][maxnb] index, float
+ * coupling); each sweep updates the nperm <= n spins its permutation lists
+ * (nperm = the reference's nspins), so perms is int32 [R][nsweeps][nperm]. */
+int pq_qa_sparse_reforder(int8_t* spins, const int32_t* nb_idx, const float* nb_j,
+                          int n, int nperm, int maxnb, int P, int R,
+                          const float* jperp, int nsched, int mcsteps, float temp,
+                          const int32_t* perms, const int32_t* rands, int64_t rand_stride,
+                          int64_t* rand_used, int flags, int32_t* status, void* stream);
+
+/* Replaces qmc.QuantumAnneal_dense (reference piqmc/qmc.pyx:141-242).  J is dense
+ * float64 row-major n*n; the upper triangle and the diagonal are read. */
+int pq_qa_dense_reforder(int8_t* spins, const double* J, int n, int P, int R,
+                         const float* jperp, int nsched, int mcsteps, float temp,
+                         const int32_t* perms, const int32_t* rands, int64_t rand_stride,
+                         int64_t* rand_used, int flags, int32_t* status, void* stream);
+
+/* Replaces sa.Anneal (reference piqmc/sa.pyx:50-120).  temps[g] = (float)sched[g];
+ * spins are int8 [R][n]. */
+int pq_sa_sparse_reforder(int8_t* spins, const int32_t* nb_idx, const float* nb_j,
+                          int n, int maxnb, int R, const float* temps, int nsched, int mcsteps,
+                          const int32_t* perms, const int32_t* rands, int64_t rand_stride,
+                          int64_t* rand_used, int32_t* status, void* stream);
+
+/* The same three sweeps with the exp-parity hooks.  ov_x/ov_y (device, may be
+ * NULL): sorted FP32 bit patterns x and the host libm's exp((double)x), used in
+ * place of the device exp for "close calls" (exp(x) within ~4.5 ulp of the
+ * uniform, where a last-bit difference between exp implementations could change
+ * the decision).  close_x/close_y/close_cnt (device, may be NULL): close calls
+ * that found no override, with the device exp value used; the host compares them
+ * with its own exp and reruns with overrides when one differs. */
+int pq_qa_sparse_reforder_ex(int8_t* spins, const int32_t* nb_idx, const float* nb_j, int n,
+                             int nperm, int maxnb, int P, int R, const float* jperp, int nsched, int mcsteps,
+                             float temp, const int32_t* perms, const int32_t* rands,
+                             int64_t rand_stride, int64_t* rand_used, int flags,
+                             const uint32_t* ov_x, const double* ov_y, int ov_n,
+                             uint32_t* close_x, double* close_y, int close_cap, int* close_cnt,
+                             int32_t* status, void* stream);
+int pq_qa_dense_reforder_ex(int8_t* spins, const double* J, int n, int P, int R, const float* jperp,
+                            int nsched, int mcsteps, float temp, const int32_t* perms,
+                            const int32_t* rands, int64_t rand_stride, int64_t* rand_used, int flags,
+                            const uint32_t* ov_x, const double* ov_y, int ov_n, uint32_t* close_x,
+                            double* close_y, int close_cap, int* close_cnt, int32_t* status,
+                            void* stream);
+int pq_sa_sparse_reforder_ex(int8_t* spins, const int32_t* nb_idx, const float* nb_j, int n,
+                             int maxnb, int R, const float* temps, int nsched, int mcsteps,
+                             const int32_t* perms, const int32_t* rands, int64_t rand_stride,
+                             int64_t* rand_used, const uint32_t* ov_x, const double* ov_y, int ov_n,
+                             uint32_t* close_x, double* close_y, int close_cap, int* close_cnt,
+                             int32_t* status, void* stream);
+
+/* Device exp((double)x) exactly as the reference-order kernels evaluate it
+ * (diagnostic for the libm parity scan): y[i] = exp(x[i]), and the range form
+ * y[i] = exp(float with bits first_bits + i). */
+int pq_exp_probe(const float* x, double* y, int64_t n, void* stream);
+int pq_exp_probe_range(uint32_t first_bits, int64_t count, double* y, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Host helpers (host memory, no GPU work).
+ * ------------------------------------------------------------------------- */
+
+/* J-perp of reference piqmc/qmc.pyx:95 in its C types (FP32 slices*temp, double
+ * log/tanh, FP32 result; generated piqmc/qmc.c:2063-2075).  Returns
+ * PQ_ERR_INVALID_ARG when slices*temp == 0 (the reference raises ZeroDivisionError). */
+int pq_jperp_schedule(const double* sched, int nsched, int P, float temp, float* out);
+
+/* The next n values of this process's libc rand() WITHOUT advancing it (the
+ * state is saved first and put back after; glibc only). */
+int pq_libc_rand_peek(int32_t* out, int64_t n);
+/* Advance this process's libc rand() by n draws. */
+int pq_libc_rand_skip(int64_t n);
+
+/* Host libm exp((double)x[i]) (host memory). */
+int pq_host_exp(const float* x, double* y, int64_t n);
+/* Number of FP32 inputs with bits in [first_bits, first_bits+count) whose host
+ * libm exp differs from dev[i]; the first cap of them go to bad_x/bad_y. */
+int64_t pq_host_exp_compare(uint32_t first_bits, int64_t count, const double* dev, uint32_t* bad_x,
+                            double* bad_y, int64_t cap);
+
+/* Neighbour table of tools.GenerateNeighbors (reference piqmc/tools.pyx:28-96) in
+ * one O(nnz) pass.  keys are the matrix's DOK keys in iteration order; out is
+ * float64 [nspins][maxnb][2], zero-filled first.  Returns PQ_ERR_TOO_LARGE when a
+ * row needs more than maxnb slots (the reference raises IndexError), and
+ * PQ_ERR_BAD_INDEX for keys outside [0, nspins). */
+int pq_generate_neighbors(int nspins, int64_t nkeys, const int64_t* rows, const int64_t* cols,
+                          const double* vals, int maxnb, double* out);
+
+/* Greedy colouring of the neighbour graph in spin order; color[i] in [0, ncolors).
+ * nb_idx is host int32 [n][maxnb] (self entries and padding are ignored when
+ * nb_j == 0 or index == i).  Returns the number of colours (> 0), or minus a
+ * status. */
+int pq_color_graph(int n, int maxnb, const int32_t* nb_idx, const float* nb_j, int32_t* color);
+
+/* ---------------------------------------------------------------------------
+ * Fast packed sweeps (new; no reference counterpart beyond the physics of
+ * qmc.QuantumAnneal with both reference quirks corrected).
+ *
+ * The graph is in "device order": spins are split into M update classes
+ * (independent sets: each colour of a greedy colouring cut into sub-classes),
+ * class c occupying device slots [c*S, c*S + class_size[c]) of a padded index
+ * space of n = M*S slots (unused slots are never read or written).  Couplings
+ * in SoA: nbr[m*n + i] (int32 device slot) and cpl[m*n + i] (float), m <
+ * maxdeg, padding = (i, 0.0f); field[i] = diagonal term.  One call anneals R
+ * replicas through nsched schedule steps; each step does mcsteps local sweeps
+ * then `global_moves` world-line flip passes.  A sweep visits the M classes in
+ * order (order_mode 0) or in a fresh random order per replica and sweep
+ * (order_mode 1, which brings the annealing dynamics close to the reference's
+ * random sequential order).  Counter-based Philox4x32-10 keyed by seed;
+ * `sweep_base` offsets the sweep counter so an anneal split over several calls
+ * draws the same numbers as one call.
+ * ------------------------------------------------------------------------- */
+#define PQ_MAX_CLASSES 32
+typedef struct pq_fast_params {
+    int n;              /* padded device slots = nclass * class_stride */
+    int P;              /* Trotter slices, 1..64 */
+    int R;              /* replicas */
+    int maxdeg;         /* couplings per spin (padded) */
+    int nclass;         /* update classes M, 1..PQ_MAX_CLASSES */
+    int class_stride;   /* S */
+    int class_size[PQ_MAX_CLASSES];
+    int order_mode;     /* 0 = fixed class order, 1 = random per (replica, sweep) */
+    int nsched;         /* schedule steps in this call */
+    int mcsteps;        /* local sweeps per schedule step */
+    int global_moves;   /* world-line flip passes per schedule step */
+    float temp;         /* temperature T */
+    float beta;         /* 1/T as the caller rounded it (FP32) */
+    uint64_t seed;      /* Philox key */
+    int64_t sweep_base; /* sweep counter of this call's first sweep */
+    int replica_base;   /* replica id of this call's first replica (RNG stream) */
+    int threads;        /* threads per CTA (0 = auto) */
+    int replicas_per_cta; /* (0 = auto) */
+} pq_fast_params;
+
+/* words: packed layout in device order, 32-bit words when P <= 32 else 64-bit;
+ * in/out.  jperp: device float [nsched] (ignored for P = 1).  accepts (optional,
+ * may be NULL): one device uint64 counter incremented by the accepted local flips. */
+int pq_qa_fast(void* words, const int32_t* nbr, const float* cpl, const float* field,
+               const float* jperp, const pq_fast_params* prm, unsigned long long* accepts,
+               int32_t* status, void* stream);
+
+/* pq_qa_fast with an optional per-step inverse temperature: betas (device float
+ * [nsched], may be NULL = prm->beta for every step).  With P = 1 this is a
+ * packed classical annealer (sa.Anneal physics, reference piqmc/sa.pyx:50-120,
+ * on the colour order). */
+int pq_qa_fast_ex(void* words, const int32_t* nbr, const float* cpl, const float* field,
+                  const float* jperp, const float* betas, const pq_fast_params* prm,
+                  unsigned long long* accepts, int32_t* status, void* stream);
+
+/* FP64 classical energy of every (replica, slice) from a CSR of the coupling
+ * matrix (row_ptr int64 [n+1], col int32, val double; diagonal = field),
+ * reference piqmc/sa.pyx:25-44: E = -sum_{(i,j) off-diag} J_ij s_i s_j - sum_i J_ii s_i,
+ * every stored entry once.  words (packed) and the CSR use the same spin order;
+ * out double [R][P]. */
+int pq_energy_packed(const void* words, int word_bits, int n, int P, int R,
+                     const int64_t* row_ptr, const int32_t* col, const double* val,
+                     double* out, void* stream);
+
+/* FP32 FMA throughput probe (diagnostic, used as the measured FP32 peak of
+ * the sweep's roofline): blocks x threads threads run 8 x iters dependent-free
+ * FMAs each (2 flop per FMA).  out: device float [blocks] (written only to keep
+ * the work live). */
+int pq_fp32_fma_probe(float* out, int iters, int blocks, int threads, void* stream);
+
+/* int8 layout [R][n][P] -> packed words [R][word_stride] and back.  perm[i] is
+ * the word slot of spin i (NULL = identity, then word_stride >= n); slots that no
+ * spin maps to are left untouched by packing. */
+int pq_pack_spins(const int8_t* spins, int n, int P, int R, const int32_t* perm,
+                  void* words, int word_bits, int word_stride, void* stream);
+int pq_unpack_spins(const void* words, int word_bits, int n, int P, int R, const int32_t* perm,
+                    int word_stride, int8_t* spins, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PIQMC_GB300_H */

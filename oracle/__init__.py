@@ -1,0 +1,249 @@
+"""piqmc CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+A plain-C restatement (``piqmc_oracle.c``) of the reference's sweeps, wrapped
+with ctypes, plus helpers that rebuild the exact random streams the reference
+consumes.  The product never imports this package: only ``tests/``,
+``__graft_entry__.smoke()`` and the CPU-baseline legs of ``bench.py`` do, to
+check or time beside the CUDA path.
+
+Reference semantics restated here (file:line within hadsed/pathintegral-qmc):
+
+* ``qa_sparse``  -- ``qmc.QuantumAnneal``        piqmc/qmc.pyx:30-136
+* ``qa_dense``   -- ``qmc.QuantumAnneal_dense``  piqmc/qmc.pyx:141-242
+* ``sa_sparse``  -- ``sa.Anneal``                piqmc/sa.pyx:50-120
+* ``jperp``      -- J-perp formula               piqmc/qmc.pyx:95, piqmc/qmc.c:2063-2075
+* ``classical_energy`` -- ``sa.ClassicalIsingEnergy`` piqmc/sa.pyx:25-44
+* ``generate_neighbors`` -- ``tools.GenerateNeighbors`` piqmc/tools.pyx:28-96
+* ``reference_perms`` -- the ``rng.permutation`` calls of piqmc/qmc.pyx:90-91,136
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libpiqmc_oracle.so")
+SOURCES = ("piqmc_oracle.c", "fast_oracle.c")
+
+FIX_Q2 = 1
+FIX_Q1 = 2
+
+
+def build(force=False):
+    """Compile the oracle's C with strict IEEE semantics (no contraction)."""
+    srcs = [os.path.join(HERE, s) for s in SOURCES if os.path.exists(os.path.join(HERE, s))]
+    if not force and os.path.exists(LIB) and all(
+            os.path.getmtime(LIB) >= os.path.getmtime(s) for s in srcs):
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    tmp = LIB + ".tmp%d" % os.getpid()
+    subprocess.check_call(["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math",
+                           "-fPIC", "-shared"] + srcs + ["-o", tmp, "-lm"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        P = ctypes.c_void_p
+        i32, i64, f32 = ctypes.c_int, ctypes.c_int64, ctypes.c_float
+        L.orc_qa_sparse.argtypes = [i32, i32, i32, P, P, P, i32, i32, f32, P, P, i64, P, i32]
+        L.orc_qa_sparse.restype = i64
+        L.orc_qa_dense.argtypes = [i32, i32, P, P, i32, i32, f32, P, P, i64, P, i32]
+        L.orc_qa_dense.restype = i64
+        L.orc_sa_sparse.argtypes = [i32, i32, P, P, P, i32, i32, P, P, i64, P]
+        L.orc_sa_sparse.restype = i64
+        L.orc_jperp.argtypes = [P, i32, i32, f32, P]
+        L.orc_jperp.restype = None
+        L.orc_libc_rand.argtypes = [P, i64]
+        L.orc_libc_rand.restype = None
+        L.orc_libc_srand.argtypes = [ctypes.c_uint]
+        L.orc_libc_srand.restype = None
+        _setup_fast(L)
+        _lib = L
+    return _lib
+
+
+def _setup_fast(L):
+    if not hasattr(L, "orc_fast_anneal"):
+        return
+    P = ctypes.c_void_p
+    i32, i64, f32, u64 = ctypes.c_int, ctypes.c_int64, ctypes.c_float, ctypes.c_uint64
+    L.orc_philox4x32_10.argtypes = [P, P, P]
+    L.orc_philox4x32_10.restype = None
+    L.orc_expf.argtypes = [f32]
+    L.orc_expf.restype = f32
+    L.orc_fast_anneal.argtypes = [i32, i32, i32, P, P, P, i32, i32, P, i32, P, i32, i32, f32, u64,
+                                  i64, i32, i32, P, P]
+    L.orc_fast_anneal.restype = i64
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+# ----------------------------------------------------------------------------------------
+# streams the reference consumes
+# ----------------------------------------------------------------------------------------
+
+def libc_srand(seed):
+    lib().orc_libc_srand(int(seed) & 0xFFFFFFFF)
+
+
+def libc_rand(count):
+    """The next ``count`` values of this process's libc ``rand()``."""
+    out = np.empty(int(count), dtype=np.int32)
+    if count:
+        lib().orc_libc_rand(_p(out), int(count))
+    return out
+
+
+def libc_stream(seed, count):
+    libc_srand(seed)
+    return libc_rand(count)
+
+
+def reference_perms(rng, n, nsweeps):
+    """Spin orders of ``nsweeps`` sweeps, drawn exactly as the reference draws them.
+
+    The reference draws ``rng.permutation(range(n))`` once (piqmc/qmc.pyx:90-91) and
+    then ``rng.permutation(previous)`` after every sweep (piqmc/qmc.pyx:136), so
+    ``nsweeps + 1`` calls in total; the last result is never used for a sweep.
+    """
+    out = np.empty((nsweeps, n), dtype=np.int64)
+    cur = rng.permutation(range(n))
+    for t in range(nsweeps):
+        out[t] = cur
+        cur = rng.permutation(cur)
+    return out
+
+
+# ----------------------------------------------------------------------------------------
+# reference sweeps
+# ----------------------------------------------------------------------------------------
+
+def split_neighbors(nbs):
+    """(n, maxnb, 2) float64 -> (int32 index, float32 coupling), as the reference reads them."""
+    nbs = np.asarray(nbs, dtype=np.float64)
+    idx = np.ascontiguousarray(np.trunc(nbs[:, :, 0]).astype(np.int32))
+    jv = np.ascontiguousarray(nbs[:, :, 1].astype(np.float32))
+    return idx, jv
+
+
+def jperp(sched, P, temp):
+    sched = np.ascontiguousarray(sched, dtype=np.float64)
+    out = np.empty(len(sched), dtype=np.float32)
+    lib().orc_jperp(_p(sched), len(sched), int(P), float(np.float32(temp)), _p(out))
+    return out
+
+
+def qa_sparse(spins, nbs, sched, mcsteps, temp, perms, rands, flags=0):
+    """Run the QuantumAnneal restatement on int8 spins (n, P), in place.
+
+    Returns the number of ``rands`` consumed (-1 when the stream ran out).
+    """
+    n, P = spins.shape
+    assert spins.dtype == np.int8 and spins.flags.c_contiguous
+    idx, jv = split_neighbors(nbs)
+    jp = jperp(sched, P, temp)
+    perms = np.ascontiguousarray(perms, dtype=np.int64)
+    rands = np.ascontiguousarray(rands, dtype=np.int32)
+    assert perms.shape == (len(sched) * mcsteps, n)
+    return lib().orc_qa_sparse(n, P, idx.shape[1], _p(idx), _p(jv), _p(jp), len(sched), mcsteps,
+                               float(np.float32(temp)), _p(perms), _p(rands), len(rands),
+                               _p(spins), flags)
+
+
+def qa_dense(spins, J, sched, mcsteps, temp, perms, rands, flags=0):
+    n, P = spins.shape
+    assert spins.dtype == np.int8 and spins.flags.c_contiguous
+    J = np.ascontiguousarray(J, dtype=np.float64)
+    jp = jperp(sched, P, temp)
+    perms = np.ascontiguousarray(perms, dtype=np.int64)
+    rands = np.ascontiguousarray(rands, dtype=np.int32)
+    return lib().orc_qa_dense(n, P, _p(J), _p(jp), len(sched), mcsteps, float(np.float32(temp)),
+                              _p(perms), _p(rands), len(rands), _p(spins), flags)
+
+
+def sa_sparse(spins, nbs, sched, mcsteps, perms, rands):
+    n = spins.shape[0]
+    assert spins.dtype == np.int8 and spins.flags.c_contiguous
+    idx, jv = split_neighbors(nbs)
+    temps = np.ascontiguousarray(np.asarray(sched, dtype=np.float64).astype(np.float32))
+    perms = np.ascontiguousarray(perms, dtype=np.int64)
+    rands = np.ascontiguousarray(rands, dtype=np.int32)
+    return lib().orc_sa_sparse(n, idx.shape[1], _p(idx), _p(jv), _p(temps), len(temps), mcsteps,
+                               _p(perms), _p(rands), len(rands), _p(spins))
+
+
+# ----------------------------------------------------------------------------------------
+# packed fast sweep (restated from its specification; see fast_oracle.c)
+# ----------------------------------------------------------------------------------------
+
+def philox4x32_10(ctr, key):
+    c = np.ascontiguousarray(ctr, dtype=np.uint32)
+    k = np.ascontiguousarray(key, dtype=np.uint32)
+    out = np.empty(4, dtype=np.uint32)
+    lib().orc_philox4x32_10(_p(c), _p(k), _p(out))
+    return out
+
+
+def expf_neg(x):
+    return np.float32(lib().orc_expf(float(np.float32(x))))
+
+
+def fast_anneal(nbr, cpl, field, class_size, class_stride, words, P, jperp, mcsteps, beta, seed,
+                sweep_base=0, replica=0, global_moves=0, betas=None, order_mode=1):
+    """Run one replica (uint64 world-lines ``words``, device order) in place; returns accepted flips.
+
+    nbr/cpl: (maxdeg, n) SoA tables, field (n,), class_size (M,), all in device order.
+    """
+    nbr = np.ascontiguousarray(nbr, dtype=np.int32)
+    cpl = np.ascontiguousarray(cpl, dtype=np.float32)
+    field = np.ascontiguousarray(field, dtype=np.float32)
+    csz = np.ascontiguousarray(class_size, dtype=np.int32)
+    jp = np.ascontiguousarray(jperp, dtype=np.float32)
+    assert words.dtype == np.uint64 and words.flags.c_contiguous
+    maxdeg, n = nbr.shape
+    bt = None if betas is None else np.ascontiguousarray(betas, dtype=np.float32)
+    return lib().orc_fast_anneal(n, int(P), maxdeg, _p(nbr), _p(cpl), _p(field), len(csz), int(class_stride),
+                                 _p(csz), int(order_mode), _p(jp), len(jp), int(mcsteps), float(np.float32(beta)),
+                                 int(seed) & (2**64 - 1), int(sweep_base), int(replica), int(global_moves),
+                                 _p(words), None if bt is None else _p(bt))
+
+
+# ----------------------------------------------------------------------------------------
+# energy and neighbour table
+# ----------------------------------------------------------------------------------------
+
+def classical_energy(spins, J):
+    """E = -s^T J_off s - sum(diag(J) s) in FP64 (reference piqmc/sa.pyx:41-44)."""
+    Jd = np.asarray(J.todense() if hasattr(J, "todense") else J, dtype=np.float64).copy()
+    d = np.diag(Jd).copy()
+    np.fill_diagonal(Jd, 0.0)
+    s = np.asarray(spins, dtype=np.float64)
+    return -s @ (Jd @ s) - np.sum(d * s)
+
+
+def generate_neighbors(nspins, J, maxnb):
+    """Neighbour table in DOK key order (reference piqmc/tools.pyx:77-92), O(n*nnz) as there."""
+    J = J.todok()
+    nbs = np.zeros((nspins, maxnb, 2))
+    for ispin in range(nspins):
+        ipair = 0
+        for pair in J.keys():
+            if pair[0] == ispin:
+                nbs[ispin, ipair] = (pair[1], J[pair])
+                ipair += 1
+            elif pair[1] == ispin:
+                nbs[ispin, ipair] = (pair[0], J[pair])
+                ipair += 1
+    return nbs

@@ -1,0 +1,185 @@
+/*
+ * CPU restatement of the packed fast sweep -- TEST INFRASTRUCTURE ONLY.
+ *
+ * The packed kernel has no reference counterpart (the reference has no
+ * parallel-correct sweep, no Philox and no world-line moves); this file
+ * restates, from its specification, the algorithm that kernel runs, so the
+ * GPU result can be checked bit for bit.  The algorithm itself is judged
+ * against the reference statistically: its physics is qmc.QuantumAnneal
+ * (reference piqmc/qmc.pyx:30-136) with the per-spin energy reset and the
+ * k-1/k+1 Trotter coupling, which orc_qa_sparse(flags = FIX_Q1|FIX_Q2) runs in
+ * the reference's own sequential order.
+ *
+ * Specification (mirrors the kernel's header comment):
+ *  - M update classes (independent sets); class c = device slots [c*S, c*S + size[c]).
+ *  - a sweep visits the classes in order ord[0..M-1]: identity when order_mode = 0, else
+ *    Fisher-Yates with words w[] of Philox(ctr = {0xFFFFFFFF, sweep, replica, 2 << 24 | b}),
+ *    b = 0, 1, ...: for j = M-1..1 swap ord[j], ord[(w[M-1-j] * (j+1)) >> 32]; parity
+ *    word = w[M-1] (0 when order_mode = 0).
+ *  - for the p-th visited class, slice classes in order qq = 0..nq-1, q = qq ^ bit p of
+ *    the parity word when P is even (two slice classes), q = qq otherwise; slice
+ *    classes: P even {even k},{odd k}; P odd {even k < P-1},{odd k},{P-1}; P = 1 {0}.
+ *  - update of spin i, slice k (FP32, one rounding per op, in order):
+ *      e = s_i h_i; e += J_m s_i s_jm (m = 0..maxdeg-1); t = jp s_i s_{k-1} + jp s_i s_{k+1};
+ *      ediff = -2 (e + t); flip if ediff > 0 or u < expf_neg(ediff * beta).
+ *  - u = (r >> 8) * 2^-24, r = word (m & 3) of Philox4x32-10(ctr = {i, sweep, replica,
+ *    q << 16 | m >> 2}, key = {seed lo, seed hi}) for the m-th slice of class q.
+ *  - world-line move after the local sweeps of each schedule step: classes in order
+ *    0..M-1, per spin E = sum_k e_k (FP32, k ascending), ediff = -2E, u from word 0 of
+ *    Philox(ctr = {i, last sweep of the step, replica, 1 << 24 | gm << 16 | class}).
+ *  - expf_neg: Cody-Waite reduction with ln2 = 0xB17200p-24 + lo, Taylor degree 7,
+ *    0 below x = -87.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+void orc_philox4x32_10(const uint32_t* ctr, const uint32_t* key, uint32_t* out) {
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int r = 0; r < 10; ++r) {
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        const uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        c0 = hi1 ^ c1 ^ k0;
+        c1 = lo1;
+        c2 = hi0 ^ c3 ^ k1;
+        c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+static inline float fbits(uint32_t b) { float f; memcpy(&f, &b, 4); return f; }
+static inline uint32_t bitsf(float f) { uint32_t b; memcpy(&b, &f, 4); return b; }
+
+float orc_expf(float x) {
+    if (!(x >= -87.0f)) return 0.0f;
+    const float t = x * 1.44269502162933349609375f;
+    const float nf = rintf(t);
+    float r = fmaf(-nf, 0.693145751953125f, x);
+    r = fmaf(-nf, 1.428606765330187045e-06f, r);
+    float p = 1.98412701138295233249664306640625e-04f;
+    p = fmaf(p, r, 1.388888922519981861114501953125e-03f);
+    p = fmaf(p, r, 8.333333767950534820556640625e-03f);
+    p = fmaf(p, r, 4.16666679084300994873046875e-02f);
+    p = fmaf(p, r, 1.666666716337203979492187500e-01f);
+    p = fmaf(p, r, 0.5f);
+    p = fmaf(p, r, 1.0f);
+    p = fmaf(p, r, 1.0f);
+    const int n = (int)nf;
+    return p * fbits((uint32_t)(n + 127) << 23);
+}
+
+static inline float u01(uint32_t r) { return (float)(r >> 8) * 5.9604644775390625e-8f; }
+
+static inline float signed_by(float v, uint64_t w, int k) {
+    return ((w >> k) & 1) ? fbits(bitsf(v) ^ 0x80000000u) : v;
+}
+
+/* local field part of one update: e = s_i h_i + sum_m J_m s_i s_jm  (FP32, in order) */
+static inline float local_e(const uint64_t* w, int i, int n, int maxdeg, const int32_t* nbr,
+                            const float* cpl, float h, int k) {
+    const uint64_t wi = w[i];
+    float e = signed_by(h, wi, k);
+    for (int m = 0; m < maxdeg; ++m) {
+        const int j = nbr[(int64_t)m * n + i];
+        e = e + signed_by(cpl[(int64_t)m * n + i], wi ^ w[j], k);
+    }
+    return e;
+}
+
+static int slice_count(int P, int q) {
+    if (P == 1) return 1;
+    if ((P & 1) == 0) return P >> 1;
+    return q == 2 ? 1 : (P - 1) >> 1;
+}
+
+static void class_order(int M, int order_mode, const uint32_t* key, uint32_t sweep, uint32_t replica,
+                        int* ord, uint32_t* parity) {
+    for (int c = 0; c < M; ++c) ord[c] = c;
+    *parity = 0;
+    if (order_mode == 0) return;
+    uint32_t w[4 * 9];
+    const int nb = (M + 3) / 4;
+    for (int b = 0; b < nb; ++b) {
+        const uint32_t ctr[4] = {0xFFFFFFFFu, sweep, replica, (2u << 24) | (uint32_t)b};
+        orc_philox4x32_10(ctr, key, w + 4 * b);
+    }
+    for (int j = M - 1; j >= 1; --j) {
+        const uint32_t k = (uint32_t)(((uint64_t)w[M - 1 - j] * (uint32_t)(j + 1)) >> 32);
+        const int t = ord[j]; ord[j] = ord[k]; ord[k] = t;
+    }
+    *parity = w[M - 1];
+}
+
+/* One replica through nsched schedule steps; w[i] holds device slot i's world-line
+ * (bit k set = -1).  betas may be NULL (then beta for every step).  Returns the
+ * number of accepted local flips. */
+int64_t orc_fast_anneal(int n, int P, int maxdeg, const int32_t* nbr, const float* cpl, const float* field,
+                        int M, int S, const int32_t* csize, int order_mode, const float* jperp, int nsched,
+                        int mcsteps, float beta, uint64_t seed, int64_t sweep_base, int replica,
+                        int global_moves, uint64_t* w, const float* betas) {
+    const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    const int nclass_q = P == 1 ? 1 : ((P & 1) ? 3 : 2);
+    int64_t nacc = 0;
+    int ord[32];
+    for (int g = 0; g < nsched; ++g) {
+        const float jp = P == 1 ? 0.0f : jperp[g];
+        const float bt = betas ? betas[g] : beta;
+        for (int step = 0; step < mcsteps; ++step) {
+            const uint32_t sweep = (uint32_t)(sweep_base + (int64_t)g * mcsteps + step);
+            uint32_t parity;
+            class_order(M, order_mode, key, sweep, (uint32_t)replica, ord, &parity);
+            for (int p = 0; p < M; ++p) {
+                const int cls = ord[p];
+                for (int qq = 0; qq < nclass_q; ++qq) {
+                    const int q = nclass_q == 2 ? (qq ^ (int)((parity >> p) & 1u)) : qq;
+                    const int nq = slice_count(P, q);
+                    for (int i = cls * S; i < cls * S + csize[cls]; ++i) {
+                        const uint64_t wi = w[i];
+                        uint64_t flips = 0;
+                        for (int m = 0; m < nq; ++m) {
+                            const int k = q == 2 ? P - 1 : 2 * m + q;
+                            uint32_t rnd[4];
+                            const uint32_t ctr[4] = {(uint32_t)i, sweep, (uint32_t)replica,
+                                                     (uint32_t)((q << 16) | (m >> 2))};
+                            orc_philox4x32_10(ctr, key, rnd);
+                            const float e = local_e(w, i, n, maxdeg, nbr, cpl, field[i], k);
+                            const int kl = k == 0 ? P - 1 : k - 1, kr = k == P - 1 ? 0 : k + 1;
+                            const int bl = (int)(((wi >> k) ^ (wi >> kl)) & 1);
+                            const int br = (int)(((wi >> k) ^ (wi >> kr)) & 1);
+                            const float t = (bl ? -jp : jp) + (br ? -jp : jp);
+                            const float ediff = -2.0f * (e + t);
+                            int acc = ediff > 0.0f;
+                            if (!acc) acc = u01(rnd[m & 3]) < orc_expf(ediff * bt);
+                            if (acc) { flips |= (uint64_t)1 << k; ++nacc; }
+                        }
+                        w[i] = wi ^ flips;
+                    }
+                }
+            }
+        }
+        for (int gm = 0; gm < global_moves; ++gm) {
+            const uint32_t sweep = (uint32_t)(sweep_base + (int64_t)g * mcsteps + mcsteps - 1);
+            const uint64_t mask = P >= 64 ? ~(uint64_t)0 : (((uint64_t)1 << P) - 1);
+            for (int cls = 0; cls < M; ++cls) {
+                for (int i = cls * S; i < cls * S + csize[cls]; ++i) {
+                    float E = 0.0f;
+                    for (int k = 0; k < P; ++k) E = E + local_e(w, i, n, maxdeg, nbr, cpl, field[i], k);
+                    const float ediff = -2.0f * E;
+                    uint32_t rnd[4];
+                    const uint32_t ctr[4] = {(uint32_t)i, sweep, (uint32_t)replica,
+                                             (uint32_t)((1u << 24) | ((uint32_t)gm << 16) | (uint32_t)cls)};
+                    orc_philox4x32_10(ctr, key, rnd);
+                    int acc = ediff > 0.0f;
+                    if (!acc) acc = u01(rnd[0]) < orc_expf(ediff * bt);
+                    if (acc) w[i] ^= mask;
+                }
+            }
+        }
+    }
+    return nacc;
+}

@@ -1,0 +1,77 @@
+// Shared device helpers: status words, Philox4x32-10, the sweep's own exp.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "piqmc_gb300.h"
+
+#define PQ_CUDA_TRY(expr)                                 \
+    do {                                                  \
+        cudaError_t e_ = (expr);                          \
+        if (e_ != cudaSuccess) return -(int)e_;           \
+    } while (0)
+
+static inline int pq_launch_status() {
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? PQ_OK : -(int)e;
+}
+
+// First error wins; later ones are dropped.
+__device__ __forceinline__ void pq_set_status(int32_t* status, int code) {
+    if (status) atomicCAS(status, 0, code);
+}
+
+// ----------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy
+// as 1, 2, 3", SC'11): 10 rounds of the 4x32 Philox S-box with the published
+// multipliers and Weyl key increments.
+// ----------------------------------------------------------------------------
+struct pq_u32x4 { uint32_t x, y, z, w; };
+
+__device__ __forceinline__ pq_u32x4 pq_philox(pq_u32x4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = pq_u32x4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+
+// Uniform in [0, 1) with 24 random bits: (r >> 8) * 2^-24, exact in FP32.
+__device__ __forceinline__ float pq_u01(uint32_t r) { return (float)(r >> 8) * 5.9604644775390625e-8f; }
+
+// ----------------------------------------------------------------------------
+// exp(x) for x <= 0, written for bit-identical results on the GPU and in the CPU
+// restatement of the fast sweep (every step is one IEEE-rounded FP32 op or an
+// fma, in a fixed order):
+//   n = rint(x * log2(e));  r = x - n*ln2 (two-constant Cody-Waite split,
+//   ln2 = LN2_HI + LN2_LO with LN2_HI = 0xB17200 * 2^-24 exact in 16 bits);
+//   exp(r) by its Taylor series to degree 7 (|r| <= ln2/2, truncation < 5e-9
+//   relative); result = poly * 2^n built from exponent bits.
+// Inputs below -87 return 0 (exp(-87) < 1.7e-38: below every nonzero 24-bit
+// uniform, so only u == 0 could tell the difference).
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ float pq_expf_neg(float x) {
+    if (!(x >= -87.0f)) return 0.0f;
+    const float LOG2E = 1.44269502162933349609375f;   // log2(e) rounded to FP32
+    const float LN2_HI = 0.693145751953125f;          // 0xB17200p-24
+    const float LN2_LO = 1.428606765330187045e-06f;   // ln2 - LN2_HI rounded to FP32
+    const float t = __fmul_rn(x, LOG2E);
+    const float nf = rintf(t);
+    float r = __fmaf_rn(-nf, LN2_HI, x);
+    r = __fmaf_rn(-nf, LN2_LO, r);
+    // 1/k! for k = 7..2, rounded to FP32
+    float p = 1.98412701138295233249664306640625e-04f;       // 1/5040
+    p = __fmaf_rn(p, r, 1.388888922519981861114501953125e-03f);  // 1/720
+    p = __fmaf_rn(p, r, 8.333333767950534820556640625e-03f);     // 1/120
+    p = __fmaf_rn(p, r, 4.16666679084300994873046875e-02f);      // 1/24
+    p = __fmaf_rn(p, r, 1.666666716337203979492187500e-01f);     // 1/6
+    p = __fmaf_rn(p, r, 0.5f);
+    p = __fmaf_rn(p, r, 1.0f);
+    p = __fmaf_rn(p, r, 1.0f);
+    const int n = (int)nf;                               // in [-126, 0]
+    return __fmul_rn(p, __int_as_float((n + 127) << 23));
+}

@@ -1,0 +1,352 @@
+// Reference-order sweeps: the reference's own update order and arithmetic.
+//
+// One thread walks one replica through the schedule exactly as the Cython loop
+// does (reference piqmc/qmc.pyx:93-136, piqmc/qmc.pyx:197-242,
+// piqmc/sa.pyx:94-120): same spin order (the caller's permutations), same
+// FP32 accumulator rounded after every FP64 term, same FP32 divide, libm-style
+// FP64 exp, same uniforms (the caller's libc rand() stream, consumed only when
+// the Metropolis test reaches its random branch).
+//
+// exp parity.  CUDA's exp() and the host libm's exp() are each within about
+// one ulp of the true value, so they can differ in the last bit.  Such a
+// difference can only change a decision when exp(x) lies within a couple of
+// ulps of the uniform q.  Every such "close call" is checked: the kernel looks
+// x up in an override table of host-libm values (sorted FP32 bit patterns),
+// and records close calls that had no override, so the host can compare them
+// with its own exp() and rerun the chunk with new overrides when one differs.
+// A run that records no close call is bit-exact whatever the host libm is.
+#include <math.h>
+
+#include "common.cuh"
+
+namespace {
+
+struct RefRng {
+    const int32_t* rands;
+    int64_t cap;
+    int64_t used;
+    bool dead;
+};
+
+struct ExpPatch {
+    const uint32_t* ov_x;   // sorted FP32 bit patterns
+    const double* ov_y;     // host libm exp of those inputs
+    int ov_n;
+    uint32_t* close_x;      // recorded close calls without an override
+    double* close_y;        // the device exp value used for them
+    int close_cap;
+    int* close_cnt;
+};
+
+__device__ __forceinline__ double patched_exp(float xf, double q, const ExpPatch& ep) {
+    double e = exp((double)xf);
+    const double d = fabs(e - q);
+    const bool close = d <= 1e-15 * fmax(e, q) || (q == 0.0 && e < 1e-300);
+    if (!close) return e;
+    const uint32_t xb = __float_as_uint(xf);
+    int lo = 0, hi = ep.ov_n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (ep.ov_x[mid] < xb) lo = mid + 1; else hi = mid;
+    }
+    if (lo < ep.ov_n && ep.ov_x[lo] == xb) return ep.ov_y[lo];
+    if (ep.close_cnt) {
+        const int slot = atomicAdd(ep.close_cnt, 1);
+        if (slot < ep.close_cap) { ep.close_x[slot] = xb; ep.close_y[slot] = e; }
+    }
+    return e;
+}
+
+// Metropolis test of reference piqmc/qmc.pyx:130-133 (ge = false) and
+// piqmc/sa.pyx:114-117 (ge = true): deterministic accept on ediff > 0 (>= 0),
+// otherwise exp((double)(ediff / temp)) > rand() / (double)RAND_MAX.
+__device__ __forceinline__ bool ref_accept(float ediff, float temp, bool ge, RefRng& rng,
+                                           const ExpPatch& ep, int32_t* status) {
+    if (ge ? (ediff >= 0.0f) : (ediff > 0.0f)) return true;
+    if (rng.used >= rng.cap) {
+        pq_set_status(status, PQ_ERR_RAND_EXHAUSTED);
+        rng.dead = true;
+        return false;
+    }
+    const int32_t rv = rng.rands[rng.used++];
+    const double q = (double)rv / 2147483647.0;  // glibc RAND_MAX
+    const float xf = __fdiv_rn(ediff, temp);
+    return patched_exp(xf, q, ep) > q;
+}
+
+// ediff = (float)((double)ediff + t): the generated C accumulates every FP64
+// term into the FP32 variable this way (piqmc/qmc.c:2201, 2233, 2346, 2375).
+__device__ __forceinline__ float acc(float ediff, double t) {
+    return __double2float_rn(__dadd_rn((double)ediff, t));
+}
+
+__global__ void qa_sparse_reforder_kernel(int8_t* __restrict__ spins, const int32_t* __restrict__ nb_idx,
+                                          const float* __restrict__ nb_j, int n, int nperm, int maxnb, int P, int R,
+                                          const float* __restrict__ jperp, int nsched, int mcsteps,
+                                          float temp, const int32_t* __restrict__ perms,
+                                          const int32_t* __restrict__ rands, int64_t rand_stride,
+                                          int64_t* __restrict__ rand_used, int flags, ExpPatch ep,
+                                          int32_t* status) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    int8_t* s = spins + (int64_t)r * n * P;
+    const int32_t* pr = perms + (int64_t)r * nsched * mcsteps * nperm;
+    RefRng rng{rands + (int64_t)r * rand_stride, rand_stride, 0, false};
+    for (int g = 0; g < nsched; ++g) {
+        const double jp = (double)jperp[g];
+        for (int step = 0; step < mcsteps; ++step) {
+            const int32_t* perm = pr + (int64_t)(g * mcsteps + step) * nperm;
+            for (int k = 0; k < P; ++k) {
+                // Q1 (reference as shipped): tidx is never assigned, so every
+                // slice couples to slices P-1 and 1 (piqmc/qmc.pyx:115-117).
+                int tl = P - 1, tr = 1;
+                if (flags & PQ_FIX_Q1) { tl = k == 0 ? P - 1 : k - 1; tr = k == P - 1 ? 0 : k + 1; }
+                // Q2 (as shipped): ediff is reset once per slice (piqmc/qmc.pyx:134-135).
+                float ediff = 0.0f;
+                for (int t = 0; t < nperm; ++t) {
+                    const int i = perm[t];
+                    if ((unsigned)i >= (unsigned)n) { pq_set_status(status, PQ_ERR_BAD_INDEX); rand_used[r] = -1; return; }
+                    if (flags & PQ_FIX_Q2) ediff = 0.0f;
+                    int8_t* si_p = s + (int64_t)i * P;
+                    const double si = (double)si_p[k];
+                    const int32_t* ni = nb_idx + (int64_t)i * maxnb;
+                    const float* nj = nb_j + (int64_t)i * maxnb;
+                    for (int m = 0; m < maxnb; ++m) {
+                        const int j = ni[m];
+                        const double jv = (double)nj[m];
+                        if (j == i) {
+                            ediff = acc(ediff, -2.0 * si * jv);
+                        } else {
+                            if ((unsigned)j >= (unsigned)n) { pq_set_status(status, PQ_ERR_BAD_INDEX); rand_used[r] = -1; return; }
+                            ediff = acc(ediff, -2.0 * si * (jv * (double)s[(int64_t)j * P + k]));
+                        }
+                    }
+                    ediff = acc(ediff, -2.0 * si * (jp * (double)si_p[tl]));
+                    ediff = acc(ediff, -2.0 * si * (jp * (double)si_p[tr]));
+                    if (ref_accept(ediff, temp, false, rng, ep, status)) si_p[k] = (int8_t)-si_p[k];
+                    if (rng.dead) { rand_used[r] = -1; return; }
+                }
+            }
+        }
+    }
+    rand_used[r] = rng.used;
+}
+
+__global__ void qa_dense_reforder_kernel(int8_t* __restrict__ spins, const double* __restrict__ J, int n,
+                                         int P, int R, const float* __restrict__ jperp, int nsched,
+                                         int mcsteps, float temp, const int32_t* __restrict__ perms,
+                                         const int32_t* __restrict__ rands, int64_t rand_stride,
+                                         int64_t* __restrict__ rand_used, int flags, ExpPatch ep,
+                                         int32_t* status) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    int8_t* s = spins + (int64_t)r * n * P;
+    const int32_t* pr = perms + (int64_t)r * nsched * mcsteps * n;
+    RefRng rng{rands + (int64_t)r * rand_stride, rand_stride, 0, false};
+    for (int g = 0; g < nsched; ++g) {
+        const double jp = (double)jperp[g];
+        for (int step = 0; step < mcsteps; ++step) {
+            const int32_t* perm = pr + (int64_t)(g * mcsteps + step) * n;
+            for (int k = 0; k < P; ++k) {
+                int tl = P - 1, tr = 1;
+                if (flags & PQ_FIX_Q1) { tl = k == 0 ? P - 1 : k - 1; tr = k == P - 1 ? 0 : k + 1; }
+                float ediff = 0.0f;
+                for (int t = 0; t < n; ++t) {
+                    const int i = perm[t];
+                    if ((unsigned)i >= (unsigned)n) { pq_set_status(status, PQ_ERR_BAD_INDEX); rand_used[r] = -1; return; }
+                    if (flags & PQ_FIX_Q2) ediff = 0.0f;
+                    int8_t* si_p = s + (int64_t)i * P;
+                    const double si = (double)si_p[k];
+                    // Upper triangle + diagonal only (piqmc/qmc.pyx:206-219); the
+                    // coupling stays FP64 here (it is never stored to a float).
+                    for (int j = 0; j < n; ++j) {
+                        if (j == i) {
+                            ediff = acc(ediff, -2.0 * si * J[(int64_t)i * n + i]);
+                        } else {
+                            const double jv = i < j ? J[(int64_t)i * n + j] : J[(int64_t)j * n + i];
+                            ediff = acc(ediff, -2.0 * si * (jv * (double)s[(int64_t)j * P + k]));
+                        }
+                    }
+                    ediff = acc(ediff, -2.0 * si * (jp * (double)si_p[tl]));
+                    ediff = acc(ediff, -2.0 * si * (jp * (double)si_p[tr]));
+                    if (ref_accept(ediff, temp, false, rng, ep, status)) si_p[k] = (int8_t)-si_p[k];
+                    if (rng.dead) { rand_used[r] = -1; return; }
+                }
+            }
+        }
+    }
+    rand_used[r] = rng.used;
+}
+
+__global__ void sa_sparse_reforder_kernel(int8_t* __restrict__ spins, const int32_t* __restrict__ nb_idx,
+                                          const float* __restrict__ nb_j, int n, int maxnb, int R,
+                                          const float* __restrict__ temps, int nsched, int mcsteps,
+                                          const int32_t* __restrict__ perms,
+                                          const int32_t* __restrict__ rands, int64_t rand_stride,
+                                          int64_t* __restrict__ rand_used, ExpPatch ep, int32_t* status) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    int8_t* s = spins + (int64_t)r * n;
+    const int32_t* pr = perms + (int64_t)r * nsched * mcsteps * n;
+    RefRng rng{rands + (int64_t)r * rand_stride, rand_stride, 0, false};
+    for (int g = 0; g < nsched; ++g) {
+        const float temp = temps[g];
+        for (int step = 0; step < mcsteps; ++step) {
+            const int32_t* perm = pr + (int64_t)(g * mcsteps + step) * n;
+            for (int t = 0; t < n; ++t) {
+                const int i = perm[t];
+                if ((unsigned)i >= (unsigned)n) { pq_set_status(status, PQ_ERR_BAD_INDEX); rand_used[r] = -1; return; }
+                float ediff = 0.0f;  // reset per spin (piqmc/sa.pyx:119)
+                const double si = (double)s[i];
+                const int32_t* ni = nb_idx + (int64_t)i * maxnb;
+                const float* nj = nb_j + (int64_t)i * maxnb;
+                for (int m = 0; m < maxnb; ++m) {
+                    const int j = ni[m];
+                    const double jv = (double)nj[m];
+                    if (j == i) {
+                        ediff = acc(ediff, -2.0 * si * jv);
+                    } else {
+                        if ((unsigned)j >= (unsigned)n) { pq_set_status(status, PQ_ERR_BAD_INDEX); rand_used[r] = -1; return; }
+                        ediff = acc(ediff, -2.0 * si * (jv * (double)s[j]));
+                    }
+                }
+                if (ref_accept(ediff, temp, true, rng, ep, status)) s[i] = (int8_t)-s[i];
+                if (rng.dead) { rand_used[r] = -1; return; }
+            }
+        }
+    }
+    rand_used[r] = rng.used;
+}
+
+__global__ void exp_probe_kernel(const float* __restrict__ x, double* __restrict__ y, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = exp((double)x[i]);
+}
+
+__global__ void exp_range_probe_kernel(uint32_t first_bits, int64_t count, double* __restrict__ y) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) y[i] = exp((double)__uint_as_float(first_bits + (uint32_t)i));
+}
+
+ExpPatch make_patch(const uint32_t* ov_x, const double* ov_y, int ov_n, uint32_t* close_x,
+                    double* close_y, int close_cap, int* close_cnt) {
+    ExpPatch ep;
+    ep.ov_x = ov_x; ep.ov_y = ov_y; ep.ov_n = ov_x && ov_y ? ov_n : 0;
+    ep.close_x = close_x; ep.close_y = close_y; ep.close_cnt = close_x && close_y ? close_cnt : nullptr;
+    ep.close_cap = close_cap;
+    return ep;
+}
+
+constexpr int kRefThreads = 32;
+
+}  // namespace
+
+static int check_common(int n, int P, int R, int nsched, int mcsteps, float temp) {
+    if (n <= 0 || P < 1 || R < 0 || nsched < 0 || mcsteps < 0) return PQ_ERR_INVALID_ARG;
+    if ((double)nsched * mcsteps * n > 2147483647.0 * 64) return PQ_ERR_TOO_LARGE;
+    (void)temp;
+    return PQ_OK;
+}
+
+extern "C" {
+
+int pq_qa_sparse_reforder_ex(int8_t* spins, const int32_t* nb_idx, const float* nb_j, int n,
+                             int nperm, int maxnb, int P, int R, const float* jperp, int nsched, int mcsteps,
+                             float temp, const int32_t* perms, const int32_t* rands,
+                             int64_t rand_stride, int64_t* rand_used, int flags,
+                             const uint32_t* ov_x, const double* ov_y, int ov_n,
+                             uint32_t* close_x, double* close_y, int close_cap, int* close_cnt,
+                             int32_t* status, void* stream) {
+    int st = check_common(n, P, R, nsched, mcsteps, temp);
+    if (st) return st;
+    if (P < 2 || maxnb < 0 || nperm < 0 || nperm > n || !spins || !rand_used ||
+        (maxnb > 0 && (!nb_idx || !nb_j)))
+        return PQ_ERR_INVALID_ARG;
+    if (R == 0) return PQ_OK;
+    ExpPatch ep = make_patch(ov_x, ov_y, ov_n, close_x, close_y, close_cap, close_cnt);
+    qa_sparse_reforder_kernel<<<(R + kRefThreads - 1) / kRefThreads, kRefThreads, 0, (cudaStream_t)stream>>>(
+        spins, nb_idx, nb_j, n, nperm, maxnb, P, R, jperp, nsched, mcsteps, temp, perms, rands, rand_stride,
+        rand_used, flags, ep, status);
+    return pq_launch_status();
+}
+
+int pq_qa_sparse_reforder(int8_t* spins, const int32_t* nb_idx, const float* nb_j, int n, int nperm,
+                          int maxnb, int P, int R, const float* jperp, int nsched, int mcsteps, float temp,
+                          const int32_t* perms, const int32_t* rands, int64_t rand_stride,
+                          int64_t* rand_used, int flags, int32_t* status, void* stream) {
+    return pq_qa_sparse_reforder_ex(spins, nb_idx, nb_j, n, nperm, maxnb, P, R, jperp, nsched, mcsteps, temp,
+                                    perms, rands, rand_stride, rand_used, flags, nullptr, nullptr, 0,
+                                    nullptr, nullptr, 0, nullptr, status, stream);
+}
+
+int pq_qa_dense_reforder_ex(int8_t* spins, const double* J, int n, int P, int R, const float* jperp,
+                            int nsched, int mcsteps, float temp, const int32_t* perms,
+                            const int32_t* rands, int64_t rand_stride, int64_t* rand_used, int flags,
+                            const uint32_t* ov_x, const double* ov_y, int ov_n, uint32_t* close_x,
+                            double* close_y, int close_cap, int* close_cnt, int32_t* status,
+                            void* stream) {
+    int st = check_common(n, P, R, nsched, mcsteps, temp);
+    if (st) return st;
+    if (P < 2 || !spins || !J || !rand_used) return PQ_ERR_INVALID_ARG;
+    if (R == 0) return PQ_OK;
+    ExpPatch ep = make_patch(ov_x, ov_y, ov_n, close_x, close_y, close_cap, close_cnt);
+    qa_dense_reforder_kernel<<<(R + kRefThreads - 1) / kRefThreads, kRefThreads, 0, (cudaStream_t)stream>>>(
+        spins, J, n, P, R, jperp, nsched, mcsteps, temp, perms, rands, rand_stride, rand_used, flags,
+        ep, status);
+    return pq_launch_status();
+}
+
+int pq_qa_dense_reforder(int8_t* spins, const double* J, int n, int P, int R, const float* jperp,
+                         int nsched, int mcsteps, float temp, const int32_t* perms,
+                         const int32_t* rands, int64_t rand_stride, int64_t* rand_used, int flags,
+                         int32_t* status, void* stream) {
+    return pq_qa_dense_reforder_ex(spins, J, n, P, R, jperp, nsched, mcsteps, temp, perms, rands,
+                                   rand_stride, rand_used, flags, nullptr, nullptr, 0, nullptr,
+                                   nullptr, 0, nullptr, status, stream);
+}
+
+int pq_sa_sparse_reforder_ex(int8_t* spins, const int32_t* nb_idx, const float* nb_j, int n,
+                             int maxnb, int R, const float* temps, int nsched, int mcsteps,
+                             const int32_t* perms, const int32_t* rands, int64_t rand_stride,
+                             int64_t* rand_used, const uint32_t* ov_x, const double* ov_y, int ov_n,
+                             uint32_t* close_x, double* close_y, int close_cap, int* close_cnt,
+                             int32_t* status, void* stream) {
+    int st = check_common(n, 1, R, nsched, mcsteps, 1.0f);
+    if (st) return st;
+    if (maxnb < 0 || !spins || !rand_used || (maxnb > 0 && (!nb_idx || !nb_j))) return PQ_ERR_INVALID_ARG;
+    if (R == 0) return PQ_OK;
+    ExpPatch ep = make_patch(ov_x, ov_y, ov_n, close_x, close_y, close_cap, close_cnt);
+    sa_sparse_reforder_kernel<<<(R + kRefThreads - 1) / kRefThreads, kRefThreads, 0, (cudaStream_t)stream>>>(
+        spins, nb_idx, nb_j, n, maxnb, R, temps, nsched, mcsteps, perms, rands, rand_stride, rand_used,
+        ep, status);
+    return pq_launch_status();
+}
+
+int pq_sa_sparse_reforder(int8_t* spins, const int32_t* nb_idx, const float* nb_j, int n, int maxnb,
+                          int R, const float* temps, int nsched, int mcsteps, const int32_t* perms,
+                          const int32_t* rands, int64_t rand_stride, int64_t* rand_used,
+                          int32_t* status, void* stream) {
+    return pq_sa_sparse_reforder_ex(spins, nb_idx, nb_j, n, maxnb, R, temps, nsched, mcsteps, perms,
+                                    rands, rand_stride, rand_used, nullptr, nullptr, 0, nullptr,
+                                    nullptr, 0, nullptr, status, stream);
+}
+
+// Device exp((double)x) exactly as the reference-order kernels evaluate it.
+int pq_exp_probe(const float* x, double* y, int64_t n, void* stream) {
+    if (n < 0 || (n > 0 && (!x || !y))) return PQ_ERR_INVALID_ARG;
+    if (n == 0) return PQ_OK;
+    exp_probe_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(x, y, n);
+    return pq_launch_status();
+}
+
+// Same, for the consecutive FP32 bit patterns first_bits .. first_bits+count-1.
+int pq_exp_probe_range(uint32_t first_bits, int64_t count, double* y, void* stream) {
+    if (count < 0 || (count > 0 && !y) || (uint64_t)first_bits + (uint64_t)count > 0x100000000ull)
+        return PQ_ERR_INVALID_ARG;
+    if (count == 0) return PQ_OK;
+    exp_range_probe_kernel<<<(unsigned)((count + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+        first_bits, count, y);
+    return pq_launch_status();
+}
+
+}  // extern "C"

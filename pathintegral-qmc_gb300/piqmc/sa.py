@@ -1,0 +1,124 @@
+"""Drop-in for ``piqmc.sa`` (reference piqmc/sa.pyx): classical annealing and the Ising energy.
+
+``Anneal`` keeps the reference's signature and in-place contract;
+``mode="reference"`` (default) reproduces the Cython sweep exactly (spin orders
+from ``rng``, uniforms from this process's libc ``rand()``), ``mode="fast"``
+runs the packed kernel with one slice.  ``ClassicalIsingEnergy`` evaluates the
+energy on the GPU in FP64.
+"""
+import numpy as np
+import scipy.sparse as sps
+import torch
+
+from . import _buffers, _device, _native, fast, reforder
+
+CHUNK_UPDATES = 1 << 24
+
+
+def _csr(J, n):
+    if sps.issparse(J):
+        C = sps.csr_matrix(J, dtype=np.float64)
+    else:
+        C = sps.csr_matrix(np.asarray(J, dtype=np.float64))
+    if C.shape[0] != n or C.shape[1] != n:
+        raise ValueError("J must be %d x %d, got %r" % (n, n, C.shape))
+    C.sum_duplicates()
+    return C
+
+
+def ClassicalIsingEnergy(spins, J):
+    """E = -s^T J_off s - sum_i J_ii s_i in FP64 (reference piqmc/sa.pyx:25-44).
+
+    ``spins`` is a +-1 vector of length n, or an (n, m) array whose columns are
+    configurations (then an array of m energies is returned).  ``J`` is a scipy
+    sparse matrix or a dense array; every stored entry counts once, as in the
+    reference's dense ``todense()`` product.  Evaluated by the GPU energy kernel;
+    the summation order differs from NumPy's, so results can differ from the
+    reference by FP64 rounding (relative ~1e-16 per term).
+    """
+    s = np.asarray(spins, dtype=np.float64)
+    one = s.ndim == 1
+    cols = s[:, None] if one else s
+    if cols.ndim != 2:
+        raise ValueError("spins must be a vector or an (n, m) array")
+    n, m = cols.shape
+    _buffers.check_pm1(cols, "spins")
+    C = _csr(J, n)
+    dev = _device.device()
+    sp = torch.from_numpy(np.ascontiguousarray(cols.T).astype(np.int8)[:, :, None]).to(dev)   # (m, n, 1)
+    words = torch.empty((m, n), dtype=torch.int32, device=dev)
+    L = _native.lib()
+    _native.check(L.pq_pack_spins(_device.ptr(sp), n, 1, m, None, _device.ptr(words), 32, n, _device.stream_handle()),
+                  "pq_pack_spins")
+    rp = torch.from_numpy(C.indptr.astype(np.int64)).to(dev)
+    ci = torch.from_numpy(C.indices.astype(np.int32)).to(dev)
+    cv = torch.from_numpy(C.data.astype(np.float64)).to(dev)
+    out = torch.empty((m, 1), dtype=torch.float64, device=dev)
+    _native.check(L.pq_energy_packed(_device.ptr(words), 32, n, 1, m, _device.ptr(rp), _device.ptr(ci),
+                                     _device.ptr(cv), _device.ptr(out), _device.stream_handle()),
+                  "pq_energy_packed")
+    e = out[:, 0].cpu().numpy()
+    return np.float64(e[0]) if one else e
+
+
+def Anneal(sched, mcsteps, svec, nbs, rng, *, mode="reference", seed=None):
+    """Classical simulated annealing of ``svec`` (+-1) in place through the temperatures ``sched``.
+
+    Reference: piqmc/sa.pyx:50-120.
+    """
+    sched = _buffers.float64_buffer(sched, 1, "sched")
+    mcsteps = _buffers.as_c_int(mcsteps, "mcsteps")
+    svec = _buffers.float64_buffer(svec, 1, "svec", writable=True)
+    nbs = _buffers.float64_buffer(nbs, 3, "nbs")
+    nspins = svec.size
+    if mcsteps < 0:
+        raise ValueError("mcsteps must be non-negative")
+    _buffers.check_pm1(svec, "svec")
+    if nspins and nbs.shape[0] < nspins:
+        raise ValueError("nbs has %d rows, fewer than svec.size=%d" % (nbs.shape[0], nspins))
+    if mode == "fast":
+        return _anneal_fast(sched, mcsteps, svec, nbs, rng, seed)
+    if mode != "reference":
+        raise ValueError("mode must be 'reference' or 'fast'")
+    idx, jv = reforder.split_neighbors(nbs, nspins)
+    bad = ((idx < 0) | (idx >= nspins)) & (idx != np.arange(nspins)[:, None])
+    if np.any(bad):
+        raise ValueError("neighbour index outside [0, %d)" % nspins)
+    cur = rng.permutation(range(nspins))
+    nsched = sched.size
+    if nsched == 0 or nspins == 0:
+        for _ in range(nsched * mcsteps if nspins == 0 else 0):
+            cur = rng.permutation(cur)
+        return None
+    spins = torch.from_numpy(svec.astype(np.int8)[None]).to(_device.device())
+    gchunk = max(1, CHUNK_UPDATES // max(1, nspins * mcsteps))
+    for g0 in range(0, nsched, gchunk):
+        g1 = min(nsched, g0 + gchunk)
+        count = (g1 - g0) * mcsteps
+        perms = np.empty((1, count, nspins), dtype=np.int32)
+        for t in range(count):
+            perms[0, t] = cur
+            cur = rng.permutation(cur)
+        rands = reforder.libc_peek(count * nspins)[None]
+        spins, used = reforder.anneal(spins, idx, jv, sched[g0:g1], mcsteps, perms, rands)
+        reforder.libc_skip(int(used[0]))
+    svec[:] = spins[0].cpu().numpy()
+    return None
+
+
+def _anneal_fast(sched, mcsteps, svec, nbs, rng, seed):
+    nspins = svec.size
+    if nspins == 0:
+        return None
+    temps = np.asarray(sched, dtype=np.float64).astype(np.float32)
+    if np.any(temps <= 0):
+        raise ValueError("mode='fast' needs positive temperatures")
+    if seed is None:
+        seed = _buffers.seed_from_rng(rng)
+    prob = fast.Problem(nbs, nrows=nspins)
+    words = prob.pack(torch.from_numpy(svec.astype(np.int8)[None, :, None]))
+    betas = torch.from_numpy((np.float32(1.0) / temps).astype(np.float32)).to(words.device)
+    fast.anneal(prob, words, np.zeros(len(temps)), 1, float(temps[0]) if len(temps) else 1.0, mcsteps=mcsteps,
+                seed=seed, jperp=torch.zeros(len(temps), dtype=torch.float32, device=words.device), betas=betas)
+    svec[:] = prob.unpack(words, 1)[0, :, 0].cpu().numpy()
+    return None

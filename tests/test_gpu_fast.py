@@ -1,0 +1,127 @@
+"""Packed fast kernel: bit-exact against its CPU restatement, and the FP64 energy pass against FP64 NumPy."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from pq_testutil import lattice
+
+pytestmark = pytest.mark.gpu
+
+
+def _words_u64(words):
+    w = words.cpu().numpy()
+    return (w.view(np.uint32).astype(np.uint64) if w.dtype == np.int32 else w.view(np.uint64)).copy()
+
+
+def _run_both(prob, P, R, sched, T, mcsteps, seed, global_moves=0, order_mode=1, betas=None, sweep_base=0,
+              replica_base=0, threads=0, rpc=0, rng=None):
+    from piqmc import fast
+    rng = rng or np.random.default_rng(seed)
+    spins = np.where(rng.random((R, prob.n, P)) < 0.5, -1, 1).astype(np.int8)
+    words = prob.pack(torch.from_numpy(spins))
+    w0 = _words_u64(words)
+    if P > 1:
+        jp = oracle.jperp(sched, P, T)
+    else:
+        jp = np.zeros(len(sched), np.float32)
+    bt = None if betas is None else torch.from_numpy(betas).cuda()
+    acc = torch.zeros(1, dtype=torch.int64, device="cuda")
+    fast.anneal(prob, words, sched, P, T, mcsteps=mcsteps, seed=seed, global_moves=global_moves,
+                order_mode=order_mode, betas=bt, sweep_base=sweep_base, replica_base=replica_base,
+                threads=threads, replicas_per_cta=rpc, accepts=acc,
+                jperp=torch.from_numpy(jp).cuda())
+    got = _words_u64(words)
+    tot = 0
+    for r in range(R):
+        w = w0[r].copy()
+        tot += oracle.fast_anneal(prob.nbr_host, prob.cpl_host, prob.field_host, prob.class_size,
+                                  prob.class_stride, w, P, jp, mcsteps, np.float32(1.0) / np.float32(T), seed,
+                                  sweep_base=sweep_base, replica=replica_base + r, global_moves=global_moves,
+                                  betas=betas, order_mode=order_mode)
+        np.testing.assert_array_equal(got[r], w, err_msg="replica %d" % r)
+    assert int(acc.item()) == tot
+    return prob, words
+
+
+@pytest.mark.parametrize("P", [1, 2, 3, 7, 20, 32, 33, 64])
+def test_fast_bit_exact_P(P):
+    from piqmc import fast, tools
+    g = np.random.default_rng(P)
+    J = lattice(6, True, g, dist=lambda r: r.normal(), fields=lambda r: r.normal(0, 0.3))
+    prob = fast.Problem(tools.GenerateNeighbors(36, J, 5))
+    _run_both(prob, P, 3, np.linspace(3.0, 1e-8, 12), 0.05 if P > 1 else 0.5, 1, seed=1000 + P)
+
+
+@pytest.mark.parametrize("order_mode,global_moves,mcsteps", [(0, 0, 1), (1, 1, 1), (1, 2, 3), (0, 1, 2)])
+def test_fast_bit_exact_modes(order_mode, global_moves, mcsteps):
+    from piqmc import fast, tools
+    g = np.random.default_rng(11)
+    J = lattice(7, True, g, dist=lambda r: r.uniform(-2, 2))   # odd periodic: 3 colours
+    prob = fast.Problem(tools.GenerateNeighbors(49, J, 4))
+    assert prob.ncolors == 3
+    _run_both(prob, 20, 5, np.linspace(3.0, 1e-8, 10), 0.05, mcsteps, seed=77, global_moves=global_moves,
+              order_mode=order_mode, sweep_base=123, replica_base=9)
+
+
+@pytest.mark.parametrize("threads,rpc", [(32, 1), (64, 2), (128, 4), (256, 0), (96, 3)])
+def test_fast_launch_shapes_do_not_change_results(threads, rpc):
+    from piqmc import fast, tools
+    g = np.random.default_rng(5)
+    J = lattice(8, True, g)
+    prob = fast.Problem(tools.GenerateNeighbors(64, J, 4))
+    _run_both(prob, 16, 7, np.linspace(3.0, 1e-8, 8), 0.05, 1, seed=3, threads=threads, rpc=rpc)
+
+
+def test_fast_sa_betas():
+    """P = 1 with a per-step inverse temperature: the packed classical annealer."""
+    from piqmc import fast, tools
+    g = np.random.default_rng(8)
+    J = lattice(8, True, g, fields=lambda r: r.uniform(-1, 1))
+    prob = fast.Problem(tools.GenerateNeighbors(64, J, 5))
+    temps = np.linspace(5.0, 0.05, 20).astype(np.float32)
+    _run_both(prob, 1, 4, np.zeros(20), 1.0, 2, seed=5, betas=(np.float32(1.0) / temps).astype(np.float32))
+
+
+def test_split_calls_equal_one_call():
+    """sweep_base makes an anneal split over calls draw the same numbers as one call."""
+    from piqmc import fast, tools
+    g = np.random.default_rng(9)
+    J = lattice(8, True, g)
+    prob = fast.Problem(tools.GenerateNeighbors(64, J, 4))
+    sched = np.linspace(3.0, 1e-8, 20)
+    spins = torch.from_numpy(np.where(g.random((4, 64, 20)) < 0.5, -1, 1).astype(np.int8))
+    a = prob.pack(spins)
+    b = a.clone()
+    fast.anneal(prob, a, sched, 20, 0.05, seed=4)
+    jp = torch.from_numpy(oracle.jperp(sched, 20, 0.05)).cuda()
+    fast.anneal(prob, b, sched[:7], 20, 0.05, seed=4, jperp=jp[:7])
+    fast.anneal(prob, b, sched[7:], 20, 0.05, seed=4, jperp=jp[7:], sweep_base=7)
+    assert torch.equal(a, b)
+
+
+def test_energy_pass_vs_fp64_numpy():
+    from piqmc import fast, tools
+    g = np.random.default_rng(10)
+    J = lattice(12, True, g, dist=lambda r: r.normal(), fields=lambda r: r.normal(0, 0.3))
+    prob = fast.Problem(tools.GenerateNeighbors(144, J, 5))
+    P, R = 20, 6
+    spins = np.where(g.random((R, 144, P)) < 0.5, -1, 1).astype(np.int8)
+    words = prob.pack(torch.from_numpy(spins))
+    E = prob.energies(words, P).cpu().numpy()
+    back = prob.unpack(words, P).cpu().numpy()
+    np.testing.assert_array_equal(back, spins)
+    for r in range(R):
+        for k in range(P):
+            ref = oracle.classical_energy(spins[r, :, k].astype(np.float64), J)
+            assert abs(E[r, k] - ref) <= 1e-12 * max(1.0, abs(ref))
+
+
+def test_classical_ising_energy_dropin():
+    import piqmc.sa as sa
+    from pq_testutil import dok_from, golden
+    g = golden("energy_16x16")
+    J = dok_from(g["rows"], g["cols"], g["vals"], 256)
+    got = sa.ClassicalIsingEnergy(g["spins"].T, J)
+    np.testing.assert_allclose(got, g["energies"], rtol=1e-13, atol=1e-12)
+    assert sa.ClassicalIsingEnergy(g["spins"][0], J) == pytest.approx(g["energies"][0], rel=1e-13)

@@ -1,0 +1,162 @@
+"""Reference-order CUDA kernels: bit-exact against the compiled reference's golden vectors and the oracle.
+
+The drop-in functions take their spin orders from the caller's RandomState and
+their uniforms from this process's libc rand(), exactly like the Cython code,
+so after each call the spins, the next libc value and the next rng value must
+all equal the reference's.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from pq_testutil import dok_from, golden, lattice
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def piqmc():
+    import piqmc.qmc  # noqa: F401
+    import piqmc.sa  # noqa: F401
+    import piqmc
+    return piqmc
+
+
+def test_dropin_qa_8x8_open(piqmc):
+    g = golden("qa_8x8_open")
+    P = int(g["P"])
+    confs = np.asfortranarray(np.tile(g["conf0"], (P, 1)).T)
+    oracle.libc_srand(int(g["cseed"]))
+    rng = np.random.RandomState(int(g["rseed"]))
+    piqmc.qmc.QuantumAnneal(g["sched"], int(g["mcsteps"]), P, float(g["T"]), int(g["n"]), confs, g["nbs"], rng)
+    np.testing.assert_array_equal(confs.astype(np.int8), g["final"])
+    assert oracle.libc_rand(1)[0] == g["next_rand"]
+    assert rng.randint(2 ** 31) == g["next_rng"]
+
+
+def test_dropin_sa_8x8_fields(piqmc):
+    g = golden("sa_8x8_fields")
+    sv = g["sv0"].copy()
+    oracle.libc_srand(int(g["cseed"]))
+    rng = np.random.RandomState(int(g["rseed"]))
+    piqmc.sa.Anneal(g["sched"], int(g["mcsteps"]), sv, g["nbs"], rng)
+    np.testing.assert_array_equal(sv.astype(np.int8), g["final"])
+    assert oracle.libc_rand(1)[0] == g["next_rand"]
+    assert rng.randint(2 ** 31) == g["next_rng"]
+
+
+def test_dropin_qa_dense_48(piqmc):
+    g = golden("qa_dense_48")
+    P = int(g["P"])
+    confs = np.asfortranarray(np.tile(g["conf0"], (P, 1)).T)
+    oracle.libc_srand(int(g["cseed"]))
+    rng = np.random.RandomState(int(g["rseed"]))
+    piqmc.qmc.QuantumAnneal_dense(g["sched"], int(g["mcsteps"]), P, float(g["T"]), g["J"].shape[0], confs, g["J"], rng)
+    np.testing.assert_array_equal(confs.astype(np.int8), g["final"])
+    assert oracle.libc_rand(1)[0] == g["next_rand"]
+    assert rng.randint(2 ** 31) == g["next_rng"]
+
+
+def test_dropin_boixo8(piqmc):
+    """The reference's own diamond-graph test (testing/test_boixo.py:90-114), bit-exact."""
+    g = golden("boixo8")
+    rng = np.random.RandomState(123)
+    confs = np.tile(np.array([2 * rng.randint(2) - 1 for _ in range(8)], dtype=np.float64), (5, 1)).T
+    oracle.libc_srand(1)
+    piqmc.qmc.QuantumAnneal(np.linspace(0.5, 1e-8, 10), 3, 5, 0.01, 8, confs, g["nbs"], rng)
+    np.testing.assert_array_equal(confs.astype(np.int8), g["final"])
+    J = dok_from(g["rows"], g["cols"], g["vals"], 8)
+    energies = [piqmc.sa.ClassicalIsingEnergy(confs[:, k], J) for k in range(5)]
+    assert np.sum(energies) == -8.0 * 5
+    for s, e in zip(g["svecs"], g["energies"]):
+        assert piqmc.sa.ClassicalIsingEnergy(s, J) == e
+
+
+def test_batch_32x32_eight_replicas(piqmc):
+    """Eight reference-order replicas in one launch, each with its recorded streams."""
+    from piqmc import reforder
+    g = golden("qa_32x32_periodic")
+    n, P, sched = int(g["n"]), int(g["P"]), g["sched"]
+    J = dok_from(g["rows"], g["cols"], g["vals"], n)
+    nbs = oracle.generate_neighbors(n, J, 4)
+    idx, jv = reforder.split_neighbors(nbs)
+    perms, rands, spins, rngs = [], [], [], []
+    L = n * P * len(sched) + 1
+    for rep in range(8):
+        rng = np.random.RandomState(int(g["rseed"][rep]))
+        perms.append(oracle.reference_perms(rng, n, len(sched)).astype(np.int32))
+        rngs.append(rng)
+        rands.append(oracle.libc_stream(int(g["cseed"][rep]), L))
+        spins.append(np.tile(g["conf0"][rep], (P, 1)).T.astype(np.int8))
+    out, used = reforder.quantum_anneal(np.array(spins), idx, jv, sched, 1, float(g["T"]), np.array(perms),
+                                        np.array(rands))
+    out = out.cpu().numpy()
+    for rep in range(8):
+        bits = np.unpackbits(g["final_bits"][rep])[: n * P].reshape(n, P).astype(bool)
+        np.testing.assert_array_equal(out[rep] < 0, bits)
+        assert rands[rep][used[rep]] == g["next_rand"][rep]
+        assert rngs[rep].randint(2 ** 31) == g["next_rng"][rep]
+
+
+@pytest.mark.parametrize("flags", [0, 1, 2, 3])
+def test_random_cases_vs_oracle(piqmc, flags):
+    from piqmc import reforder
+    g = np.random.default_rng(flags)
+    for L, P, periodic in [(5, 7, True), (6, 4, False), (4, 2, True)]:
+        J = lattice(L, periodic, g, dist=lambda r: r.normal(), fields=lambda r: r.normal(0, 0.5))
+        n = L * L
+        nbs = oracle.generate_neighbors(n, J, 5)
+        idx, jv = reforder.split_neighbors(nbs)
+        sched = np.linspace(2.0, 1e-6, 15)
+        R = 3
+        spins = np.where(g.random((R, n, P)) < 0.5, -1, 1).astype(np.int8)
+        perms = np.array([oracle.reference_perms(np.random.RandomState(r), n, 30) for r in range(R)])
+        rands = g.integers(0, 2 ** 31 - 1, size=(R, n * P * 30), dtype=np.int64).astype(np.int32)
+        out, used = reforder.quantum_anneal(spins, idx, jv, sched, 2, 0.3, perms, rands, flags=flags)
+        out = out.cpu().numpy()
+        for r in range(R):
+            sp = spins[r].copy()
+            u = oracle.qa_sparse(sp, nbs, sched, 2, 0.3, perms[r], rands[r], flags=flags)
+            np.testing.assert_array_equal(out[r], sp)
+            assert used[r] == u
+
+
+def test_edge_cases(piqmc):
+    g = np.random.default_rng(7)
+    J = lattice(4, True, g)
+    nbs = oracle.generate_neighbors(16, J, 4)
+    confs = np.ones((16, 4))
+    rng = np.random.RandomState(0)
+    before = rng.get_state()[1].copy()
+    # empty schedule: one permutation drawn, nothing else
+    piqmc.qmc.QuantumAnneal(np.zeros(0), 1, 4, 0.1, 16, confs, nbs, rng)
+    assert np.all(confs == 1)
+    # zero temperature: ZeroDivisionError like the reference (slices*temp == 0)
+    with pytest.raises(ZeroDivisionError):
+        piqmc.qmc.QuantumAnneal(np.ones(3), 1, 4, 0.0, 16, confs, nbs, rng)
+    with pytest.raises(ValueError):
+        piqmc.qmc.QuantumAnneal(np.ones(3, dtype=np.float32), 1, 4, 0.1, 16, confs, nbs, rng)
+    with pytest.raises(ValueError):
+        piqmc.qmc.QuantumAnneal(np.ones(3), 1, 4, 0.1, 16, confs[:, 0], nbs, rng)
+    bad = nbs.copy()
+    bad[3, 1, 0] = 99
+    with pytest.raises(ValueError):
+        piqmc.qmc.QuantumAnneal(np.ones(3), 1, 4, 0.1, 16, confs, bad, rng)
+    with pytest.raises(ValueError):
+        piqmc.qmc.QuantumAnneal(np.ones(3), 1, 4, 0.1, 16, confs * 0.5, nbs, rng)
+    del before
+    # nspins smaller than the rows: the rows beyond nspins are fixed boundary spins
+    confs = np.where(g.random((16, 6)) < 0.5, -1.0, 1.0)
+    c2 = confs.copy()
+    oracle.libc_srand(5)
+    piqmc.qmc.QuantumAnneal(np.linspace(1, 0.1, 4), 2, 6, 0.2, 10, confs, nbs, np.random.RandomState(3))
+    np.testing.assert_array_equal(confs[10:], c2[10:])
+    rands = oracle.libc_stream(5, 10 * 6 * 8 + 1)
+    perms = oracle.reference_perms(np.random.RandomState(3), 10, 8)
+    # oracle on the full rows with a permutation over the first 10 spins only
+    sp = c2.astype(np.int8)
+    import piqmc.reforder as rf
+    idx, jv = rf.split_neighbors(nbs)
+    out, used = rf.quantum_anneal(sp[None], idx, jv, np.linspace(1, 0.1, 4), 2, 0.2, perms[None], rands[None],
+                                  nperm=10)
+    np.testing.assert_array_equal(out.cpu().numpy()[0], confs.astype(np.int8))
