@@ -41,6 +41,9 @@ extern "C" {
 /* Semantics flags of the reference-order sweeps. 0 = the reference as shipped. */
 #define PQ_FIX_Q2 1 /* reset the energy difference per spin (reference resets it per slice) */
 #define PQ_FIX_Q1 2 /* couple slice k to k-1, k+1 (reference couples every slice to P-1 and 1) */
+#define PQ_ACC_FP64 4 /* accumulate in FP64 exactly as the generated C writes it; needed only when
+                         |2 J| or |2 J-perp| can overflow FP32 (the FP32 accumulator is otherwise
+                         identical, bit for bit) */
 
 /* Library identification. */
 int pq_version(void);
@@ -105,7 +108,7 @@ int pq_qa_dense_reforder_ex(int8_t* spins, const double* J, int n, int P, int R,
 int pq_sa_sparse_reforder_ex(int8_t* spins, const int32_t* nb_idx, const float* nb_j, int n,
                              int maxnb, int R, const float* temps, int nsched, int mcsteps,
                              const int32_t* perms, const int32_t* rands, int64_t rand_stride,
-                             int64_t* rand_used, const uint32_t* ov_x, const double* ov_y, int ov_n,
+                             int64_t* rand_used, int flags, const uint32_t* ov_x, const double* ov_y, int ov_n,
                              uint32_t* close_x, double* close_y, int close_cap, int* close_cnt,
                              int32_t* status, void* stream);
 
@@ -220,6 +223,12 @@ int pq_energy_packed(const void* words, int word_bits, int n, int P, int R,
  * FMAs each (2 flop per FMA).  out: device float [blocks] (written only to keep
  * the work live). */
 int pq_fp32_fma_probe(float* out, int iters, int blocks, int threads, void* stream);
+
+/* Diagnostic for the packed sweep's exact fast path: atomically raises *out (a
+ * non-negative double's bit pattern, device memory) to the largest
+ * |2^fl(x log2 e) (hardware approximation) / expf_neg(x) - 1| over the FP32 x
+ * with bit patterns first_bits .. first_bits+count-1 that lie in [-87, 0]. */
+int pq_guard_band_probe(uint32_t first_bits, int64_t count, unsigned long long* out, void* stream);
 
 /* int8 layout [R][n][P] -> packed words [R][word_stride] and back.  perm[i] is
  * the word slot of spin i (NULL = identity, then word_stride >= n); slots that no

@@ -22,7 +22,7 @@
  *  - update of spin i, slice k (FP32, one rounding per op, in order):
  *      e = s_i h_i; e += J_m s_i s_jm (m = 0..maxdeg-1); t = jp s_i s_{k-1} + jp s_i s_{k+1};
  *      ediff = -2 (e + t); flip if ediff > 0 or u < expf_neg(ediff * beta).
- *  - u = (r >> 8) * 2^-24, r = word (m & 3) of Philox4x32-10(ctr = {i, sweep, replica,
+ *  - u = (r >> 9) * 2^-23, r = word (m & 3) of Philox4x32-10(ctr = {i, sweep, replica,
  *    q << 16 | m >> 2}, key = {seed lo, seed hi}) for the m-th slice of class q.
  *  - world-line move after the local sweeps of each schedule step: classes in order
  *    0..M-1, per spin E = sum_k e_k (FP32, k ascending), ediff = -2E, u from word 0 of
@@ -73,7 +73,7 @@ float orc_expf(float x) {
     return p * fbits((uint32_t)(n + 127) << 23);
 }
 
-static inline float u01(uint32_t r) { return (float)(r >> 8) * 5.9604644775390625e-8f; }
+static inline float u01(uint32_t r) { return fbits((r >> 9) | 0x3f800000u) - 1.0f; }
 
 static inline float signed_by(float v, uint64_t w, int k) {
     return ((w >> k) & 1) ? fbits(bitsf(v) ^ 0x80000000u) : v;
@@ -182,4 +182,19 @@ int64_t orc_fast_anneal(int n, int P, int maxdeg, const int32_t* nbr, const floa
         }
     }
     return nacc;
+}
+
+/* Largest |orc_expf(x) / exp(x) - 1| over the FP32 inputs with bit patterns in
+ * [lo_bits, hi_bits] stepping by `step` (negative floats: larger pattern = more
+ * negative).  Used to bound the approximation the fast paths rely on. */
+double orc_expf_max_relerr(uint32_t lo_bits, uint32_t hi_bits, uint32_t step) {
+    double worst = 0.0;
+    for (uint64_t b = lo_bits; b <= hi_bits; b += step) {
+        const float x = fbits((uint32_t)b);
+        if (!(x >= -87.0f)) continue;
+        const double e = exp((double)x);
+        const double r = fabs((double)orc_expf(x) / e - 1.0);
+        if (r > worst) worst = r;
+    }
+    return worst;
 }

@@ -40,8 +40,18 @@ __device__ __forceinline__ pq_u32x4 pq_philox(pq_u32x4 c, uint32_t k0, uint32_t 
     return c;
 }
 
-// Uniform in [0, 1) with 24 random bits: (r >> 8) * 2^-24, exact in FP32.
-__device__ __forceinline__ float pq_u01(uint32_t r) { return (float)(r >> 8) * 5.9604644775390625e-8f; }
+// Uniform in [0, 1) with 23 random bits: (1 + (r >> 9) * 2^-23) - 1 = (r >> 9) * 2^-23, exact.
+__device__ __forceinline__ float pq_u01(uint32_t r) {
+    return __fsub_rn(__uint_as_float((r >> 9) | 0x3f800000u), 1.0f);
+}
+
+// Hardware 2^x approximation (MUFU), used only inside a guard band that makes the
+// final decision independent of its exact rounding.
+__device__ __forceinline__ float pq_ex2_approx(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 
 // ----------------------------------------------------------------------------
 // exp(x) for x <= 0, written for bit-identical results on the GPU and in the CPU

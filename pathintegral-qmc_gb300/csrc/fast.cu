@@ -23,7 +23,7 @@
 //   e = s_i h_i;  e += J_im s_i s_jm for m = 0..maxdeg-1 (table order);
 //   t = (J-perp s_i s_{k-1}) + (J-perp s_i s_{k+1})      (exact);
 //   ediff = -2 (e + t);  flip if ediff > 0 or u < expf_neg(ediff * beta).
-// Uniforms: Philox4x32-10, key = seed.  Local update: counter = (device slot i,
+// u = (r >> 9) * 2^-23.  Uniforms: Philox4x32-10, key = seed.  Local update: counter = (device slot i,
 // sweep, replica, q << 16 | m >> 2), word m & 3 for the m-th slice of class q.
 // World-line move: counter = (i, last sweep of the step, replica,
 // 1 << 24 | gm << 16 | class), word 0.  Class order of a sweep: counter =
@@ -121,7 +121,58 @@ __device__ __forceinline__ void load_site(const W* rw, int i, int n, int maxdeg,
     }
 }
 
-template <typename W, int MAXDEG>
+// Metropolis decision for sum = e + t (ediff = -2 sum): flip when sum < 0, else
+// when u < expf_neg(fl(sum * m2beta)) with m2beta = -2 beta.  The hardware 2^x
+// (argument fl(sum * m2blog2e), m2blog2e = fl(-2 beta log2 e)) settles it outside
+// a 1e-4 relative guard band -- its error against expf_neg is below 2e-5 for every
+// argument above -87 -- and expf_neg itself settles the rest, so the result is
+// exactly the specification's.
+__device__ __forceinline__ bool decide(float sum, float u, float m2beta, float m2blog2e) {
+    if (sum < 0.0f) return true;
+    const float pf = pq_ex2_approx(__fmul_rn(sum, m2blog2e));
+    if (u > __fmul_rn(pf, 1.0001f)) return false;
+    if (u < __fmul_rn(pf, 0.9999f) && pf > 1e-30f) return true;
+    return u < pq_expf_neg(__fmul_rn(sum, m2beta));
+}
+
+// One spin's local update over the slices of slice class q, P = 2 * NQ <= 32
+// slices fixed at compile time, DEG couplings.  Same arithmetic and uniforms as
+// the generic path.
+template <int NQ, int DEG>
+__device__ __forceinline__ uint32_t update_fixed(uint32_t wi, const uint32_t (&d)[DEG], const float (&J)[DEG], float h,
+                                                 float jp, int q, uint32_t i, uint32_t sweep, uint32_t rep, uint32_t key0,
+                                                 uint32_t key1, float m2beta, float m2blog2e) {
+    constexpr int P = 2 * NQ;
+    constexpr uint32_t MASK = P >= 32 ? 0xffffffffu : ((1u << P) - 1u);
+    const uint32_t up = ((wi << 1) | (wi >> (P - 1))) & MASK;
+    const uint32_t dn = ((wi >> 1) | (wi << (P - 1))) & MASK;
+    const uint32_t wq = wi >> q, dl = (wi ^ up) >> q, dr = (wi ^ dn) >> q;
+    uint32_t dq[DEG];
+#pragma unroll
+    for (int m = 0; m < DEG; ++m) dq[m] = d[m] >> q;
+    uint32_t flips = 0;
+#pragma unroll
+    for (int blk = 0; blk < (NQ + 3) / 4; ++blk) {
+        const pq_u32x4 rnd = pq_philox(pq_u32x4{i, sweep, rep, (uint32_t)((q << 16) | blk)}, key0, key1);
+        const uint32_t rw4[4] = {rnd.x, rnd.y, rnd.z, rnd.w};
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+            const int mm = blk * 4 + jj;
+            if (mm < NQ) {
+                const int sh = 31 - 2 * mm;  // bit 2*mm of the q-shifted words -> sign bit
+                float e = flip_sign(h, (wq << sh) & 0x80000000u);
+#pragma unroll
+                for (int m = 0; m < DEG; ++m) e = __fadd_rn(e, flip_sign(J[m], (dq[m] << sh) & 0x80000000u));
+                const float t = __fadd_rn(flip_sign(jp, (dl << sh) & 0x80000000u), flip_sign(jp, (dr << sh) & 0x80000000u));
+                const float sum = __fadd_rn(e, t);
+                if (decide(sum, pq_u01(rw4[jj]), m2beta, m2blog2e)) flips |= 1u << (2 * mm);
+            }
+        }
+    }
+    return flips << q;
+}
+
+template <typename W, int MAXDEG, int NQC>
 __global__ void __launch_bounds__(512) qa_fast_kernel(W* __restrict__ words, const int32_t* __restrict__ nbr,
                                                       const float* __restrict__ cpl,
                                                       const float* __restrict__ field,
@@ -154,6 +205,8 @@ __global__ void __launch_bounds__(512) qa_fast_kernel(W* __restrict__ words, con
     for (int g = 0; g < a.nsched; ++g) {
         const float jp = P == 1 ? 0.0f : jperp[g];
         const float beta = betas ? betas[g] : a.beta;
+        const float m2beta = __fmul_rn(-2.0f, beta);                          // exact
+        const float m2blog2e = __fmul_rn(m2beta, 1.44269502162933349609375f);  // guard-band argument scale
         for (int step = 0; step < a.mcsteps; ++step) {
             const uint32_t sweep = (uint32_t)(a.sweep_base + (int64_t)g * a.mcsteps + step);
             if (threadIdx.x < nrep)
@@ -175,11 +228,18 @@ __global__ void __launch_bounds__(512) qa_fast_kernel(W* __restrict__ words, con
                             float J[MAXDEG];
                             load_site<W, MAXDEG>(rw, i, n, a.maxdeg, nbr, cpl, wi, d, J, bad);
                             const float h = __ldg(field + i);
+                            const uint32_t ctr2 = (uint32_t)(a.replica_base + r0 + rl);
+                            if constexpr (NQC > 0) {
+                                const uint32_t fl = update_fixed<NQC, MAXDEG>(
+                                    (uint32_t)wi, reinterpret_cast<const uint32_t(&)[MAXDEG]>(d), J, h, jp, q,
+                                    (uint32_t)i, sweep, ctr2, a.key0, a.key1, m2beta, m2blog2e);
+                                rw[i] = wi ^ (W)fl;
+                                nacc += __popc(fl);
+                            } else {
                             W dl, dr;
                             trotter_diffs<W>(wi, P, mask, dl, dr);
                             W flips = 0;
                             const int nq = slice_count(P, q);
-                            const uint32_t ctr2 = (uint32_t)(a.replica_base + r0 + rl);
                             for (int mb = 0; mb * 4 < nq; ++mb) {
                                 const pq_u32x4 rnd = pq_philox(
                                     pq_u32x4{(uint32_t)i, sweep, ctr2, (uint32_t)((q << 16) | mb)}, a.key0, a.key1);
@@ -195,15 +255,14 @@ __global__ void __launch_bounds__(512) qa_fast_kernel(W* __restrict__ words, con
                                             if (m < a.maxdeg) e = __fadd_rn(e, flip_sign(J[m], bit_to_sign<W>(d[m], k)));
                                         const float t = __fadd_rn(flip_sign(jp, bit_to_sign<W>(dl, k)),
                                                                   flip_sign(jp, bit_to_sign<W>(dr, k)));
-                                        const float ediff = __fmul_rn(-2.0f, __fadd_rn(e, t));
-                                        bool acc = ediff > 0.0f;
-                                        if (!acc) acc = pq_u01(rw4[jj]) < pq_expf_neg(__fmul_rn(ediff, beta));
+                                        const bool acc = decide(__fadd_rn(e, t), pq_u01(rw4[jj]), m2beta, m2blog2e);
                                         flips |= (W)acc << k;
                                         nacc += acc;
                                     }
                                 }
                             }
                             rw[i] = wi ^ flips;
+                            }
                         }
                         s += blockDim.x;
                         while (s >= S) { s -= S; ++rl; }
@@ -235,14 +294,11 @@ __global__ void __launch_bounds__(512) qa_fast_kernel(W* __restrict__ words, con
                                 if (m < a.maxdeg) e = __fadd_rn(e, flip_sign(J[m], bit_to_sign<W>(d[m], k)));
                             E = __fadd_rn(E, e);
                         }
-                        const float ediff = __fmul_rn(-2.0f, E);
                         const uint32_t ctr2 = (uint32_t)(a.replica_base + r0 + rl);
                         const pq_u32x4 rnd = pq_philox(
                             pq_u32x4{(uint32_t)i, sweep, ctr2, (uint32_t)((1u << 24) | ((uint32_t)gm << 16) | (uint32_t)cls)},
                             a.key0, a.key1);
-                        bool acc = ediff > 0.0f;
-                        if (!acc) acc = pq_u01(rnd.x) < pq_expf_neg(__fmul_rn(ediff, beta));
-                        if (acc) rw[i] = wi ^ mask;
+                        if (decide(E, pq_u01(rnd.x), m2beta, m2blog2e)) rw[i] = wi ^ mask;
                     }
                     s += blockDim.x;
                     while (s >= S) { s -= S; ++rl; }
@@ -310,20 +366,20 @@ __global__ void unpack_kernel(const W* __restrict__ words, int n, int P, int R, 
     for (int k = 0; k < P; ++k) s[k] = ((w >> k) & 1) ? -1 : 1;
 }
 
-template <typename W, int MAXDEG>
+template <typename W, int MAXDEG, int NQC>
 int launch_fast(void* words, const int32_t* nbr, const float* cpl, const float* field, const float* jperp,
                 const float* betas, const FastArgs& a, int threads, unsigned long long* accepts,
                 int32_t* status, cudaStream_t stream) {
     const size_t smem = (size_t)a.rpc * a.n * sizeof(W);
     static bool attr_set = false;
     if (!attr_set) {
-        PQ_CUDA_TRY(cudaFuncSetAttribute(qa_fast_kernel<W, MAXDEG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        PQ_CUDA_TRY(cudaFuncSetAttribute(qa_fast_kernel<W, MAXDEG, NQC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          220 * 1024));
         attr_set = true;
     }
     const int grid = (a.R + a.rpc - 1) / a.rpc;
-    qa_fast_kernel<W, MAXDEG><<<grid, threads, smem, stream>>>((W*)words, nbr, cpl, field, jperp, betas, a,
-                                                               accepts, status);
+    qa_fast_kernel<W, MAXDEG, NQC><<<grid, threads, smem, stream>>>((W*)words, nbr, cpl, field, jperp, betas, a,
+                                                                    accepts, status);
     return pq_launch_status();
 }
 
@@ -331,12 +387,20 @@ template <typename W>
 int dispatch_deg(void* words, const int32_t* nbr, const float* cpl, const float* field, const float* jperp,
                  const float* betas, const FastArgs& a, int threads, unsigned long long* accepts,
                  int32_t* status, cudaStream_t stream) {
+    if constexpr (sizeof(W) == 4) {
+        // compile-time slice counts for the common even P with exactly four couplings
+        if (a.maxdeg == 4) {
+            if (a.P == 20) return launch_fast<W, 4, 10>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status, stream);
+            if (a.P == 16) return launch_fast<W, 4, 8>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status, stream);
+            if (a.P == 32) return launch_fast<W, 4, 16>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status, stream);
+        }
+    }
     if (a.maxdeg <= 4)
-        return launch_fast<W, 4>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status, stream);
+        return launch_fast<W, 4, 0>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status, stream);
     if (a.maxdeg <= 8)
-        return launch_fast<W, 8>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status, stream);
+        return launch_fast<W, 8, 0>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status, stream);
     if (a.maxdeg <= 16)
-        return launch_fast<W, 16>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status, stream);
+        return launch_fast<W, 16, 0>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status, stream);
     return PQ_ERR_UNSUPPORTED;
 }
 
@@ -351,9 +415,35 @@ __global__ void fma_probe_kernel(float* out, int iters, float a, float b) {
     if (s == 1234.5f) out[blockIdx.x] = s;  // keeps the chains live
 }
 
+// Largest |ex2.approx(fl(x log2 e)) / expf_neg(x) - 1| over FP32 x with the given
+// bit patterns (x >= -87, expf_neg(x) > 1e-30); atomic max on the bit pattern of a
+// non-negative double.
+__global__ void guard_probe_kernel(uint32_t first_bits, int64_t count, unsigned long long* out) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double worst = 0.0;
+    if (t < count) {
+        const float x = __uint_as_float(first_bits + (uint32_t)t);
+        if (x >= -87.0f && x <= 0.0f) {
+            const float ps = pq_expf_neg(x);
+            const float pf = pq_ex2_approx(__fmul_rn(x, 1.44269502162933349609375f));
+            if (ps > 1e-30f) worst = fabs((double)pf / (double)ps - 1.0);
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) worst = fmax(worst, __shfl_down_sync(0xffffffffu, worst, off));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(worst));
+}
+
 }  // namespace
 
 extern "C" {
+
+// Diagnostic: checks the accuracy the packed sweep's guard band relies on.
+int pq_guard_band_probe(uint32_t first_bits, int64_t count, unsigned long long* out, void* stream) {
+    if (!out || count < 0 || (uint64_t)first_bits + (uint64_t)count > 0x100000000ull) return PQ_ERR_INVALID_ARG;
+    if (count == 0) return PQ_OK;
+    guard_probe_kernel<<<(unsigned)((count + 255) / 256), 256, 0, (cudaStream_t)stream>>>(first_bits, count, out);
+    return pq_launch_status();
+}
 
 // FP32 FMA peak probe: blocks x threads threads, each 8 x iters FMAs (2 flop each).
 int pq_fp32_fma_probe(float* out, int iters, int blocks, int threads, void* stream) {

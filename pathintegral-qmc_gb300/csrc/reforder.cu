@@ -15,6 +15,18 @@
 // and records close calls that had no override, so the host can compare them
 // with its own exp() and rerun the chunk with new overrides when one differs.
 // A run that records no close call is bit-exact whatever the host libm is.
+//
+// Speed.  FP64 is a narrow pipe on this GPU, so the common path avoids it
+// without changing a single decision:
+//  * every sparse-sweep term is +-2 x (an FP32 value), exact in FP32, and
+//    (float)((double)a + (double)b) equals the FP32 sum a + b for FP32 a, b
+//    (double rounding through a format with 53 >= 2*24 + 2 bits is innocuous),
+//    so the accumulator runs in FP32 (flag PQ_ACC_FP64 forces the FP64 form for
+//    couplings near the FP32 overflow threshold, where 2J would overflow);
+//  * the Metropolis test first compares an FP32 exp (max relative error 7.9e-8
+//    over every FP32 input in [-87, 0], checked exhaustively) and an FP32
+//    uniform (relative error < 2e-7) with a 2e-6 relative guard band; only
+//    inside the band -- or for rand() == 0 -- does it evaluate the FP64 test.
 #include <math.h>
 
 #include "common.cuh"
@@ -57,6 +69,17 @@ __device__ __forceinline__ double patched_exp(float xf, double q, const ExpPatch
     return e;
 }
 
+// Decision of exp(x) > rv / RAND_MAX when it is certain from FP32 values:
+// 1 accept, 0 reject, -1 undecided (inside the guard band, rv == 0, x > 0 or NaN).
+__device__ __forceinline__ int fp32_decide(float xf, int32_t rv) {
+    if (rv <= 0 || !(xf <= 0.0f)) return -1;
+    const float ef = pq_expf_neg(xf);
+    const float qf = __fmul_rn((float)rv, 4.656612873077392578125e-10f);  // 2^-31; (rv/(2^31-1))(1 - 4.7e-10)
+    if (ef > __fmul_rn(qf, 1.000002f)) return 1;
+    if (ef < __fmul_rn(qf, 0.999998f)) return 0;
+    return -1;
+}
+
 // Metropolis test of reference piqmc/qmc.pyx:130-133 (ge = false) and
 // piqmc/sa.pyx:114-117 (ge = true): deterministic accept on ediff > 0 (>= 0),
 // otherwise exp((double)(ediff / temp)) > rand() / (double)RAND_MAX.
@@ -69,8 +92,10 @@ __device__ __forceinline__ bool ref_accept(float ediff, float temp, bool ge, Ref
         return false;
     }
     const int32_t rv = rng.rands[rng.used++];
-    const double q = (double)rv / 2147483647.0;  // glibc RAND_MAX
     const float xf = __fdiv_rn(ediff, temp);
+    const int quick = fp32_decide(xf, rv);
+    if (quick >= 0) return quick != 0;
+    const double q = (double)rv / 2147483647.0;  // glibc RAND_MAX
     return patched_exp(xf, q, ep) > q;
 }
 
@@ -80,6 +105,15 @@ __device__ __forceinline__ float acc(float ediff, double t) {
     return __double2float_rn(__dadd_rn((double)ediff, t));
 }
 
+// The same for a term -2 * s * v with v an FP32 value and s = +-1: the term is
+// exact in FP32, and the double-rounded sum equals the FP32 sum (see above).
+template <bool FP64>
+__device__ __forceinline__ float acc2(float ediff, float s2, float v) {
+    if (FP64) return acc(ediff, (double)s2 * (double)v);
+    return __fadd_rn(ediff, __fmul_rn(s2, v));
+}
+
+template <bool FP64>
 __global__ void qa_sparse_reforder_kernel(int8_t* __restrict__ spins, const int32_t* __restrict__ nb_idx,
                                           const float* __restrict__ nb_j, int n, int nperm, int maxnb, int P, int R,
                                           const float* __restrict__ jperp, int nsched, int mcsteps,
@@ -93,7 +127,7 @@ __global__ void qa_sparse_reforder_kernel(int8_t* __restrict__ spins, const int3
     const int32_t* pr = perms + (int64_t)r * nsched * mcsteps * nperm;
     RefRng rng{rands + (int64_t)r * rand_stride, rand_stride, 0, false};
     for (int g = 0; g < nsched; ++g) {
-        const double jp = (double)jperp[g];
+        const float jpf = jperp[g];
         for (int step = 0; step < mcsteps; ++step) {
             const int32_t* perm = pr + (int64_t)(g * mcsteps + step) * nperm;
             for (int k = 0; k < P; ++k) {
@@ -108,21 +142,21 @@ __global__ void qa_sparse_reforder_kernel(int8_t* __restrict__ spins, const int3
                     if ((unsigned)i >= (unsigned)n) { pq_set_status(status, PQ_ERR_BAD_INDEX); rand_used[r] = -1; return; }
                     if (flags & PQ_FIX_Q2) ediff = 0.0f;
                     int8_t* si_p = s + (int64_t)i * P;
-                    const double si = (double)si_p[k];
+                    const float s2 = -2.0f * (float)si_p[k];
                     const int32_t* ni = nb_idx + (int64_t)i * maxnb;
                     const float* nj = nb_j + (int64_t)i * maxnb;
                     for (int m = 0; m < maxnb; ++m) {
                         const int j = ni[m];
-                        const double jv = (double)nj[m];
+                        const float jv = nj[m];
                         if (j == i) {
-                            ediff = acc(ediff, -2.0 * si * jv);
+                            ediff = acc2<FP64>(ediff, s2, jv);
                         } else {
                             if ((unsigned)j >= (unsigned)n) { pq_set_status(status, PQ_ERR_BAD_INDEX); rand_used[r] = -1; return; }
-                            ediff = acc(ediff, -2.0 * si * (jv * (double)s[(int64_t)j * P + k]));
+                            ediff = acc2<FP64>(ediff, s2, s[(int64_t)j * P + k] > 0 ? jv : -jv);
                         }
                     }
-                    ediff = acc(ediff, -2.0 * si * (jp * (double)si_p[tl]));
-                    ediff = acc(ediff, -2.0 * si * (jp * (double)si_p[tr]));
+                    ediff = acc2<FP64>(ediff, s2, si_p[tl] > 0 ? jpf : -jpf);
+                    ediff = acc2<FP64>(ediff, s2, si_p[tr] > 0 ? jpf : -jpf);
                     if (ref_accept(ediff, temp, false, rng, ep, status)) si_p[k] = (int8_t)-si_p[k];
                     if (rng.dead) { rand_used[r] = -1; return; }
                 }
@@ -178,6 +212,7 @@ __global__ void qa_dense_reforder_kernel(int8_t* __restrict__ spins, const doubl
     rand_used[r] = rng.used;
 }
 
+template <bool FP64>
 __global__ void sa_sparse_reforder_kernel(int8_t* __restrict__ spins, const int32_t* __restrict__ nb_idx,
                                           const float* __restrict__ nb_j, int n, int maxnb, int R,
                                           const float* __restrict__ temps, int nsched, int mcsteps,
@@ -197,17 +232,17 @@ __global__ void sa_sparse_reforder_kernel(int8_t* __restrict__ spins, const int3
                 const int i = perm[t];
                 if ((unsigned)i >= (unsigned)n) { pq_set_status(status, PQ_ERR_BAD_INDEX); rand_used[r] = -1; return; }
                 float ediff = 0.0f;  // reset per spin (piqmc/sa.pyx:119)
-                const double si = (double)s[i];
+                const float s2 = -2.0f * (float)s[i];
                 const int32_t* ni = nb_idx + (int64_t)i * maxnb;
                 const float* nj = nb_j + (int64_t)i * maxnb;
                 for (int m = 0; m < maxnb; ++m) {
                     const int j = ni[m];
-                    const double jv = (double)nj[m];
+                    const float jv = nj[m];
                     if (j == i) {
-                        ediff = acc(ediff, -2.0 * si * jv);
+                        ediff = acc2<FP64>(ediff, s2, jv);
                     } else {
                         if ((unsigned)j >= (unsigned)n) { pq_set_status(status, PQ_ERR_BAD_INDEX); rand_used[r] = -1; return; }
-                        ediff = acc(ediff, -2.0 * si * (jv * (double)s[j]));
+                        ediff = acc2<FP64>(ediff, s2, s[j] > 0 ? jv : -jv);
                     }
                 }
                 if (ref_accept(ediff, temp, true, rng, ep, status)) s[i] = (int8_t)-s[i];
@@ -264,9 +299,15 @@ int pq_qa_sparse_reforder_ex(int8_t* spins, const int32_t* nb_idx, const float* 
         return PQ_ERR_INVALID_ARG;
     if (R == 0) return PQ_OK;
     ExpPatch ep = make_patch(ov_x, ov_y, ov_n, close_x, close_y, close_cap, close_cnt);
-    qa_sparse_reforder_kernel<<<(R + kRefThreads - 1) / kRefThreads, kRefThreads, 0, (cudaStream_t)stream>>>(
-        spins, nb_idx, nb_j, n, nperm, maxnb, P, R, jperp, nsched, mcsteps, temp, perms, rands, rand_stride,
-        rand_used, flags, ep, status);
+    const dim3 grid((R + kRefThreads - 1) / kRefThreads), block(kRefThreads);
+    if (flags & PQ_ACC_FP64)
+        qa_sparse_reforder_kernel<true><<<grid, block, 0, (cudaStream_t)stream>>>(
+            spins, nb_idx, nb_j, n, nperm, maxnb, P, R, jperp, nsched, mcsteps, temp, perms, rands, rand_stride,
+            rand_used, flags, ep, status);
+    else
+        qa_sparse_reforder_kernel<false><<<grid, block, 0, (cudaStream_t)stream>>>(
+            spins, nb_idx, nb_j, n, nperm, maxnb, P, R, jperp, nsched, mcsteps, temp, perms, rands, rand_stride,
+            rand_used, flags, ep, status);
     return pq_launch_status();
 }
 
@@ -308,7 +349,7 @@ int pq_qa_dense_reforder(int8_t* spins, const double* J, int n, int P, int R, co
 int pq_sa_sparse_reforder_ex(int8_t* spins, const int32_t* nb_idx, const float* nb_j, int n,
                              int maxnb, int R, const float* temps, int nsched, int mcsteps,
                              const int32_t* perms, const int32_t* rands, int64_t rand_stride,
-                             int64_t* rand_used, const uint32_t* ov_x, const double* ov_y, int ov_n,
+                             int64_t* rand_used, int flags, const uint32_t* ov_x, const double* ov_y, int ov_n,
                              uint32_t* close_x, double* close_y, int close_cap, int* close_cnt,
                              int32_t* status, void* stream) {
     int st = check_common(n, 1, R, nsched, mcsteps, 1.0f);
@@ -316,9 +357,13 @@ int pq_sa_sparse_reforder_ex(int8_t* spins, const int32_t* nb_idx, const float* 
     if (maxnb < 0 || !spins || !rand_used || (maxnb > 0 && (!nb_idx || !nb_j))) return PQ_ERR_INVALID_ARG;
     if (R == 0) return PQ_OK;
     ExpPatch ep = make_patch(ov_x, ov_y, ov_n, close_x, close_y, close_cap, close_cnt);
-    sa_sparse_reforder_kernel<<<(R + kRefThreads - 1) / kRefThreads, kRefThreads, 0, (cudaStream_t)stream>>>(
-        spins, nb_idx, nb_j, n, maxnb, R, temps, nsched, mcsteps, perms, rands, rand_stride, rand_used,
-        ep, status);
+    const dim3 grid((R + kRefThreads - 1) / kRefThreads), block(kRefThreads);
+    if (flags & PQ_ACC_FP64)
+        sa_sparse_reforder_kernel<true><<<grid, block, 0, (cudaStream_t)stream>>>(
+            spins, nb_idx, nb_j, n, maxnb, R, temps, nsched, mcsteps, perms, rands, rand_stride, rand_used, ep, status);
+    else
+        sa_sparse_reforder_kernel<false><<<grid, block, 0, (cudaStream_t)stream>>>(
+            spins, nb_idx, nb_j, n, maxnb, R, temps, nsched, mcsteps, perms, rands, rand_stride, rand_used, ep, status);
     return pq_launch_status();
 }
 
@@ -327,7 +372,7 @@ int pq_sa_sparse_reforder(int8_t* spins, const int32_t* nb_idx, const float* nb_
                           const int32_t* rands, int64_t rand_stride, int64_t* rand_used,
                           int32_t* status, void* stream) {
     return pq_sa_sparse_reforder_ex(spins, nb_idx, nb_j, n, maxnb, R, temps, nsched, mcsteps, perms,
-                                    rands, rand_stride, rand_used, nullptr, nullptr, 0, nullptr,
+                                    rands, rand_stride, rand_used, 0, nullptr, nullptr, 0, nullptr,
                                     nullptr, 0, nullptr, status, stream);
 }
 

