@@ -1,0 +1,149 @@
+"""Host-side logic and the C ABI library, without a GPU."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+import scipy.sparse as sps
+
+import oracle
+from pq_testutil import ROOT, dok_from, golden, lattice
+
+
+@pytest.fixture(scope="session")
+def native():
+    import build_native
+    build_native.build()
+    from piqmc import _native
+    return _native.lib()
+
+
+def _header_symbols():
+    text = open(os.path.join(ROOT, "include", "piqmc_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(pq_\w+)\s*\(", text)))
+
+
+def test_library_exports_every_header_symbol(native):
+    syms = _header_symbols()
+    assert len(syms) >= 20
+    lib = ctypes.CDLL(os.path.join(ROOT, "pathintegral-qmc_gb300", "piqmc", "_native", "libpiqmc_gb300.so"))
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+    from piqmc import _native
+    assert set(_native.SIGNATURES) >= set(syms)
+    assert native.pq_version() >= 1
+    assert native.pq_strerror(2) == b"index outside [0, nspins)"
+
+
+def test_generate_neighbors_golden_and_random(native):
+    from piqmc import tools
+    g = golden("neighbors_5node")
+    J = dok_from(g["rows"], g["cols"], g["vals"], 5)
+    np.testing.assert_array_equal(tools.GenerateNeighbors(5, J, 4), g["nbs"])
+    rng = np.random.default_rng(3)
+    for trial in range(5):
+        n = 30
+        A = sps.random(n, n, density=0.08, random_state=trial, format="dok")
+        for i in range(0, n, 3):
+            A[i, i] = rng.normal()
+        deg = np.zeros(n, int)
+        for (a, b) in A.keys():
+            deg[a] += 1
+            if a != b:
+                deg[b] += 1
+        m = int(deg.max())
+        np.testing.assert_array_equal(tools.GenerateNeighbors(n, A, m), oracle.generate_neighbors(n, A, m))
+        with pytest.raises(IndexError):
+            tools.GenerateNeighbors(n, A, m - 1)
+
+
+def test_generate_neighbors_savepath(native, tmp_path):
+    from piqmc import tools
+    J = lattice(4, True, np.random.default_rng(0))
+    p = str(tmp_path / "nbs.npy")
+    nbs = tools.GenerateNeighbors(16, J, 4, savepath=p)
+    np.testing.assert_array_equal(np.load(p), nbs)
+
+
+def test_bits_spins():
+    from piqmc import tools
+    a = np.array([0., 1., 0., 1., 0., 1., 0., 1., 0., 1.])
+    b = tools.bits2spins(a)
+    assert np.all(b == [1, -1, 1, -1, 1, -1, 1, -1, 1, -1])
+    assert np.all(tools.spins2bits(b) == a)
+
+
+def test_jperp_matches_oracle(native):
+    from piqmc.reforder import jperp_schedule
+    for P, T in [(20, 0.05), (5, 0.01), (32, 1.7), (2, 0.3)]:
+        s = np.linspace(3.0, 1e-8, 57)
+        np.testing.assert_array_equal(jperp_schedule(s, P, T), oracle.jperp(s, P, T))
+    with pytest.raises(ZeroDivisionError):
+        jperp_schedule(np.ones(3), 4, 0.0)
+
+
+def test_libc_peek_does_not_advance_and_skip_does(native):
+    from piqmc.reforder import libc_peek, libc_skip
+    oracle.libc_srand(1234)
+    a = libc_peek(1000)
+    b = oracle.libc_rand(1000)
+    np.testing.assert_array_equal(a, b)
+    oracle.libc_srand(99)
+    peek = libc_peek(50)
+    libc_skip(20)
+    np.testing.assert_array_equal(oracle.libc_rand(30), peek[20:])
+
+
+def _problem(nbs):
+    from piqmc import fast
+    return fast.Problem(nbs, on_device=False)
+
+
+@pytest.mark.parametrize("L,periodic,fields", [(8, True, False), (7, True, True), (6, False, True), (16, True, False)])
+def test_problem_classes_are_independent_sets(native, L, periodic, fields):
+    from piqmc import tools
+    g = np.random.default_rng(L)
+    J = lattice(L, periodic, g, fields=(lambda r: r.normal()) if fields else None)
+    nbs = tools.GenerateNeighbors(L * L, J, 5 if fields else 4)
+    p = _problem(nbs)
+    n = L * L
+    assert sorted(p.perm.tolist()) == sorted(set(p.perm.tolist())) and len(p.perm) == n
+    assert np.all(p.inv[p.perm] == np.arange(n))
+    assert p.nclass <= 32 and p.nclass * p.class_stride == p.nslots
+    cls = p.perm // p.class_stride
+    assert np.all(p.perm % p.class_stride < p.class_size[cls])
+    # independence: no coupling inside a class
+    for (a, b) in J.keys():
+        if a != b:
+            assert cls[a] != cls[b]
+    # SoA tables: every coupling of spin i appears (device slots) with its FP32 value
+    for i in range(n):
+        row = [(int(p.nbr_host[m, p.perm[i]]), float(p.cpl_host[m, p.perm[i]])) for m in range(p.nbr_host.shape[0])
+               if p.cpl_host[m, p.perm[i]] != 0.0]
+        want = [(int(p.perm[int(j)]), float(np.float32(v))) for j, v in nbs[i] if int(j) != i and v != 0.0]
+        assert row == want
+    # FP64 CSR reproduces the classical energy
+    s = np.where(g.random(n) < 0.5, -1.0, 1.0)
+    sd = np.zeros(p.nslots)
+    sd[p.perm] = s
+    E = 0.0
+    for r in range(p.nslots):
+        for e in range(p.csr_ptr[r], p.csr_ptr[r + 1]):
+            c = p.csr_col[e]
+            E += p.csr_val[e] * sd[r] * (1.0 if c == r else sd[c])
+    assert abs(-E - oracle.classical_energy(s, J)) < 1e-10
+
+
+def test_greedy_colouring(native):
+    from piqmc import _native, tools
+    J = lattice(5, True, np.random.default_rng(1))
+    nbs = tools.GenerateNeighbors(25, J, 4)
+    idx = np.ascontiguousarray(np.trunc(nbs[:, :, 0]).astype(np.int32))
+    jv = np.ascontiguousarray(nbs[:, :, 1].astype(np.float32))
+    col = np.empty(25, np.int32)
+    nc = native.pq_color_graph(25, 4, idx.ctypes.data, jv.ctypes.data, col.ctypes.data)
+    assert nc >= 3
+    for (a, b) in J.keys():
+        assert col[a] != col[b]
