@@ -209,6 +209,56 @@ int pq_qa_fast_ex(void* words, const int32_t* nbr, const float* cpl, const float
                   const float* jperp, const float* betas, const pq_fast_params* prm,
                   unsigned long long* accepts, int32_t* status, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Batched persistent packed sweep (new): many instances of uneven size, slice
+ * count and replica count in one launch.  Per-instance tables live in pools
+ * (tab_off indexes nbr_pool/cpl_pool, laid out [maxdeg][n] per instance; the
+ * other offsets index their pools); each item is nrep consecutive replicas of one
+ * instance whose words start at byte word_off of words_pool, and runs on a group
+ * of `gwarps` warps of a CTA using shared memory from byte smem_off of the CTA's
+ * dynamic shared memory (pq_batch_smem_bytes each).  A task = items
+ * [item0, item0 + nitems), all with the same gwarps, nitems * gwarps <= warps of
+ * the CTA.  Persistent CTAs pop tasks from *queue_head (scratch, reset by the
+ * call).  Results equal pq_qa_fast on each instance with key0/key1 as its seed
+ * and replica0 as its replica_base.
+ * ------------------------------------------------------------------------- */
+typedef struct pq_batch_inst {
+    int64_t tab_off;    /* into nbr_pool / cpl_pool */
+    int64_t field_off;  /* into field_pool */
+    int csize_off;      /* into csize_pool (nclass entries) */
+    int jperp_off;      /* into jperp_pool (the instance's whole schedule) */
+    int n, P, maxdeg, nclass, stride;
+    uint32_t key0, key1;
+    int pad_;
+} pq_batch_inst;
+
+typedef struct pq_batch_item {
+    int inst, nrep, replica0, smem_off;
+    int64_t word_off;   /* bytes into words_pool */
+} pq_batch_item;
+
+typedef struct pq_batch_task {
+    int item0, nitems, gwarps, pad_;
+} pq_batch_task;
+
+typedef struct pq_batch_run {
+    int nsched;         /* schedule steps of this call */
+    int sched_base;     /* index of its first step in each instance's J-perp schedule */
+    int mcsteps, global_moves, order_mode;
+    float beta;         /* 1/T (FP32) */
+    int64_t sweep_base; /* sweep counter of the first sweep = sched_base * mcsteps for a split anneal */
+} pq_batch_run;
+
+int pq_batch_anneal(const pq_batch_task* tasks, int ntasks, const pq_batch_item* items,
+                    const pq_batch_inst* insts, const int32_t* nbr_pool, const float* cpl_pool,
+                    const float* field_pool, const int32_t* csize_pool, const float* jperp_pool,
+                    void* words_pool, int* queue_head, const pq_batch_run* run, int grid, int threads,
+                    int smem_bytes, unsigned long long* accepts, int32_t* status, void* stream);
+/* Shared memory one item of nrep replicas of an n-slot, P-slice instance needs. */
+int pq_batch_smem_bytes(int nrep, int n, int P);
+/* Resident CTAs per SM of the batched kernel for a launch shape, and the SM count. */
+int pq_batch_occupancy(int threads, int smem_bytes, int* blocks_per_sm, int* sm_count);
+
 /* FP64 classical energy of every (replica, slice) from a CSR of the coupling
  * matrix (row_ptr int64 [n+1], col int32, val double; diagonal = field),
  * reference piqmc/sa.pyx:25-44: E = -sum_{(i,j) off-diag} J_ij s_i s_j - sum_i J_ii s_i,

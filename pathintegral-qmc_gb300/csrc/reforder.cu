@@ -113,57 +113,89 @@ __device__ __forceinline__ float acc2(float ediff, float s2, float v) {
     return __fadd_rn(ediff, __fmul_rn(s2, v));
 }
 
-template <bool FP64>
-__global__ void qa_sparse_reforder_kernel(int8_t* __restrict__ spins, const int32_t* __restrict__ nb_idx,
-                                          const float* __restrict__ nb_j, int n, int nperm, int maxnb, int P, int R,
-                                          const float* __restrict__ jperp, int nsched, int mcsteps,
-                                          float temp, const int32_t* __restrict__ perms,
-                                          const int32_t* __restrict__ rands, int64_t rand_stride,
-                                          int64_t* __restrict__ rand_used, int flags, ExpPatch ep,
-                                          int32_t* status) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+// One CTA (one warp) per replica; lane 0 walks the replica.  The replica's
+// spins are staged in shared memory when they fit (SMEM), and for MAXNB > 0 the
+// neighbour row is read with all its loads issued before the (ordered) sums.
+template <bool FP64, int MAXNB, bool SMEM>
+__global__ void __launch_bounds__(32) qa_sparse_reforder_kernel(
+    int8_t* __restrict__ spins, const int32_t* __restrict__ nb_idx, const float* __restrict__ nb_j, int n, int nperm,
+    int maxnb, int P, int R, const float* __restrict__ jperp, int nsched, int mcsteps, float temp,
+    const int32_t* __restrict__ perms, const int32_t* __restrict__ rands, int64_t rand_stride,
+    int64_t* __restrict__ rand_used, int flags, ExpPatch ep, int32_t* status) {
+    extern __shared__ __align__(16) int8_t sh_spins[];
+    const int r = blockIdx.x;
     if (r >= R) return;
-    int8_t* s = spins + (int64_t)r * n * P;
-    const int32_t* pr = perms + (int64_t)r * nsched * mcsteps * nperm;
-    RefRng rng{rands + (int64_t)r * rand_stride, rand_stride, 0, false};
-    for (int g = 0; g < nsched; ++g) {
-        const float jpf = jperp[g];
-        for (int step = 0; step < mcsteps; ++step) {
-            const int32_t* perm = pr + (int64_t)(g * mcsteps + step) * nperm;
-            for (int k = 0; k < P; ++k) {
-                // Q1 (reference as shipped): tidx is never assigned, so every
-                // slice couples to slices P-1 and 1 (piqmc/qmc.pyx:115-117).
-                int tl = P - 1, tr = 1;
-                if (flags & PQ_FIX_Q1) { tl = k == 0 ? P - 1 : k - 1; tr = k == P - 1 ? 0 : k + 1; }
-                // Q2 (as shipped): ediff is reset once per slice (piqmc/qmc.pyx:134-135).
-                float ediff = 0.0f;
-                for (int t = 0; t < nperm; ++t) {
-                    const int i = perm[t];
-                    if ((unsigned)i >= (unsigned)n) { pq_set_status(status, PQ_ERR_BAD_INDEX); rand_used[r] = -1; return; }
-                    if (flags & PQ_FIX_Q2) ediff = 0.0f;
-                    int8_t* si_p = s + (int64_t)i * P;
-                    const float s2 = -2.0f * (float)si_p[k];
-                    const int32_t* ni = nb_idx + (int64_t)i * maxnb;
-                    const float* nj = nb_j + (int64_t)i * maxnb;
-                    for (int m = 0; m < maxnb; ++m) {
-                        const int j = ni[m];
-                        const float jv = nj[m];
-                        if (j == i) {
-                            ediff = acc2<FP64>(ediff, s2, jv);
+    int8_t* gs = spins + (int64_t)r * n * P;
+    int8_t* s = SMEM ? sh_spins : gs;
+    if (SMEM) {
+        for (int64_t t = threadIdx.x; t < (int64_t)n * P; t += blockDim.x) sh_spins[t] = gs[t];
+        __syncwarp();
+    }
+    if (threadIdx.x == 0) {
+        const int32_t* pr = perms + (int64_t)r * nsched * mcsteps * nperm;
+        RefRng rng{rands + (int64_t)r * rand_stride, rand_stride, 0, false};
+        bool bad = false;
+        for (int g = 0; g < nsched; ++g) {
+            const float jpf = jperp[g];
+            for (int step = 0; step < mcsteps; ++step) {
+                const int32_t* perm = pr + (int64_t)(g * mcsteps + step) * nperm;
+                for (int k = 0; k < P; ++k) {
+                    // Q1 (reference as shipped): tidx is never assigned, so every
+                    // slice couples to slices P-1 and 1 (piqmc/qmc.pyx:115-117).
+                    int tl = P - 1, tr = 1;
+                    if (flags & PQ_FIX_Q1) { tl = k == 0 ? P - 1 : k - 1; tr = k == P - 1 ? 0 : k + 1; }
+                    // Q2 (as shipped): ediff is reset once per slice (piqmc/qmc.pyx:134-135).
+                    float ediff = 0.0f;
+                    for (int t = 0; t < nperm; ++t) {
+                        int i = perm[t];
+                        if ((unsigned)i >= (unsigned)n) { bad = true; i = 0; }
+                        if (flags & PQ_FIX_Q2) ediff = 0.0f;
+                        int8_t* si_p = s + (int64_t)i * P;
+                        const float s2 = -2.0f * (float)si_p[k];
+                        const int32_t* ni = nb_idx + (int64_t)i * maxnb;
+                        const float* nj = nb_j + (int64_t)i * maxnb;
+                        if constexpr (MAXNB > 0) {
+                            int jj[MAXNB];
+                            float vv[MAXNB];
+                            int8_t sj[MAXNB];
+#pragma unroll
+                            for (int m = 0; m < MAXNB; ++m) { jj[m] = __ldg(ni + m); vv[m] = __ldg(nj + m); }
+#pragma unroll
+                            for (int m = 0; m < MAXNB; ++m) {
+                                if ((unsigned)jj[m] >= (unsigned)n) { bad = true; jj[m] = i; }
+                                sj[m] = s[(int64_t)jj[m] * P + k];
+                            }
+#pragma unroll
+                            for (int m = 0; m < MAXNB; ++m)
+                                ediff = acc2<FP64>(ediff, s2, jj[m] == i ? vv[m] : (sj[m] > 0 ? vv[m] : -vv[m]));
                         } else {
-                            if ((unsigned)j >= (unsigned)n) { pq_set_status(status, PQ_ERR_BAD_INDEX); rand_used[r] = -1; return; }
-                            ediff = acc2<FP64>(ediff, s2, s[(int64_t)j * P + k] > 0 ? jv : -jv);
+                            for (int m = 0; m < maxnb; ++m) {
+                                int j = ni[m];
+                                const float jv = nj[m];
+                                if (j == i) {
+                                    ediff = acc2<FP64>(ediff, s2, jv);
+                                } else {
+                                    if ((unsigned)j >= (unsigned)n) { bad = true; j = i; }
+                                    ediff = acc2<FP64>(ediff, s2, s[(int64_t)j * P + k] > 0 ? jv : -jv);
+                                }
+                            }
                         }
+                        ediff = acc2<FP64>(ediff, s2, si_p[tl] > 0 ? jpf : -jpf);
+                        ediff = acc2<FP64>(ediff, s2, si_p[tr] > 0 ? jpf : -jpf);
+                        if (ref_accept(ediff, temp, false, rng, ep, status)) si_p[k] = (int8_t)-si_p[k];
+                        if (rng.dead) goto done;
                     }
-                    ediff = acc2<FP64>(ediff, s2, si_p[tl] > 0 ? jpf : -jpf);
-                    ediff = acc2<FP64>(ediff, s2, si_p[tr] > 0 ? jpf : -jpf);
-                    if (ref_accept(ediff, temp, false, rng, ep, status)) si_p[k] = (int8_t)-si_p[k];
-                    if (rng.dead) { rand_used[r] = -1; return; }
                 }
             }
         }
+    done:
+        if (bad) pq_set_status(status, PQ_ERR_BAD_INDEX);
+        rand_used[r] = (rng.dead || bad) ? -1 : rng.used;
     }
-    rand_used[r] = rng.used;
+    if (SMEM) {
+        __syncwarp();
+        for (int64_t t = threadIdx.x; t < (int64_t)n * P; t += blockDim.x) gs[t] = sh_spins[t];
+    }
 }
 
 __global__ void qa_dense_reforder_kernel(int8_t* __restrict__ spins, const double* __restrict__ J, int n,
@@ -263,6 +295,8 @@ __global__ void exp_range_probe_kernel(uint32_t first_bits, int64_t count, doubl
     if (i < count) y[i] = exp((double)__uint_as_float(first_bits + (uint32_t)i));
 }
 
+constexpr size_t kRefSmemMax = 200 * 1024;
+
 ExpPatch make_patch(const uint32_t* ov_x, const double* ov_y, int ov_n, uint32_t* close_x,
                     double* close_y, int close_cap, int* close_cnt) {
     ExpPatch ep;
@@ -270,6 +304,60 @@ ExpPatch make_patch(const uint32_t* ov_x, const double* ov_y, int ov_n, uint32_t
     ep.close_x = close_x; ep.close_y = close_y; ep.close_cnt = close_x && close_y ? close_cnt : nullptr;
     ep.close_cap = close_cap;
     return ep;
+}
+
+template <bool FP64, int MAXNB, bool SMEM>
+int launch_qa_sparse_t(int8_t* spins, const int32_t* nb_idx, const float* nb_j, int n, int nperm, int maxnb, int P,
+                       int R, const float* jperp, int nsched, int mcsteps, float temp, const int32_t* perms,
+                       const int32_t* rands, int64_t rand_stride, int64_t* rand_used, int flags, const ExpPatch& ep,
+                       int32_t* status, cudaStream_t stream) {
+    const size_t smem = SMEM ? (size_t)n * P : 0;
+    if (SMEM) {
+        PQ_CUDA_TRY(cudaFuncSetAttribute(qa_sparse_reforder_kernel<FP64, MAXNB, SMEM>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    }
+    qa_sparse_reforder_kernel<FP64, MAXNB, SMEM><<<R, 32, smem, stream>>>(
+        spins, nb_idx, nb_j, n, nperm, maxnb, P, R, jperp, nsched, mcsteps, temp, perms, rands, rand_stride, rand_used,
+        flags, ep, status);
+    return pq_launch_status();
+}
+
+template <bool FP64, int MAXNB>
+int launch_qa_sparse_s(int8_t* spins, const int32_t* nb_idx, const float* nb_j, int n, int nperm, int maxnb, int P,
+                       int R, const float* jperp, int nsched, int mcsteps, float temp, const int32_t* perms,
+                       const int32_t* rands, int64_t rand_stride, int64_t* rand_used, int flags, const ExpPatch& ep,
+                       int32_t* status, cudaStream_t stream) {
+    if ((size_t)n * P <= kRefSmemMax)
+        return launch_qa_sparse_t<FP64, MAXNB, true>(spins, nb_idx, nb_j, n, nperm, maxnb, P, R, jperp, nsched, mcsteps,
+                                                      temp, perms, rands, rand_stride, rand_used, flags, ep, status, stream);
+    return launch_qa_sparse_t<FP64, MAXNB, false>(spins, nb_idx, nb_j, n, nperm, maxnb, P, R, jperp, nsched, mcsteps,
+                                                   temp, perms, rands, rand_stride, rand_used, flags, ep, status, stream);
+}
+
+template <bool FP64>
+int launch_qa_sparse_f(int8_t* spins, const int32_t* nb_idx, const float* nb_j, int n, int nperm, int maxnb, int P,
+                       int R, const float* jperp, int nsched, int mcsteps, float temp, const int32_t* perms,
+                       const int32_t* rands, int64_t rand_stride, int64_t* rand_used, int flags, const ExpPatch& ep,
+                       int32_t* status, cudaStream_t stream) {
+    if (maxnb == 4)
+        return launch_qa_sparse_s<FP64, 4>(spins, nb_idx, nb_j, n, nperm, maxnb, P, R, jperp, nsched, mcsteps, temp,
+                                           perms, rands, rand_stride, rand_used, flags, ep, status, stream);
+    if (maxnb == 5)
+        return launch_qa_sparse_s<FP64, 5>(spins, nb_idx, nb_j, n, nperm, maxnb, P, R, jperp, nsched, mcsteps, temp,
+                                           perms, rands, rand_stride, rand_used, flags, ep, status, stream);
+    return launch_qa_sparse_s<FP64, 0>(spins, nb_idx, nb_j, n, nperm, maxnb, P, R, jperp, nsched, mcsteps, temp,
+                                       perms, rands, rand_stride, rand_used, flags, ep, status, stream);
+}
+
+int launch_qa_sparse(int8_t* spins, const int32_t* nb_idx, const float* nb_j, int n, int nperm, int maxnb, int P, int R,
+                     const float* jperp, int nsched, int mcsteps, float temp, const int32_t* perms,
+                     const int32_t* rands, int64_t rand_stride, int64_t* rand_used, int flags, const ExpPatch& ep,
+                     int32_t* status, cudaStream_t stream) {
+    if (flags & PQ_ACC_FP64)
+        return launch_qa_sparse_f<true>(spins, nb_idx, nb_j, n, nperm, maxnb, P, R, jperp, nsched, mcsteps, temp, perms,
+                                        rands, rand_stride, rand_used, flags, ep, status, stream);
+    return launch_qa_sparse_f<false>(spins, nb_idx, nb_j, n, nperm, maxnb, P, R, jperp, nsched, mcsteps, temp, perms,
+                                     rands, rand_stride, rand_used, flags, ep, status, stream);
 }
 
 constexpr int kRefThreads = 32;
@@ -299,16 +387,8 @@ int pq_qa_sparse_reforder_ex(int8_t* spins, const int32_t* nb_idx, const float* 
         return PQ_ERR_INVALID_ARG;
     if (R == 0) return PQ_OK;
     ExpPatch ep = make_patch(ov_x, ov_y, ov_n, close_x, close_y, close_cap, close_cnt);
-    const dim3 grid((R + kRefThreads - 1) / kRefThreads), block(kRefThreads);
-    if (flags & PQ_ACC_FP64)
-        qa_sparse_reforder_kernel<true><<<grid, block, 0, (cudaStream_t)stream>>>(
-            spins, nb_idx, nb_j, n, nperm, maxnb, P, R, jperp, nsched, mcsteps, temp, perms, rands, rand_stride,
-            rand_used, flags, ep, status);
-    else
-        qa_sparse_reforder_kernel<false><<<grid, block, 0, (cudaStream_t)stream>>>(
-            spins, nb_idx, nb_j, n, nperm, maxnb, P, R, jperp, nsched, mcsteps, temp, perms, rands, rand_stride,
-            rand_used, flags, ep, status);
-    return pq_launch_status();
+    return launch_qa_sparse(spins, nb_idx, nb_j, n, nperm, maxnb, P, R, jperp, nsched, mcsteps, temp, perms, rands,
+                            rand_stride, rand_used, flags, ep, status, (cudaStream_t)stream);
 }
 
 int pq_qa_sparse_reforder(int8_t* spins, const int32_t* nb_idx, const float* nb_j, int n, int nperm,

@@ -1,0 +1,360 @@
+// The packed sweep of one work item (a few replicas of one instance), run by a
+// group of warps that synchronises on its own barrier.  Shared by the
+// single-instance kernel (fast.cu: one group = the whole CTA) and the
+// persistent batched kernel (batch.cu: several groups per CTA).
+//
+// Physics: qmc.QuantumAnneal (reference piqmc/qmc.pyx:30-136) with its two
+// quirks corrected -- the energy difference is recomputed for every spin, and
+// slice k couples to slices k-1 and k+1 (periodic).  Acceptance follows the
+// reference's convention: flip when ediff > 0, else when u < exp(ediff / T),
+// with J-perp = -(P T / 2) ln tanh(G / (P T)).
+//
+// Order of one local sweep: the M update classes (independent sets) are
+// visited in a per-(replica, sweep) random order (or 0..M-1); within a class
+// every spin updates all slices of one slice class at once, then all slices of
+// the other.  Spins of one class share no coupling and slices of one slice
+// class are not Trotter neighbours, so the updates of a phase are independent
+// and the sweep equals a sequential sweep in a definite order.  Slice classes:
+// P even -> {even k}, {odd k}; P odd -> {even k < P-1}, {odd k}, {P-1};
+// P = 1 -> {0} (no Trotter term).  For P even the random order also picks,
+// per class, which slice class goes first.
+//
+// Arithmetic of one update (spin i of replica r, slice k), every op one IEEE
+// FP32 rounding, in this order:
+//   e = s_i h_i;  e += J_im s_i s_jm for m = 0..maxdeg-1 (table order);
+//   t = (J-perp s_i s_{k-1}) + (J-perp s_i s_{k+1})      (exact);
+//   ediff = -2 (e + t);  flip if ediff > 0 or u < expf_neg(ediff * beta),
+// u = (r >> 9) * 2^-23.  Uniforms: Philox4x32-10, key = seed.  Local update:
+// counter = (device slot i, sweep, replica, q << 16 | m >> 2), word m & 3 for
+// the m-th slice of class q.  World-line move: counter = (i, last sweep of the
+// step, replica, 1 << 24 | gm << 16 | class), word 0.  Class order of a sweep:
+// counter = (0xFFFFFFFF, sweep, replica, 2 << 24 | b); words w[0..] of blocks
+// b = 0,1,..; Fisher-Yates for j = M-1..1 swaps order[j] with
+// order[(w[M-1-j] * (j+1)) >> 32]; w[M-1] bit p = which slice class goes first
+// for the p-th visited class.
+#pragma once
+#include "common.cuh"
+
+namespace pq {
+
+constexpr int kMaxClasses = PQ_MAX_CLASSES;
+
+// Everything one work item needs; the tables are the instance's.
+struct Item {
+    const int32_t* nbr;       // [maxdeg][n] device slots
+    const float* cpl;         // [maxdeg][n]
+    const float* field;       // [n]
+    const int32_t* csize;     // [nclass] class sizes (global or shared memory)
+    const float* jperp;       // [nsched]
+    const float* betas;       // [nsched] or null (then beta)
+    void* words;              // [nrep][n] world-lines (uint32 or uint64)
+    int n, P, maxdeg, nclass, stride, order_mode;
+    int nrep;
+    uint32_t replica0;        // RNG replica id of the first replica
+    uint32_t key0, key1;
+    int64_t sweep_base;
+    int nsched, mcsteps, global_moves;
+    float beta;
+};
+
+// A set of warps of one CTA working on one item.
+struct Group {
+    int tid;    // thread index within the group
+    int nthr;   // threads in the group (a multiple of 32)
+    int bar;    // named barrier id; 0 = __syncthreads (the group is the whole CTA)
+};
+
+__device__ __forceinline__ void group_sync(const Group& g) {
+    if (g.bar == 0) __syncthreads();
+    else asm volatile("bar.sync %0, %1;" ::"r"(g.bar), "r"(g.nthr) : "memory");
+}
+
+template <typename W>
+__device__ __forceinline__ uint32_t bit_to_sign(W d, int k) {
+    return (uint32_t)(d >> k) << 31;
+}
+
+template <typename W>
+__device__ __forceinline__ W full_mask(int P) {
+    return P >= (int)(8 * sizeof(W)) ? ~(W)0 : (((W)1 << P) - 1);
+}
+
+// Bits k of the result: s^k xor s^{k-1} (left) and s^k xor s^{k+1} (right), periodic in P.
+template <typename W>
+__device__ __forceinline__ void trotter_diffs(W w, int P, W mask, W& dl, W& dr) {
+    const W up = ((w << 1) | (w >> (P - 1))) & mask;   // bit k = s^{k-1}
+    const W dn = ((w >> 1) | (w << (P - 1))) & mask;   // bit k = s^{k+1}
+    dl = w ^ up;
+    dr = w ^ dn;
+}
+
+__device__ __forceinline__ float flip_sign(float v, uint32_t signbit) {
+    return __uint_as_float(__float_as_uint(v) ^ signbit);
+}
+
+__device__ __forceinline__ int slice_count(int P, int q) {
+    if (P == 1) return 1;
+    if ((P & 1) == 0) return P >> 1;
+    return q == 2 ? 1 : (P - 1) >> 1;
+}
+
+__device__ __forceinline__ int slice_of(int P, int q, int m) { return q == 2 ? P - 1 : 2 * m + q; }
+
+// Class visiting order of one (replica, sweep) and the slice-class parity word.
+__device__ inline void class_order(int M, int order_mode, uint32_t key0, uint32_t key1, uint32_t sweep,
+                                   uint32_t replica, uint8_t* order, uint32_t* parity) {
+    for (int c = 0; c < M; ++c) order[c] = (uint8_t)c;
+    if (order_mode == 0) { *parity = 0; return; }
+    uint32_t w[4] = {0, 0, 0, 0};
+    int used = 4, blk = 0;
+    for (int j = M - 1; j >= 0; --j) {
+        if (used == 4) {
+            const pq_u32x4 r = pq_philox(pq_u32x4{0xFFFFFFFFu, sweep, replica, (2u << 24) | (uint32_t)blk++}, key0, key1);
+            w[0] = r.x; w[1] = r.y; w[2] = r.z; w[3] = r.w;
+            used = 0;
+        }
+        const uint32_t x = w[used++];
+        if (j == 0) { *parity = x; break; }
+        const uint32_t k = (uint32_t)(((uint64_t)x * (uint32_t)(j + 1)) >> 32);
+        const uint8_t t = order[j]; order[j] = order[k]; order[k] = t;
+    }
+}
+
+template <typename W, int MAXDEG>
+__device__ __forceinline__ void load_site(const W* rw, int i, int n, int maxdeg, const int32_t* __restrict__ nbr,
+                                          const float* __restrict__ cpl, W wi, W (&d)[MAXDEG], float (&J)[MAXDEG],
+                                          bool& bad) {
+#pragma unroll
+    for (int m = 0; m < MAXDEG; ++m) {
+        if (m < maxdeg) {
+            int j = __ldg(nbr + (int64_t)m * n + i);
+            if ((unsigned)j >= (unsigned)n) { bad = true; j = i; }
+            J[m] = __ldg(cpl + (int64_t)m * n + i);
+            d[m] = wi ^ rw[j];
+        } else {
+            J[m] = 0.0f;
+            d[m] = 0;
+        }
+    }
+}
+
+// Metropolis decision for sum = e + t (ediff = -2 sum): flip when sum < 0, else
+// when u < expf_neg(fl(sum * m2beta)) with m2beta = -2 beta.  The hardware 2^x
+// (argument fl(sum * m2blog2e), m2blog2e = fl(-2 beta log2 e)) settles it outside
+// a 1e-4 relative guard band -- its error against expf_neg is below 2e-5 for every
+// argument above -87 -- and expf_neg itself settles the rest, so the result is
+// exactly the specification's.
+__device__ __forceinline__ bool decide(float sum, float u, float m2beta, float m2blog2e) {
+    if (sum < 0.0f) return true;
+    const float pf = pq_ex2_approx(__fmul_rn(sum, m2blog2e));
+    if (u > __fmul_rn(pf, 1.0001f)) return false;
+    if (u < __fmul_rn(pf, 0.9999f) && pf > 1e-30f) return true;
+    return u < pq_expf_neg(__fmul_rn(sum, m2beta));
+}
+
+// One spin's local update over the slices of slice class q, P = 2 * NQ <= 32
+// slices fixed at compile time, DEG couplings.  Same arithmetic and uniforms as
+// the generic path.
+template <int NQ, int DEG>
+__device__ __forceinline__ uint32_t update_fixed(uint32_t wi, const uint32_t (&d)[DEG], const float (&J)[DEG], float h,
+                                                 float jp, int q, uint32_t i, uint32_t sweep, uint32_t rep, uint32_t key0,
+                                                 uint32_t key1, float m2beta, float m2blog2e) {
+    constexpr int P = 2 * NQ;
+    constexpr uint32_t MASK = P >= 32 ? 0xffffffffu : ((1u << P) - 1u);
+    const uint32_t up = ((wi << 1) | (wi >> (P - 1))) & MASK;
+    const uint32_t dn = ((wi >> 1) | (wi << (P - 1))) & MASK;
+    const uint32_t wq = wi >> q, dl = (wi ^ up) >> q, dr = (wi ^ dn) >> q;
+    uint32_t dq[DEG];
+#pragma unroll
+    for (int m = 0; m < DEG; ++m) dq[m] = d[m] >> q;
+    uint32_t flips = 0;
+#pragma unroll
+    for (int blk = 0; blk < (NQ + 3) / 4; ++blk) {
+        const pq_u32x4 rnd = pq_philox(pq_u32x4{i, sweep, rep, (uint32_t)((q << 16) | blk)}, key0, key1);
+        const uint32_t rw4[4] = {rnd.x, rnd.y, rnd.z, rnd.w};
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+            const int mm = blk * 4 + jj;
+            if (mm < NQ) {
+                const int sh = 31 - 2 * mm;  // bit 2*mm of the q-shifted words -> sign bit
+                float e = flip_sign(h, (wq << sh) & 0x80000000u);
+#pragma unroll
+                for (int m = 0; m < DEG; ++m) e = __fadd_rn(e, flip_sign(J[m], (dq[m] << sh) & 0x80000000u));
+                const float t = __fadd_rn(flip_sign(jp, (dl << sh) & 0x80000000u), flip_sign(jp, (dr << sh) & 0x80000000u));
+                const float sum = __fadd_rn(e, t);
+                if (decide(sum, pq_u01(rw4[jj]), m2beta, m2blog2e)) flips |= 1u << (2 * mm);
+            }
+        }
+    }
+    return flips << q;
+}
+
+// Anneal one item through its schedule.  sw: shared memory holding the item's
+// nrep x n words (staged by the caller); order: nrep x kMaxClasses bytes;
+// parity: nrep words.  Counts accepted local flips into nacc and out-of-range
+// indices into bad.
+template <typename W, int MAXDEG, int NQC>
+__device__ void run_item(const Item& it, W* sw, uint8_t* order, uint32_t* parity, const Group& g, bool& bad,
+                         unsigned long long& nacc) {
+    const int n = it.n, P = it.P, S = it.stride, nrep = it.nrep;
+    const W mask = full_mask<W>(P);
+    const int nclass_q = P == 1 ? 1 : ((P & 1) ? 3 : 2);
+    for (int gs = 0; gs < it.nsched; ++gs) {
+        const float jp = P == 1 ? 0.0f : __ldg(it.jperp + gs);
+        const float beta = it.betas ? __ldg(it.betas + gs) : it.beta;
+        const float m2beta = __fmul_rn(-2.0f, beta);                          // exact
+        const float m2blog2e = __fmul_rn(m2beta, 1.44269502162933349609375f);  // guard-band argument scale
+        for (int step = 0; step < it.mcsteps; ++step) {
+            const uint32_t sweep = (uint32_t)(it.sweep_base + (int64_t)gs * it.mcsteps + step);
+            if (g.tid < nrep)
+                class_order(it.nclass, it.order_mode, it.key0, it.key1, sweep, it.replica0 + g.tid,
+                            order + g.tid * kMaxClasses, parity + g.tid);
+            group_sync(g);
+            for (int p = 0; p < it.nclass; ++p) {
+                for (int qq = 0; qq < nclass_q; ++qq) {
+                    int rl = 0, s = g.tid;
+                    while (s >= S) { s -= S; ++rl; }
+                    for (; rl < nrep;) {
+                        const int cls = order[rl * kMaxClasses + p];
+                        const int q = nclass_q == 2 ? (qq ^ (int)((parity[rl] >> p) & 1u)) : qq;
+                        if (s < it.csize[cls]) {
+                            const int i = cls * S + s;
+                            W* rw = sw + rl * n;
+                            const W wi = rw[i];
+                            W d[MAXDEG];
+                            float J[MAXDEG];
+                            load_site<W, MAXDEG>(rw, i, n, it.maxdeg, it.nbr, it.cpl, wi, d, J, bad);
+                            const float h = __ldg(it.field + i);
+                            const uint32_t rep = it.replica0 + rl;
+                            if constexpr (NQC > 0) {
+                                const uint32_t fl = update_fixed<NQC, MAXDEG>(
+                                    (uint32_t)wi, reinterpret_cast<const uint32_t(&)[MAXDEG]>(d), J, h, jp, q,
+                                    (uint32_t)i, sweep, rep, it.key0, it.key1, m2beta, m2blog2e);
+                                rw[i] = wi ^ (W)fl;
+                                nacc += __popc(fl);
+                            } else {
+                                W dl, dr;
+                                trotter_diffs<W>(wi, P, mask, dl, dr);
+                                W flips = 0;
+                                const int nq = slice_count(P, q);
+                                for (int mb = 0; mb * 4 < nq; ++mb) {
+                                    const pq_u32x4 rnd = pq_philox(
+                                        pq_u32x4{(uint32_t)i, sweep, rep, (uint32_t)((q << 16) | mb)}, it.key0, it.key1);
+                                    const uint32_t rw4[4] = {rnd.x, rnd.y, rnd.z, rnd.w};
+#pragma unroll
+                                    for (int jj = 0; jj < 4; ++jj) {
+                                        const int mm = mb * 4 + jj;
+                                        if (mm < nq) {
+                                            const int k = slice_of(P, q, mm);
+                                            float e = flip_sign(h, bit_to_sign<W>(wi, k));
+#pragma unroll
+                                            for (int m = 0; m < MAXDEG; ++m)
+                                                if (m < it.maxdeg) e = __fadd_rn(e, flip_sign(J[m], bit_to_sign<W>(d[m], k)));
+                                            const float t = __fadd_rn(flip_sign(jp, bit_to_sign<W>(dl, k)),
+                                                                      flip_sign(jp, bit_to_sign<W>(dr, k)));
+                                            const bool acc = decide(__fadd_rn(e, t), pq_u01(rw4[jj]), m2beta, m2blog2e);
+                                            flips |= (W)acc << k;
+                                            nacc += acc;
+                                        }
+                                    }
+                                }
+                                rw[i] = wi ^ flips;
+                            }
+                        }
+                        s += g.nthr;
+                        while (s >= S) { s -= S; ++rl; }
+                    }
+                    group_sync(g);
+                }
+            }
+        }
+        // world-line moves: flip spin i in every slice at once, classes in order
+        for (int gm = 0; gm < it.global_moves; ++gm) {
+            const uint32_t sweep = (uint32_t)(it.sweep_base + (int64_t)gs * it.mcsteps + it.mcsteps - 1);
+            for (int cls = 0; cls < it.nclass; ++cls) {
+                const int csz = it.csize[cls];
+                int rl = 0, s = g.tid;
+                while (s >= S) { s -= S; ++rl; }
+                for (; rl < nrep;) {
+                    if (s < csz) {
+                        const int i = cls * S + s;
+                        W* rw = sw + rl * n;
+                        const W wi = rw[i];
+                        W d[MAXDEG];
+                        float J[MAXDEG];
+                        load_site<W, MAXDEG>(rw, i, n, it.maxdeg, it.nbr, it.cpl, wi, d, J, bad);
+                        const float h = __ldg(it.field + i);
+                        float E = 0.0f;
+                        for (int k = 0; k < P; ++k) {
+                            float e = flip_sign(h, bit_to_sign<W>(wi, k));
+#pragma unroll
+                            for (int m = 0; m < MAXDEG; ++m)
+                                if (m < it.maxdeg) e = __fadd_rn(e, flip_sign(J[m], bit_to_sign<W>(d[m], k)));
+                            E = __fadd_rn(E, e);
+                        }
+                        const pq_u32x4 rnd = pq_philox(
+                            pq_u32x4{(uint32_t)i, sweep, it.replica0 + rl,
+                                     (uint32_t)((1u << 24) | ((uint32_t)gm << 16) | (uint32_t)cls)},
+                            it.key0, it.key1);
+                        if (decide(E, pq_u01(rnd.x), m2beta, m2blog2e)) rw[i] = wi ^ mask;
+                    }
+                    s += g.nthr;
+                    while (s >= S) { s -= S; ++rl; }
+                }
+                group_sync(g);
+            }
+        }
+    }
+}
+
+// Stage an item's words into shared memory / write them back (group-strided).
+template <typename W>
+__device__ __forceinline__ void stage_in(const Item& it, W* sw, const Group& g) {
+    const W* src = reinterpret_cast<const W*>(it.words);
+    for (int t = g.tid; t < it.nrep * it.n; t += g.nthr) sw[t] = src[t];
+    group_sync(g);
+}
+
+template <typename W>
+__device__ __forceinline__ void stage_out(const Item& it, const W* sw, const Group& g) {
+    W* dst = reinterpret_cast<W*>(it.words);
+    group_sync(g);
+    for (int t = g.tid; t < it.nrep * it.n; t += g.nthr) dst[t] = sw[t];
+}
+
+// Word type / degree / compile-time P dispatch of one item.
+__device__ inline void run_item_any(const Item& it, unsigned char* smem, const Group& g, bool& bad,
+                                    unsigned long long& nacc) {
+    // layout of the item's shared memory: words, then order bytes, then parity words
+    const size_t wbytes = it.P <= 32 ? 4 : 8;
+    const size_t words_bytes = ((size_t)it.nrep * it.n * wbytes + 15) & ~(size_t)15;
+    uint8_t* order = smem + words_bytes;
+    uint32_t* parity = reinterpret_cast<uint32_t*>(order + (((size_t)it.nrep * kMaxClasses + 15) & ~(size_t)15));
+    if (it.P <= 32) {
+        uint32_t* sw = reinterpret_cast<uint32_t*>(smem);
+        stage_in<uint32_t>(it, sw, g);
+        if (it.maxdeg == 4 && it.P == 20) run_item<uint32_t, 4, 10>(it, sw, order, parity, g, bad, nacc);
+        else if (it.maxdeg == 4 && it.P == 16) run_item<uint32_t, 4, 8>(it, sw, order, parity, g, bad, nacc);
+        else if (it.maxdeg == 4 && it.P == 32) run_item<uint32_t, 4, 16>(it, sw, order, parity, g, bad, nacc);
+        else if (it.maxdeg <= 4) run_item<uint32_t, 4, 0>(it, sw, order, parity, g, bad, nacc);
+        else if (it.maxdeg <= 8) run_item<uint32_t, 8, 0>(it, sw, order, parity, g, bad, nacc);
+        else run_item<uint32_t, 16, 0>(it, sw, order, parity, g, bad, nacc);
+        stage_out<uint32_t>(it, sw, g);
+    } else {
+        uint64_t* sw = reinterpret_cast<uint64_t*>(smem);
+        stage_in<uint64_t>(it, sw, g);
+        if (it.maxdeg <= 4) run_item<uint64_t, 4, 0>(it, sw, order, parity, g, bad, nacc);
+        else if (it.maxdeg <= 8) run_item<uint64_t, 8, 0>(it, sw, order, parity, g, bad, nacc);
+        else run_item<uint64_t, 16, 0>(it, sw, order, parity, g, bad, nacc);
+        stage_out<uint64_t>(it, sw, g);
+    }
+}
+
+// Shared memory one item needs (words + order bytes + parity words), 16-byte aligned.
+__host__ __device__ inline size_t item_smem_bytes(int nrep, int n, int P) {
+    const size_t wbytes = P <= 32 ? 4 : 8;
+    return (((size_t)nrep * n * wbytes + 15) & ~(size_t)15) + (((size_t)nrep * kMaxClasses + 15) & ~(size_t)15) +
+           (((size_t)nrep * 4 + 15) & ~(size_t)15);
+}
+
+}  // namespace pq

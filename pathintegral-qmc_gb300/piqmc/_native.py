@@ -47,6 +47,13 @@ class FastParams(ctypes.Structure):
     ]
 
 
+class BatchRun(ctypes.Structure):
+    """Mirror of ``pq_batch_run``."""
+    _fields_ = [("nsched", ctypes.c_int), ("sched_base", ctypes.c_int), ("mcsteps", ctypes.c_int),
+                ("global_moves", ctypes.c_int), ("order_mode", ctypes.c_int), ("beta", ctypes.c_float),
+                ("sweep_base", ctypes.c_int64)]
+
+
 _V, _I32, _I64, _U32, _F32, _U64 = (ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_uint32,
                                      ctypes.c_float, ctypes.c_uint64)
 
@@ -79,6 +86,9 @@ SIGNATURES = {
     "pq_qa_fast_ex": (_I32, [_V, _V, _V, _V, _V, _V, ctypes.POINTER(FastParams), _V, _V, _V]),
     "pq_guard_band_probe": (_I32, [_U32, _I64, _V, _V]),
     "pq_fp32_fma_probe": (_I32, [_V, _I32, _I32, _I32, _V]),
+    "pq_batch_anneal": (_I32, [_V, _I32, _V, _V, _V, _V, _V, _V, _V, _V, _V, _V, _I32, _I32, _I32, _V, _V, _V]),
+    "pq_batch_smem_bytes": (_I32, [_I32, _I32, _I32]),
+    "pq_batch_occupancy": (_I32, [_I32, _I32, _V, _V]),
     "pq_energy_packed": (_I32, [_V, _I32, _I32, _I32, _I32, _V, _V, _V, _V, _V]),
     "pq_pack_spins": (_I32, [_V, _I32, _I32, _I32, _V, _V, _I32, _I32, _V]),
     "pq_unpack_spins": (_I32, [_V, _I32, _I32, _I32, _I32, _V, _I32, _V, _V]),
