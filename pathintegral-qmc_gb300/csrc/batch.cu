@@ -39,7 +39,7 @@ __device__ __forceinline__ void run_task_item(const pq_batch_item& bi, const pq_
     run_item_any(it, smem + bi.smem_off, g, bad, nacc);
 }
 
-__global__ void __launch_bounds__(256) batch_kernel(const pq_batch_task* __restrict__ tasks, int ntasks,
+__global__ void __launch_bounds__(256, 3) batch_kernel(const pq_batch_task* __restrict__ tasks, int ntasks,
                                                     const pq_batch_item* __restrict__ items,
                                                     const pq_batch_inst* __restrict__ insts, const int32_t* nbr_pool,
                                                     const float* cpl_pool, const float* field_pool,
@@ -103,6 +103,7 @@ int pq_batch_anneal(const pq_batch_task* tasks, int ntasks, const pq_batch_item*
     if (ntasks == 0 || run->nsched == 0) return PQ_OK;
     if (!tasks || !items || !insts || !field_pool || !csize_pool || !jperp_pool || !words_pool || !queue_head)
         return PQ_ERR_INVALID_ARG;
+    // instances are checked on the host (maxdeg <= 8: the batched kernel carries no wider variant)
     if (run->order_mode != 0 && run->order_mode != 1) return PQ_ERR_INVALID_ARG;
     static bool attr = false;
     if (!attr) {

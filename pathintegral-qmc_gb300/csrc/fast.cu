@@ -132,12 +132,14 @@ template <typename W>
 int dispatch_deg(void* words, const int32_t* nbr, const float* cpl, const float* field, const float* jperp,
                  const float* betas, const FastArgs& a, int threads, unsigned long long* accepts,
                  int32_t* status, cudaStream_t stream) {
-    if constexpr (sizeof(W) == 4) {
-        // compile-time slice counts for the common even P with exactly four couplings
-        if (a.maxdeg == 4) {
+    // compile-time slice counts for the common even P with exactly four couplings
+    if (a.maxdeg == 4) {
+        if constexpr (sizeof(W) == 4) {
             if (a.P == 20) return launch_fast<W, 4, 10>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status, stream);
             if (a.P == 16) return launch_fast<W, 4, 8>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status, stream);
             if (a.P == 32) return launch_fast<W, 4, 16>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status, stream);
+        } else {
+            if (a.P == 64) return launch_fast<W, 4, 32>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status, stream);
         }
     }
     if (a.maxdeg <= 4)
@@ -230,20 +232,23 @@ int pq_qa_fast_ex(void* words, const int32_t* nbr, const float* cpl, const float
     int threads = p.threads > 0 ? p.threads : 0;
     int rpc = p.replicas_per_cta;
     if (rpc <= 0) {
-        // enough replicas per CTA to give every thread work, within the smem budget
-        const int tgt = threads > 0 ? threads : 128;
-        rpc = (tgt + p.class_stride - 1) / p.class_stride;
+        // enough replicas per CTA for 128 items per phase, within the smem budget
+        rpc = (128 + p.class_stride - 1) / p.class_stride;
         if (rpc < 1) rpc = 1;
-        const size_t cap = kSmemBudget / 2 / ((size_t)p.n * wbytes);
+        const size_t cap = kSmemBudget / 2 / item_smem_bytes(1, p.n, p.P);
         if ((size_t)rpc > cap) rpc = cap < 1 ? 1 : (int)cap;
     }
     if (rpc > kMaxRpc) rpc = kMaxRpc;
     if (threads <= 0) {
+        // the largest of 128, 96, 64, 32 that divides the items of a phase; else round up
         const int items = rpc * p.class_stride;
-        threads = items >= 256 ? 256 : ((items + 31) / 32) * 32;
+        threads = 0;
+        for (int t = 128; t >= 32 && !threads; t -= 32)
+            if (items >= t && items % t == 0) threads = t;
+        if (!threads) threads = items >= 128 ? 128 : ((items + 31) / 32) * 32;
     }
     if (threads % 32 || threads > 512 || threads < rpc) return PQ_ERR_INVALID_ARG;
-    if ((size_t)rpc * p.n * wbytes > kSmemBudget) return PQ_ERR_TOO_LARGE;
+    if (item_smem_bytes(rpc, p.n, p.P) > kSmemBudget) return PQ_ERR_TOO_LARGE;
     a.rpc = rpc;
     cudaStream_t st = (cudaStream_t)stream;
     if (wbytes == 4) return dispatch_deg<uint32_t>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status, st);

@@ -152,31 +152,24 @@ __device__ __forceinline__ bool decide(float sum, float u, float m2beta, float m
     return u < pq_expf_neg(__fmul_rn(sum, m2beta));
 }
 
-// One spin's local update over the slices of slice class q, P = 2 * NQ <= 32
-// slices fixed at compile time, DEG couplings.  Same arithmetic and uniforms as
-// the generic path.
-template <int NQ, int DEG>
-__device__ __forceinline__ uint32_t update_fixed(uint32_t wi, const uint32_t (&d)[DEG], const float (&J)[DEG], float h,
-                                                 float jp, int q, uint32_t i, uint32_t sweep, uint32_t rep, uint32_t key0,
-                                                 uint32_t key1, float m2beta, float m2blog2e) {
-    constexpr int P = 2 * NQ;
-    constexpr uint32_t MASK = P >= 32 ? 0xffffffffu : ((1u << P) - 1u);
-    const uint32_t up = ((wi << 1) | (wi >> (P - 1))) & MASK;
-    const uint32_t dn = ((wi >> 1) | (wi << (P - 1))) & MASK;
-    const uint32_t wq = wi >> q, dl = (wi ^ up) >> q, dr = (wi ^ dn) >> q;
-    uint32_t dq[DEG];
-#pragma unroll
-    for (int m = 0; m < DEG; ++m) dq[m] = d[m] >> q;
+// Core of the compile-time path: NQH slices m = 0..NQH-1 whose bits sit at
+// positions 2m of the 32-bit (q-shifted) words wq, dq, dl, dr; the m-th uses
+// word m & 3 of Philox block blk0 + (m >> 2).  Returns the flips at bits 2m.
+template <int NQH, int DEG>
+__device__ __forceinline__ uint32_t update_half(uint32_t wq, const uint32_t (&dq)[DEG], uint32_t dl, uint32_t dr,
+                                                const float (&J)[DEG], float h, float jp, int q, int blk0, uint32_t i,
+                                                uint32_t sweep, uint32_t rep, uint32_t key0, uint32_t key1,
+                                                float m2beta, float m2blog2e) {
     uint32_t flips = 0;
 #pragma unroll
-    for (int blk = 0; blk < (NQ + 3) / 4; ++blk) {
-        const pq_u32x4 rnd = pq_philox(pq_u32x4{i, sweep, rep, (uint32_t)((q << 16) | blk)}, key0, key1);
+    for (int blk = 0; blk < (NQH + 3) / 4; ++blk) {
+        const pq_u32x4 rnd = pq_philox(pq_u32x4{i, sweep, rep, (uint32_t)((q << 16) | (blk0 + blk))}, key0, key1);
         const uint32_t rw4[4] = {rnd.x, rnd.y, rnd.z, rnd.w};
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
             const int mm = blk * 4 + jj;
-            if (mm < NQ) {
-                const int sh = 31 - 2 * mm;  // bit 2*mm of the q-shifted words -> sign bit
+            if (mm < NQH) {
+                const int sh = 31 - 2 * mm;  // bit 2*mm -> sign bit
                 float e = flip_sign(h, (wq << sh) & 0x80000000u);
 #pragma unroll
                 for (int m = 0; m < DEG; ++m) e = __fadd_rn(e, flip_sign(J[m], (dq[m] << sh) & 0x80000000u));
@@ -186,6 +179,35 @@ __device__ __forceinline__ uint32_t update_fixed(uint32_t wi, const uint32_t (&d
             }
         }
     }
+    return flips;
+}
+
+// One spin's local update over the slices of slice class q, P = 2 * NQ slices
+// fixed at compile time (NQ <= 16 with 32-bit words, NQ = 32 with 64-bit words
+// as two 32-bit halves), DEG couplings.  Same arithmetic and uniforms as the
+// generic path.
+template <int NQ, int DEG, typename W>
+__device__ __forceinline__ W update_fixed(W wi, const W (&d)[DEG], const float (&J)[DEG], float h, float jp, int q,
+                                          uint32_t i, uint32_t sweep, uint32_t rep, uint32_t key0, uint32_t key1,
+                                          float m2beta, float m2blog2e) {
+    constexpr int P = 2 * NQ;
+    constexpr int BITS = 8 * sizeof(W);
+    constexpr W MASK = P >= BITS ? ~(W)0 : (((W)1 << P) - 1);
+    const W up = ((wi << 1) | (wi >> (P - 1))) & MASK;
+    const W dn = ((wi >> 1) | (wi << (P - 1))) & MASK;
+    const W dlw = wi ^ up, drw = wi ^ dn;
+    W flips = 0;
+#pragma unroll
+    for (int half = 0; half < (P + 31) / 32; ++half) {
+        constexpr int NQH = NQ < 16 ? NQ : 16;
+        uint32_t dq[DEG];
+#pragma unroll
+        for (int m = 0; m < DEG; ++m) dq[m] = (uint32_t)(d[m] >> (32 * half)) >> q;
+        const uint32_t f = update_half<NQH, DEG>((uint32_t)(wi >> (32 * half)) >> q, dq,
+                                                 (uint32_t)(dlw >> (32 * half)) >> q, (uint32_t)(drw >> (32 * half)) >> q,
+                                                 J, h, jp, q, 4 * half, i, sweep, rep, key0, key1, m2beta, m2blog2e);
+        flips |= (W)f << (32 * half);
+    }
     return flips << q;
 }
 
@@ -193,9 +215,27 @@ __device__ __forceinline__ uint32_t update_fixed(uint32_t wi, const uint32_t (&d
 // nrep x n words (staged by the caller); order: nrep x kMaxClasses bytes;
 // parity: nrep words.  Counts accepted local flips into nacc and out-of-range
 // indices into bad.
+template <typename W, int MAXDEG, int NQC, bool INLINE>
+__device__ __forceinline__ void run_item_body(const Item& it, W* sw, uint8_t* order, uint32_t* parity, const Group& g,
+                                              bool& bad, unsigned long long& nacc);
+
+// The single-instance kernel inlines the item loop; the batched kernel calls one
+// out-of-line copy per variant, so each variant keeps its own register budget.
 template <typename W, int MAXDEG, int NQC>
-__device__ void run_item(const Item& it, W* sw, uint8_t* order, uint32_t* parity, const Group& g, bool& bad,
-                         unsigned long long& nacc) {
+__device__ __forceinline__ void run_item(const Item& it, W* sw, uint8_t* order, uint32_t* parity, const Group& g,
+                                         bool& bad, unsigned long long& nacc) {
+    run_item_body<W, MAXDEG, NQC, true>(it, sw, order, parity, g, bad, nacc);
+}
+
+template <typename W, int MAXDEG, int NQC>
+__device__ __noinline__ void run_item_call(const Item& it, W* sw, uint8_t* order, uint32_t* parity, const Group& g,
+                                           bool& bad, unsigned long long& nacc) {
+    run_item_body<W, MAXDEG, NQC, false>(it, sw, order, parity, g, bad, nacc);
+}
+
+template <typename W, int MAXDEG, int NQC, bool INLINE>
+__device__ __forceinline__ void run_item_body(const Item& it, W* sw, uint8_t* order, uint32_t* parity, const Group& g,
+                                              bool& bad, unsigned long long& nacc) {
     const int n = it.n, P = it.P, S = it.stride, nrep = it.nrep;
     const W mask = full_mask<W>(P);
     const int nclass_q = P == 1 ? 1 : ((P & 1) ? 3 : 2);
@@ -227,11 +267,10 @@ __device__ void run_item(const Item& it, W* sw, uint8_t* order, uint32_t* parity
                             const float h = __ldg(it.field + i);
                             const uint32_t rep = it.replica0 + rl;
                             if constexpr (NQC > 0) {
-                                const uint32_t fl = update_fixed<NQC, MAXDEG>(
-                                    (uint32_t)wi, reinterpret_cast<const uint32_t(&)[MAXDEG]>(d), J, h, jp, q,
-                                    (uint32_t)i, sweep, rep, it.key0, it.key1, m2beta, m2blog2e);
-                                rw[i] = wi ^ (W)fl;
-                                nacc += __popc(fl);
+                                const W fl = update_fixed<NQC, MAXDEG, W>(wi, d, J, h, jp, q, (uint32_t)i, sweep, rep,
+                                                                          it.key0, it.key1, m2beta, m2blog2e);
+                                rw[i] = wi ^ fl;
+                                nacc += sizeof(W) == 8 ? __popcll((unsigned long long)fl) : __popc((uint32_t)fl);
                             } else {
                                 W dl, dr;
                                 trotter_diffs<W>(wi, P, mask, dl, dr);
@@ -333,19 +372,18 @@ __device__ inline void run_item_any(const Item& it, unsigned char* smem, const G
     if (it.P <= 32) {
         uint32_t* sw = reinterpret_cast<uint32_t*>(smem);
         stage_in<uint32_t>(it, sw, g);
-        if (it.maxdeg == 4 && it.P == 20) run_item<uint32_t, 4, 10>(it, sw, order, parity, g, bad, nacc);
-        else if (it.maxdeg == 4 && it.P == 16) run_item<uint32_t, 4, 8>(it, sw, order, parity, g, bad, nacc);
-        else if (it.maxdeg == 4 && it.P == 32) run_item<uint32_t, 4, 16>(it, sw, order, parity, g, bad, nacc);
-        else if (it.maxdeg <= 4) run_item<uint32_t, 4, 0>(it, sw, order, parity, g, bad, nacc);
-        else if (it.maxdeg <= 8) run_item<uint32_t, 8, 0>(it, sw, order, parity, g, bad, nacc);
-        else run_item<uint32_t, 16, 0>(it, sw, order, parity, g, bad, nacc);
+        if (it.maxdeg == 4 && it.P == 20) run_item_call<uint32_t, 4, 10>(it, sw, order, parity, g, bad, nacc);
+        else if (it.maxdeg == 4 && it.P == 16) run_item_call<uint32_t, 4, 8>(it, sw, order, parity, g, bad, nacc);
+        else if (it.maxdeg == 4 && it.P == 32) run_item_call<uint32_t, 4, 16>(it, sw, order, parity, g, bad, nacc);
+        else if (it.maxdeg <= 4) run_item_call<uint32_t, 4, 0>(it, sw, order, parity, g, bad, nacc);
+        else run_item_call<uint32_t, 8, 0>(it, sw, order, parity, g, bad, nacc);
         stage_out<uint32_t>(it, sw, g);
     } else {
         uint64_t* sw = reinterpret_cast<uint64_t*>(smem);
         stage_in<uint64_t>(it, sw, g);
-        if (it.maxdeg <= 4) run_item<uint64_t, 4, 0>(it, sw, order, parity, g, bad, nacc);
-        else if (it.maxdeg <= 8) run_item<uint64_t, 8, 0>(it, sw, order, parity, g, bad, nacc);
-        else run_item<uint64_t, 16, 0>(it, sw, order, parity, g, bad, nacc);
+        if (it.maxdeg == 4 && it.P == 64) run_item_call<uint64_t, 4, 32>(it, sw, order, parity, g, bad, nacc);
+        else if (it.maxdeg <= 4) run_item_call<uint64_t, 4, 0>(it, sw, order, parity, g, bad, nacc);
+        else run_item_call<uint64_t, 8, 0>(it, sw, order, parity, g, bad, nacc);
         stage_out<uint64_t>(it, sw, g);
     }
 }

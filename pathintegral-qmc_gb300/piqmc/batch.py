@@ -68,6 +68,8 @@ class Batch:
             raise ValueError("slices must be in 1..64 and replicas >= 1")
         self.problems = [nbs if isinstance(nbs, Problem) else Problem(nbs, on_device=False, subclasses=subclasses)
                          for nbs in nbs_list]
+        if any(pb.maxdeg > 8 for pb in self.problems):
+            raise _native.PiqmcError(_native.PQ_ERR_UNSUPPORTED, "batched sweeps support at most 8 couplings per spin")
         lib = _native.lib()
         # pools
         inst = np.zeros(n_inst, dtype=INST_DTYPE)

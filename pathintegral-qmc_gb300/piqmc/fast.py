@@ -53,7 +53,7 @@ def word_dtype(P):
 class Problem:
     """A sparse Ising instance in device order (see module docstring)."""
 
-    def __init__(self, nbs, nrows=None, on_device=True, subclasses=8):
+    def __init__(self, nbs, nrows=None, on_device=True, subclasses=8, quantum=None):
         idx, jv = split_neighbors(nbs, nrows)
         nbs = np.asarray(nbs, dtype=np.float64)
         n, maxnb = idx.shape
@@ -86,14 +86,23 @@ class Problem:
         self.ncolors = int(nc)
         K = max(1, min(int(subclasses), MAX_CLASSES // self.ncolors))
         self.subclasses = K
-        # sub-class by rank of a fixed hash within the colour: near-equal sizes
+        # sub-class sizes are multiples of `quantum` spins (the thread count a
+        # replica's CTA uses), so every thread has the same work in every phase
+        if quantum is None:
+            quantum = 128 if n >= 4096 else 32
+        self.quantum = int(quantum)
         h = _mix32(np.arange(n, dtype=np.uint64))
         cls = np.empty(n, dtype=np.int64)
+        base = 0
         for c in range(self.ncolors):
             members = np.nonzero(color == c)[0]
             ranked = members[np.argsort(h[members], kind="stable")]
-            cls[ranked] = c * K + (np.arange(len(members)) * K) // max(len(members), 1)
-        M = self.ncolors * K
+            m = len(members)
+            chunk = -(-max(m, 1) // K)
+            chunk = -(-chunk // self.quantum) * self.quantum if m >= K * self.quantum else chunk
+            cls[ranked] = base + np.arange(m) // chunk
+            base += -(-m // chunk) if m else 0
+        M = int(base)
         sizes = np.bincount(cls, minlength=M)
         S = int(sizes.max()) if n else 1
         self.nclass, self.class_stride, self.class_size = M, S, sizes.astype(np.int32)
