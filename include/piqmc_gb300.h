@@ -254,6 +254,22 @@ int pq_batch_anneal(const pq_batch_task* tasks, int ntasks, const pq_batch_item*
                     const float* field_pool, const int32_t* csize_pool, const float* jperp_pool,
                     void* words_pool, int* queue_head, const pq_batch_run* run, int grid, int threads,
                     int smem_bytes, unsigned long long* accepts, int32_t* status, void* stream);
+/* No counterpart in the reference.  The same batched anneal for callers that
+ * cannot allocate device memory -- for instance a host application that hands
+ * this library only its own input and output buffers, or code running where
+ * cudaMalloc is not allowed -- so it has no queue_head argument: the task counter
+ * lives in a 256-byte static device array of this library (held on every GPU
+ * that loads it until the process exits).  The first call on each device looks
+ * that array's address up (cudaGetSymbolAddress), so make the first call on a
+ * device before any stream capture.  Each call resets the counter; all calls
+ * share it, so calls that overlap on the GPU (other streams, other threads) race
+ * and must be serialised by the caller.  Limit: ntasks + grid <= 2^31 - 1 (the
+ * counter is 32-bit), else PQ_ERR_TOO_LARGE.  Allocates nothing. */
+int pq_batch_anneal_noalloc(const pq_batch_task* tasks, int ntasks, const pq_batch_item* items,
+                            const pq_batch_inst* insts, const int32_t* nbr_pool, const float* cpl_pool,
+                            const float* field_pool, const int32_t* csize_pool, const float* jperp_pool,
+                            void* words_pool, const pq_batch_run* run, int grid, int threads, int smem_bytes,
+                            unsigned long long* accepts, int32_t* status, void* stream);
 /* Shared memory one item of nrep replicas of an n-slot, P-slice instance needs. */
 int pq_batch_smem_bytes(int nrep, int n, int P);
 /* Resident CTAs per SM of the batched kernel for a launch shape, and the SM count. */

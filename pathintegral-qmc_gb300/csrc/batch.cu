@@ -75,9 +75,50 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(const pq_batch_task* __re
     }
 }
 
+// Scratch of pq_batch_anneal_noalloc: the persistent CTAs' task counter lives
+// here instead of in caller memory.  One 32-bit counter in a 256-byte array
+// (the whole array is reserved on every device that loads the library, until
+// the process exits).  Every call shares it.
+constexpr int kNoAllocScratchInts = 64;
+static __device__ __align__(256) int g_noalloc_scratch[kNoAllocScratchInts];
+
+// Device address of the scratch, looked up once per device (host code cannot use
+// the symbol itself: on the host it names a stand-in, not device memory).
+constexpr int kNoAllocMaxDevices = 64;
+static int* g_noalloc_ptr[kNoAllocMaxDevices];
+
+int noalloc_scratch(int** out) {
+    int dev = 0;
+    PQ_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return PQ_ERR_UNSUPPORTED;
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        PQ_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_ptr[dev] = static_cast<int*>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return PQ_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+// pq_batch_anneal without the caller's queue_head: for callers that cannot
+// allocate device memory.  Rejects ntasks + grid beyond the 32-bit counter.
+int pq_batch_anneal_noalloc(const pq_batch_task* tasks, int ntasks, const pq_batch_item* items,
+                            const pq_batch_inst* insts, const int32_t* nbr_pool, const float* cpl_pool,
+                            const float* field_pool, const int32_t* csize_pool, const float* jperp_pool,
+                            void* words_pool, const pq_batch_run* run, int grid, int threads, int smem_bytes,
+                            unsigned long long* accepts, int32_t* status, void* stream) {
+    if (ntasks < 0 || grid <= 0 || (int64_t)ntasks + grid > (int64_t)INT32_MAX) return PQ_ERR_TOO_LARGE;
+    int* head = nullptr;
+    const int st = noalloc_scratch(&head);  // first call on a device: symbol lookup
+    if (st != PQ_OK) return st;
+    return pq_batch_anneal(tasks, ntasks, items, insts, nbr_pool, cpl_pool, field_pool, csize_pool, jperp_pool,
+                           words_pool, head, run, grid, threads, smem_bytes, accepts, status, stream);
+}
+
 
 int pq_batch_smem_bytes(int nrep, int n, int P) { return (int)item_smem_bytes(nrep, n, P); }
 

@@ -87,6 +87,8 @@ SIGNATURES = {
     "pq_guard_band_probe": (_I32, [_U32, _I64, _V, _V]),
     "pq_fp32_fma_probe": (_I32, [_V, _I32, _I32, _I32, _V]),
     "pq_batch_anneal": (_I32, [_V, _I32, _V, _V, _V, _V, _V, _V, _V, _V, _V, _V, _I32, _I32, _I32, _V, _V, _V]),
+    "pq_batch_anneal_noalloc": (_I32, [_V, _I32, _V, _V, _V, _V, _V, _V, _V, _V, _V, _I32, _I32, _I32, _V, _V,
+                                       _V]),
     "pq_batch_smem_bytes": (_I32, [_I32, _I32, _I32]),
     "pq_batch_occupancy": (_I32, [_I32, _I32, _V, _V]),
     "pq_energy_packed": (_I32, [_V, _I32, _I32, _I32, _I32, _V, _V, _V, _V, _V]),
