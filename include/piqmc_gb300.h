@@ -275,6 +275,16 @@ int pq_batch_smem_bytes(int nrep, int n, int P);
 /* Resident CTAs per SM of the batched kernel for a launch shape, and the SM count. */
 int pq_batch_occupancy(int threads, int smem_bytes, int* blocks_per_sm, int* sm_count);
 
+/* ---------------------------------------------------------------------------
+ * Tensor-core GEMM (new): D[M][N] = alpha * A[M][K] B[N][K]^T (+ bias[n]),
+ * BF16 row-major operands (K contiguous, leading dimensions lda/ldb elements,
+ * multiples of 8, 16-byte aligned), FP32 D (ldd floats), FP32 accumulation in
+ * TMEM via tcgen05.mma.  M % 128 == 0, N % 64 == 0, K % 64 == 0.  bias may be
+ * NULL.  A timed-out completion wait sets *status = PQ_ERR_TIMEOUT.
+ * ------------------------------------------------------------------------- */
+int pq_tc_gemm_bf16(const void* A, int lda, const void* B, int ldb, float* D, int ldd, int M, int N, int K,
+                    float alpha, const float* bias, int32_t* status, void* stream);
+
 /* FP64 classical energy of every (replica, slice) from a CSR of the coupling
  * matrix (row_ptr int64 [n+1], col int32, val double; diagonal = field),
  * reference piqmc/sa.pyx:25-44: E = -sum_{(i,j) off-diag} J_ij s_i s_j - sum_i J_ii s_i,
