@@ -285,6 +285,27 @@ int pq_batch_occupancy(int threads, int smem_bytes, int* blocks_per_sm, int* sm_
 int pq_tc_gemm_bf16(const void* A, int lda, const void* B, int ldb, float* D, int ldd, int M, int N, int K,
                     float alpha, const float* bias, int32_t* status, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Dense packed sweep (new; the physics of qmc.QuantumAnneal_dense, reference
+ * piqmc/qmc.pyx:141-242, with both quirks corrected).  words: uint32 [R][N]
+ * world-lines (P <= 32).  F: FP32 local fields f = h + K s of every
+ * configuration c = r*P + k, row c at F + c*ldf (the split-BF16 tensor-core GEMM
+ * of pq_tc_gemm_bf16 produces them); they are copied to shared memory and
+ * updated incrementally (rank-1) on every accepted flip.  K: FP32 symmetric
+ * couplings [N][N] with zero diagonal.  units: the nunits integers coprime to N
+ * (spin orders are random affine maps i = a t + b mod N, one per sweep shared by
+ * every slice like the reference's permutation, or one per slice when
+ * per_slice_order != 0).
+ * ------------------------------------------------------------------------- */
+int pq_dense_sweep(uint32_t* words, const float* F, int ldf, const float* K, const int32_t* units, int nunits,
+                   const float* jperp, int N, int P, int R, int nsched, int mcsteps, float beta, uint64_t seed,
+                   int64_t sweep_base, int replica_base, int per_slice_order, unsigned long long* accepts,
+                   void* stream);
+/* words [R][N] -> the GEMM operand: BF16 +-1 rows c = r*P + k (Mpad rows, zero
+ * padding), each row = [s over j < Npad, the same again] (2*Npad columns, so one
+ * GEMM against [K_hi | K_lo] sums both halves of the split couplings). */
+int pq_dense_unpack_bf16(const uint32_t* words, int N, int P, int R, int Npad, int Mpad, void* A, void* stream);
+
 /* FP64 classical energy of every (replica, slice) from a CSR of the coupling
  * matrix (row_ptr int64 [n+1], col int32, val double; diagonal = field),
  * reference piqmc/sa.pyx:25-44: E = -sum_{(i,j) off-diag} J_ij s_i s_j - sum_i J_ii s_i,

@@ -84,6 +84,9 @@ def _setup_fast(L):
     L.orc_fast_anneal.argtypes = [i32, i32, i32, P, P, P, i32, i32, P, i32, P, i32, i32, f32, u64,
                                   i64, i32, i32, P, P]
     L.orc_fast_anneal.restype = i64
+    if hasattr(L, "orc_dense_sweep"):
+        L.orc_dense_sweep.argtypes = [i32, i32, P, P, P, i32, P, i32, i32, f32, u64, i64, i32, P, i32]
+        L.orc_dense_sweep.restype = i64
 
 
 def _p(a):
@@ -218,6 +221,20 @@ def fast_anneal(nbr, cpl, field, class_size, class_stride, words, P, jperp, mcst
                                  _p(csz), int(order_mode), _p(jp), len(jp), int(mcsteps), float(np.float32(beta)),
                                  int(seed) & (2**64 - 1), int(sweep_base), int(replica), int(global_moves),
                                  _p(words), None if bt is None else _p(bt))
+
+
+def dense_sweep(F, K, units, words, P, jperp, mcsteps, beta, seed, sweep_base=0, replica=0, per_slice_order=False):
+    """Run the dense packed sweep of one replica in place on FP32 fields F (P, N) and uint32 words (N,)."""
+    F = np.ascontiguousarray(F, dtype=np.float32)
+    K = np.ascontiguousarray(K, dtype=np.float32)
+    units = np.ascontiguousarray(units, dtype=np.int32)
+    jp = np.ascontiguousarray(jperp, dtype=np.float32)
+    assert words.dtype == np.uint32 and words.flags.c_contiguous
+    N = K.shape[0]
+    n = lib().orc_dense_sweep(N, int(P), _p(F), _p(K), _p(units), len(units), _p(jp), len(jp), int(mcsteps),
+                              float(np.float32(beta)), int(seed) & (2**64 - 1), int(sweep_base), int(replica),
+                              _p(words), int(bool(per_slice_order)))
+    return n, F
 
 
 # ----------------------------------------------------------------------------------------

@@ -198,3 +198,57 @@ double orc_expf_max_relerr(uint32_t lo_bits, uint32_t hi_bits, uint32_t step) {
     }
     return worst;
 }
+
+/* Restatement of the dense packed sweep of one replica (spec in the header of
+ * csrc/dense.cu), starting from given FP32 fields F (P rows of N) and updating
+ * them in place with the kernel's rank-1 corrections.  K: FP32 [N][N] symmetric,
+ * zero diagonal; units: the integers coprime to N.  Returns accepted flips. */
+int64_t orc_dense_sweep(int N, int P, float* F, const float* K, const int32_t* units, int nunits,
+                        const float* jperp, int nsched, int mcsteps, float beta, uint64_t seed, int64_t sweep_base,
+                        int replica, uint32_t* w, int per_slice_order) {
+    const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    const int nclass_q = P == 1 ? 1 : ((P & 1) ? 3 : 2);
+    int64_t nacc = 0;
+    for (int g = 0; g < nsched; ++g) {
+        const float jp = P == 1 ? 0.0f : jperp[g];
+        for (int step = 0; step < mcsteps; ++step) {
+            const uint32_t sweep = (uint32_t)(sweep_base + (int64_t)g * mcsteps + step);
+            for (int q = 0; q < nclass_q; ++q) {
+                const int nq = slice_count(P, q);
+                /* slices of one class are independent: run them one after another */
+                for (int m = 0; m < nq; ++m) {
+                    const int k = q == 2 ? P - 1 : 2 * m + q;
+                    uint32_t ord[4];
+                    const uint32_t octr[4] = {0xFFFFFFFEu, sweep, (uint32_t)replica,
+                                              (3u << 24) | (uint32_t)(per_slice_order ? k : 0)};
+                    orc_philox4x32_10(octr, key, ord);
+                    const uint32_t a = (uint32_t)units[ord[0] % (uint32_t)nunits], b = ord[1] % (uint32_t)N;
+                    float* fk = F + (size_t)k * N;
+                    const int kl = k == 0 ? P - 1 : k - 1, kr = k == P - 1 ? 0 : k + 1;
+                    for (int t = 0; t < N; ++t) {
+                        uint32_t rnd[4];
+                        const uint32_t ctr[4] = {(uint32_t)k, sweep, (uint32_t)replica, (4u << 24) | (uint32_t)(t >> 2)};
+                        orc_philox4x32_10(ctr, key, rnd);
+                        const int i = (int)(((uint64_t)a * (uint32_t)t + b) % (uint32_t)N);
+                        const uint32_t wi = w[i];
+                        const int sbit = (int)((wi >> k) & 1u);
+                        const float e = sbit ? -fk[i] : fk[i];
+                        const int bl = (int)(((wi >> k) ^ (wi >> kl)) & 1u), br = (int)(((wi >> k) ^ (wi >> kr)) & 1u);
+                        const float tt = (bl ? -jp : jp) + (br ? -jp : jp);
+                        const float ediff = -2.0f * (e + tt);
+                        int acc = ediff > 0.0f;
+                        if (!acc) acc = u01(rnd[t & 3]) < orc_expf(ediff * beta);
+                        if (acc) {
+                            const float c = sbit ? 2.0f : -2.0f;
+                            const float* Ki = K + (size_t)i * N;
+                            for (int j = 0; j < N; ++j) fk[j] = fmaf(c, Ki[j], fk[j]);
+                            w[i] ^= 1u << k;
+                            ++nacc;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    return nacc;
+}

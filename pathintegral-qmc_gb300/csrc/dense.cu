@@ -1,0 +1,170 @@
+// Dense-J packed sweep (qmc.QuantumAnneal_dense physics, reference
+// piqmc/qmc.pyx:141-242, with both quirks corrected): local fields kept in
+// shared memory and updated by rank-1 corrections on every accepted flip;
+// periodically recomputed from scratch on the tensor cores (split-BF16 GEMM,
+// see piqmc/dense.py).
+//
+// Every spin couples to every other, so within a Trotter slice the updates are
+// sequential; the parallelism is across the slices of one slice class (one
+// warp per slice) and across replicas (one CTA per replica).
+//
+// Specification of one sweep of replica r (sweep counter `sweep`):
+//  * slice classes as in the sparse sweep; warp w handles slice k = 2w + q of
+//    class q (slice P-1 alone for the third class of odd P);
+//  * spin order of slice k: i_t = (a t + b) mod N, t = 0..N-1, with
+//    (w0, w1) = Philox(ctr = {0xFFFFFFFE, sweep, replica, 3 << 24 | kk}) words 0, 1,
+//    a = units[w0 % nunits] (a unit mod N), b = w1 % N; kk = 0 (one order shared by
+//    every slice of the sweep, as the reference shares its permutation) unless
+//    per-slice orders are requested (kk = k: anneals faster, dynamics differ);
+//  * update of spin i in slice k (FP32, one rounding per op, in order):
+//    e = s_i f_i (f = h + sum_j K_ij s_j, the stored field), t = J-perp s_i s_{k-1}
+//    + J-perp s_i s_{k+1}, sum = e + t; flip when sum < 0, else when
+//    u < expf_neg(fl(sum * (-2 beta))), u = (r >> 9) 2^-23 with r = word t & 3 of
+//    Philox(ctr = {k, sweep, replica, 4 << 24 | t >> 2});
+//  * on a flip, f_j <- fma(2 s_i_new, K_ij, f_j) for every j (K_ii = 0).
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+#include "sweep_core.cuh"
+
+namespace {
+
+using namespace pq;
+
+struct DenseArgs {
+    int N, P, R, nunits, ldf, per_slice_order;
+    int nsched, mcsteps;
+    float beta;
+    uint32_t key0, key1;
+    int64_t sweep_base;
+    int replica_base;
+};
+
+__global__ void __launch_bounds__(512) dense_sweep_kernel(uint32_t* __restrict__ words, const float* __restrict__ F,
+                                                           const float* __restrict__ K, const int32_t* __restrict__ units,
+                                                           const float* __restrict__ jperp, DenseArgs a,
+                                                           unsigned long long* __restrict__ accepts) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int N = a.N, P = a.P;
+    float* sf = reinterpret_cast<float*>(smem);                       // [P][N] fields
+    uint32_t* sw = reinterpret_cast<uint32_t*>(sf + (size_t)P * N);    // [N] world-lines
+    const int r = blockIdx.x;
+    const uint32_t rep = (uint32_t)(a.replica_base + r);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int t = threadIdx.x; t < P * N; t += blockDim.x) {
+        const int k = t / N, i = t - k * N;
+        sf[t] = F[(size_t)(r * P + k) * a.ldf + i];
+    }
+    for (int t = threadIdx.x; t < N; t += blockDim.x) sw[t] = words[(size_t)r * N + t];
+    __syncthreads();
+    const int nclass_q = P == 1 ? 1 : ((P & 1) ? 3 : 2);
+    unsigned long long nacc = 0;
+    for (int g = 0; g < a.nsched; ++g) {
+        const float jp = P == 1 ? 0.0f : jperp[g];
+        const float m2beta = __fmul_rn(-2.0f, a.beta);
+        const float m2blog2e = __fmul_rn(m2beta, 1.44269502162933349609375f);
+        for (int step = 0; step < a.mcsteps; ++step) {
+            const uint32_t sweep = (uint32_t)(a.sweep_base + (int64_t)g * a.mcsteps + step);
+            for (int q = 0; q < nclass_q; ++q) {
+                const int nq = slice_count(P, q);
+                if (warp < nq) {
+                    const int k = slice_of(P, q, warp);
+                    const uint32_t kk = a.per_slice_order ? (uint32_t)k : 0u;
+                    const pq_u32x4 ord = pq_philox(pq_u32x4{0xFFFFFFFEu, sweep, rep, (3u << 24) | kk}, a.key0, a.key1);
+                    const uint32_t am = (uint32_t)__ldg(units + ord.x % (uint32_t)a.nunits);
+                    const uint32_t bm = ord.y % (uint32_t)N;
+                    float* fk = sf + (size_t)k * N;
+                    const int kl = k == 0 ? P - 1 : k - 1, kr = k == P - 1 ? 0 : k + 1;
+                    pq_u32x4 mine{0, 0, 0, 0};
+                    for (int t = 0; t < N; ++t) {
+                        if ((t & 127) == 0) {
+                            mine = pq_philox(pq_u32x4{(uint32_t)k, sweep, rep, (4u << 24) | (uint32_t)((t >> 2) + lane)},
+                                             a.key0, a.key1);
+                        }
+                        const int src = (t & 127) >> 2;
+                        const uint32_t c0 = __shfl_sync(0xffffffffu, mine.x, src);
+                        const uint32_t c1 = __shfl_sync(0xffffffffu, mine.y, src);
+                        const uint32_t c2 = __shfl_sync(0xffffffffu, mine.z, src);
+                        const uint32_t c3 = __shfl_sync(0xffffffffu, mine.w, src);
+                        const uint32_t rnd = (t & 3) == 0 ? c0 : (t & 3) == 1 ? c1 : (t & 3) == 2 ? c2 : c3;
+                        const int i = (int)(((uint64_t)am * (uint32_t)t + bm) % (uint32_t)N);
+                        const uint32_t wi = sw[i];
+                        const uint32_t sbit = (wi >> k) & 1u;
+                        const float e = flip_sign(fk[i], sbit << 31);
+                        const float tt = __fadd_rn(flip_sign(jp, (((wi >> k) ^ (wi >> kl)) & 1u) << 31),
+                                                   flip_sign(jp, (((wi >> k) ^ (wi >> kr)) & 1u) << 31));
+                        const bool acc = decide(__fadd_rn(e, tt), pq_u01(rnd), m2beta, m2blog2e);
+                        if (acc) {
+                            // new spin = -old: s_new = +1 when the old bit was set (old spin -1)
+                            const float c = sbit ? 2.0f : -2.0f;
+                            const float* Ki = K + (size_t)i * N;
+                            for (int j = lane; j < N; j += 32) fk[j] = __fmaf_rn(c, __ldg(Ki + j), fk[j]);
+                            if (lane == 0) atomicXor(sw + i, 1u << k);
+                            ++nacc;
+                        }
+                        __syncwarp();
+                    }
+                }
+                __syncthreads();
+            }
+        }
+    }
+    for (int t = threadIdx.x; t < N; t += blockDim.x) words[(size_t)r * N + t] = sw[t];
+    if (accepts && lane == 0 && nacc) atomicAdd(accepts, nacc);
+}
+
+// words [R][N] (bits = slices) -> BF16 +-1 rows [R*P (padded to Mpad)][2 Npad]: row c = r*P + k holds
+// s_k over spins j twice (columns j and Npad + j), zeros for padding.
+__global__ void dense_unpack_kernel(const uint32_t* __restrict__ words, int N, int P, int R, int Npad, int Mpad,
+                                    __nv_bfloat16* __restrict__ A) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t total = (int64_t)Mpad * Npad;
+    if (t >= total) return;
+    const int c = (int)(t / Npad), j = (int)(t % Npad);
+    float v = 0.0f;
+    if (c < R * P && j < N) {
+        const int r = c / P, k = c % P;
+        v = ((words[(size_t)r * N + j] >> k) & 1u) ? -1.0f : 1.0f;
+    }
+    const __nv_bfloat16 b = __float2bfloat16_rn(v);
+    A[(size_t)c * 2 * Npad + j] = b;
+    A[(size_t)c * 2 * Npad + Npad + j] = b;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pq_dense_unpack_bf16(const uint32_t* words, int N, int P, int R, int Npad, int Mpad, void* A, void* stream) {
+    if (!words || !A || N <= 0 || P < 1 || P > 32 || R <= 0 || Npad < N || Mpad < R * P) return PQ_ERR_INVALID_ARG;
+    const int64_t total = (int64_t)Mpad * Npad;
+    dense_unpack_kernel<<<(unsigned)((total + 255) / 256), 256, 0, (cudaStream_t)stream>>>(words, N, P, R, Npad, Mpad,
+                                                                                            (__nv_bfloat16*)A);
+    return pq_launch_status();
+}
+
+int pq_dense_sweep(uint32_t* words, const float* F, int ldf, const float* K, const int32_t* units, int nunits,
+                   const float* jperp, int N, int P, int R, int nsched, int mcsteps, float beta, uint64_t seed,
+                   int64_t sweep_base, int replica_base, int per_slice_order, unsigned long long* accepts,
+                   void* stream) {
+    if (!words || !F || !K || !units || !jperp || N <= 0 || P < 1 || P > 32 || R < 0 || nsched < 0 || mcsteps < 0 ||
+        nunits <= 0 || ldf < N)
+        return PQ_ERR_INVALID_ARG;
+    if (R == 0 || nsched == 0) return PQ_OK;
+    const size_t smem = (size_t)P * N * 4 + (size_t)N * 4;
+    if (smem > 220 * 1024) return PQ_ERR_TOO_LARGE;
+    static bool attr = false;
+    if (!attr) {
+        PQ_CUDA_TRY(cudaFuncSetAttribute(dense_sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+        attr = true;
+    }
+    DenseArgs a;
+    a.N = N; a.P = P; a.R = R; a.nunits = nunits; a.ldf = ldf; a.per_slice_order = per_slice_order ? 1 : 0; a.nsched = nsched; a.mcsteps = mcsteps; a.beta = beta;
+    a.key0 = (uint32_t)seed; a.key1 = (uint32_t)(seed >> 32); a.sweep_base = sweep_base; a.replica_base = replica_base;
+    const int maxq = P == 1 ? 1 : (P + 1) / 2;
+    const int threads = 32 * maxq;
+    dense_sweep_kernel<<<R, threads, smem, (cudaStream_t)stream>>>(words, F, K, units, jperp, a, accepts);
+    return pq_launch_status();
+}
+
+}  // extern "C"

@@ -92,6 +92,9 @@ SIGNATURES = {
     "pq_batch_smem_bytes": (_I32, [_I32, _I32, _I32]),
     "pq_batch_occupancy": (_I32, [_I32, _I32, _V, _V]),
     "pq_tc_gemm_bf16": (_I32, [_V, _I32, _V, _I32, _V, _I32, _I32, _I32, _I32, _F32, _V, _V, _V]),
+    "pq_dense_sweep": (_I32, [_V, _V, _I32, _V, _V, _I32, _V, _I32, _I32, _I32, _I32, _I32, _F32, _U64, _I64, _I32,
+                              _I32, _V, _V]),
+    "pq_dense_unpack_bf16": (_I32, [_V, _I32, _I32, _I32, _I32, _I32, _V, _V]),
     "pq_energy_packed": (_I32, [_V, _I32, _I32, _I32, _I32, _V, _V, _V, _V, _V]),
     "pq_pack_spins": (_I32, [_V, _I32, _I32, _I32, _V, _V, _I32, _I32, _V]),
     "pq_unpack_spins": (_I32, [_V, _I32, _I32, _I32, _I32, _V, _I32, _V, _V]),

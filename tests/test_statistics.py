@@ -81,3 +81,39 @@ def test_shipped_quirks_change_the_physics(samples):
     r = samples["corrected"].min(1)
     se = np.sqrt(s.var(ddof=1) / len(s) + r.var(ddof=1) / len(r))
     assert s.mean() - r.mean() > 5 * se
+
+
+def _dense_run(kind, J, seed, P=8, T=0.05, ns=60):
+    import math
+    N = J.shape[0]
+    sched = np.linspace(3.0, 1e-8, ns)
+    rs = np.random.default_rng(5000 + seed)
+    s0 = np.where(rs.random(N) < 0.5, -1, 1).astype(np.int8)
+    if kind == "fast":
+        up = np.triu(J, 1)
+        K = up + up.T
+        sp = np.tile(s0, (P, 1)).astype(np.float64)              # (P, N)
+        F = (sp @ K.T + np.diag(J)[None, :]).astype(np.float32)
+        w = (((np.tile(s0, (P, 1)).T < 0).astype(np.uint64) << np.arange(P, dtype=np.uint64)).sum(1)).astype(np.uint32)
+        units = np.array([a for a in range(1, N) if math.gcd(a, N) == 1], np.int32)
+        oracle.dense_sweep(F, K.astype(np.float32), units, w, P, oracle.jperp(sched, P, T), 1,
+                           np.float32(1) / np.float32(T), seed, replica=seed)
+        spins = np.where((w[:, None] >> np.arange(P, dtype=np.uint32)) & 1, -1, 1)
+    else:
+        spins = np.ascontiguousarray(np.tile(s0, (P, 1)).T)
+        perms = oracle.reference_perms(np.random.RandomState(seed), N, ns)
+        rands = rs.integers(0, 2 ** 31 - 1, size=N * P * ns, dtype=np.int64).astype(np.int32)
+        oracle.qa_dense(spins, J, sched, 1, T, perms, rands, flags=3)
+    return np.array([oracle.classical_energy(spins[:, k].astype(np.float64), J) for k in range(P)])
+
+
+def test_dense_fast_matches_corrected_reference():
+    """Dense packed algorithm vs the corrected dense reference (QuantumAnneal_dense), 300 seeds, 99% CI."""
+    g = np.random.default_rng(3)
+    N = 32
+    J = np.triu(g.normal(0.0, 1.0 / np.sqrt(N), (N, N)), 1) + np.diag(g.normal(0.0, np.sqrt(0.1), N))
+    f = np.array([_dense_run("fast", J, s).min() for s in range(300)])
+    r = np.array([_dense_run("corrected", J, s).min() for s in range(300)])
+    diff = f.mean() - r.mean()
+    se = np.sqrt(f.var(ddof=1) / len(f) + r.var(ddof=1) / len(r))
+    assert abs(diff) < 2.576 * se, (f.mean(), r.mean(), se)
