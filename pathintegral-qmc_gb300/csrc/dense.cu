@@ -40,7 +40,7 @@ struct DenseArgs {
     int replica_base;
 };
 
-__global__ void __launch_bounds__(512) dense_sweep_kernel(uint32_t* __restrict__ words, const float* __restrict__ F,
+__global__ void __launch_bounds__(512, 2) dense_sweep_kernel(uint32_t* __restrict__ words, const float* __restrict__ F,
                                                            const float* __restrict__ K, const int32_t* __restrict__ units,
                                                            const float* __restrict__ jperp, DenseArgs a,
                                                            unsigned long long* __restrict__ accepts) {
@@ -76,18 +76,20 @@ __global__ void __launch_bounds__(512) dense_sweep_kernel(uint32_t* __restrict__
                     float* fk = sf + (size_t)k * N;
                     const int kl = k == 0 ? P - 1 : k - 1, kr = k == P - 1 ? 0 : k + 1;
                     pq_u32x4 mine{0, 0, 0, 0};
+                    // i_t = (a t + b) mod N, advanced incrementally (a < N, b < N)
+                    uint32_t i = bm;
                     for (int t = 0; t < N; ++t) {
                         if ((t & 127) == 0) {
                             mine = pq_philox(pq_u32x4{(uint32_t)k, sweep, rep, (4u << 24) | (uint32_t)((t >> 2) + lane)},
                                              a.key0, a.key1);
                         }
-                        const int src = (t & 127) >> 2;
-                        const uint32_t c0 = __shfl_sync(0xffffffffu, mine.x, src);
-                        const uint32_t c1 = __shfl_sync(0xffffffffu, mine.y, src);
-                        const uint32_t c2 = __shfl_sync(0xffffffffu, mine.z, src);
-                        const uint32_t c3 = __shfl_sync(0xffffffffu, mine.w, src);
-                        const uint32_t rnd = (t & 3) == 0 ? c0 : (t & 3) == 1 ? c1 : (t & 3) == 2 ? c2 : c3;
-                        const int i = (int)(((uint64_t)am * (uint32_t)t + bm) % (uint32_t)N);
+                        const uint32_t comp = (t & 3) == 0 ? mine.x : (t & 3) == 1 ? mine.y : (t & 3) == 2 ? mine.z : mine.w;
+                        const uint32_t rnd = __shfl_sync(0xffffffffu, comp, (t & 127) >> 2);
+                        uint32_t inext = i + am;
+                        if (inext >= (uint32_t)N) inext -= (uint32_t)N;
+                        // pull the next spin's coupling row into L1 (one 128-byte line per lane)
+                        if (t + 1 < N && lane * 32 < N)
+                            asm volatile("prefetch.global.L1 [%0];" ::"l"(K + (size_t)inext * N + lane * 32));
                         const uint32_t wi = sw[i];
                         const uint32_t sbit = (wi >> k) & 1u;
                         const float e = flip_sign(fk[i], sbit << 31);
@@ -98,10 +100,26 @@ __global__ void __launch_bounds__(512) dense_sweep_kernel(uint32_t* __restrict__
                             // new spin = -old: s_new = +1 when the old bit was set (old spin -1)
                             const float c = sbit ? 2.0f : -2.0f;
                             const float* Ki = K + (size_t)i * N;
-                            for (int j = lane; j < N; j += 32) fk[j] = __fmaf_rn(c, __ldg(Ki + j), fk[j]);
+                            if (N <= 512) {
+                                // all row loads in flight at once, then the updates
+                                float kv[16];
+#pragma unroll
+                                for (int m = 0; m < 16; ++m) {
+                                    const int j = lane + 32 * m;
+                                    kv[m] = j < N ? __ldg(Ki + j) : 0.0f;
+                                }
+#pragma unroll
+                                for (int m = 0; m < 16; ++m) {
+                                    const int j = lane + 32 * m;
+                                    if (j < N) fk[j] = __fmaf_rn(c, kv[m], fk[j]);
+                                }
+                            } else {
+                                for (int j = lane; j < N; j += 32) fk[j] = __fmaf_rn(c, __ldg(Ki + j), fk[j]);
+                            }
                             if (lane == 0) atomicXor(sw + i, 1u << k);
                             ++nacc;
                         }
+                        i = inext;
                         __syncwarp();
                     }
                 }
