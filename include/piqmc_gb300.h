@@ -306,6 +306,41 @@ int pq_dense_sweep(uint32_t* words, const float* F, int ldf, const float* K, con
  * GEMM against [K_hi | K_lo] sums both halves of the split couplings). */
 int pq_dense_unpack_bf16(const uint32_t* words, int N, int P, int R, int Npad, int Mpad, void* A, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Learned world-line proposals (new).  An MLP 8 -> 64 -> 64 -> 1 (ReLU) scores
+ * every spin of one update class from its world-line features; the two hidden
+ * layers run on the tensor cores (pq_tc_gemm_bf16, BF16 weights, FP32
+ * accumulation), the rest in these kernels.  Features: see csrc/mlp.cu.
+ * ------------------------------------------------------------------------- */
+/* Rows r*csize + s of X (BF16, 64 columns, only the first 8 written) get the
+ * features of spin slot cls*stride + s of replica r; rows Mpad + r*csize + s the
+ * features of the same world-line flipped; dE the classical cost of the flip. */
+int pq_mlp_features(const void* words, int word_bits, int n, int P, int R, int maxdeg, const int32_t* nbr,
+                    const float* cpl, const float* field, int cls, int stride, int csize, float beta, float jp,
+                    void* X, float* dE, int64_t Mpad, void* stream);
+/* out = BF16(relu(H)) element-wise (n elements). */
+int pq_mlp_relu_bf16(const float* H, void* out, int64_t n, void* stream);
+/* logit[r] = relu(H2[r][0..63]) . w3 + b3. */
+int pq_mlp_head(const float* H2, const float* w3, float b3, float* logit, int64_t rows, void* stream);
+/* Metropolis-Hastings world-line move of every spin of class cls: proposed with
+ * q = clamp(sigmoid(logit[row]), qmin, 1), accepted with
+ * min(1, exp(-beta dE) q'/q), q' from logit[Mpad + row] (the flipped features).
+ * counters (optional): [proposed, accepted]. */
+int pq_mlp_propose(void* words, int word_bits, int n, int P, int R, int cls, int stride, int csize,
+                   const float* logit, const float* dE, int64_t Mpad, float qmin, float beta, uint32_t move,
+                   uint64_t seed, int replica_base, unsigned long long* counters, void* stream);
+/* Training (BCE with soft targets y, mean over the batch B): head backward
+ * (dH2 row-major and transposed, grads of w3, b3, loss), hidden backward
+ * (mask by relu'(H1), transposed BF16 dH1, grad of b1), column sums, BF16
+ * transpose of a [B][64] matrix, Adam update. */
+int pq_mlp_head_backward(const float* H2, const float* logit, const float* y, const float* w3, int B, void* dH2,
+                         void* dH2T, float* gw3, float* gb3, float* loss, void* stream);
+int pq_mlp_hidden_backward(const float* G, const float* H1, int B, void* dH1T, float* gb1, void* stream);
+int pq_mlp_colsum_bf16(const void* T, int cols, int B, float* out, void* stream);
+int pq_mlp_transpose_bf16(const void* A, int B, void* AT, void* stream);
+int pq_adam(float* p, const float* g, float* m, float* v, int n, float lr, float b1, float b2, float eps, int step,
+            void* stream);
+
 /* FP64 classical energy of every (replica, slice) from a CSR of the coupling
  * matrix (row_ptr int64 [n+1], col int32, val double; diagonal = field),
  * reference piqmc/sa.pyx:25-44: E = -sum_{(i,j) off-diag} J_ij s_i s_j - sum_i J_ii s_i,

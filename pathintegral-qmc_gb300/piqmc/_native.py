@@ -95,6 +95,17 @@ SIGNATURES = {
     "pq_dense_sweep": (_I32, [_V, _V, _I32, _V, _V, _I32, _V, _I32, _I32, _I32, _I32, _I32, _F32, _U64, _I64, _I32,
                               _I32, _V, _V]),
     "pq_dense_unpack_bf16": (_I32, [_V, _I32, _I32, _I32, _I32, _I32, _V, _V]),
+    "pq_mlp_features": (_I32, [_V, _I32, _I32, _I32, _I32, _I32, _V, _V, _V, _I32, _I32, _I32, _F32, _F32, _V, _V,
+                               _I64, _V]),
+    "pq_mlp_relu_bf16": (_I32, [_V, _V, _I64, _V]),
+    "pq_mlp_head": (_I32, [_V, _V, _F32, _V, _I64, _V]),
+    "pq_mlp_propose": (_I32, [_V, _I32, _I32, _I32, _I32, _I32, _I32, _I32, _V, _V, _I64, _F32, _F32, _U32, _U64,
+                              _I32, _V, _V]),
+    "pq_mlp_head_backward": (_I32, [_V, _V, _V, _V, _I32, _V, _V, _V, _V, _V, _V]),
+    "pq_mlp_hidden_backward": (_I32, [_V, _V, _I32, _V, _V, _V]),
+    "pq_mlp_colsum_bf16": (_I32, [_V, _I32, _I32, _V, _V]),
+    "pq_mlp_transpose_bf16": (_I32, [_V, _I32, _V, _V]),
+    "pq_adam": (_I32, [_V, _V, _V, _V, _I32, _F32, _F32, _F32, _F32, _I32, _V]),
     "pq_energy_packed": (_I32, [_V, _I32, _I32, _I32, _I32, _V, _V, _V, _V, _V]),
     "pq_pack_spins": (_I32, [_V, _I32, _I32, _I32, _V, _V, _I32, _I32, _V]),
     "pq_unpack_spins": (_I32, [_V, _I32, _I32, _I32, _I32, _V, _I32, _V, _V]),
