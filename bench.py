@@ -323,10 +323,11 @@ def gpu_arm(args):
         e2e_s = float(t.item())
     e2e_value = updates * len(e2e_ms) * world / e2e_s
 
-    batched = densew = None
+    batched = densew = learnedw = None
     if not args.no_batched and rank == 0:
         batched = batched_workload(args, torch)
         densew = dense_workload(args, torch)
+        learnedw = learned_vs_plain(args, torch, prob)
 
     peak = measured_fp32_peak(lib, torch)
     achieved_tflops = value / world * FLOP_PER_UPDATE / 1e12
@@ -368,6 +369,8 @@ def gpu_arm(args):
         line["batched_uneven"] = batched
     if densew is not None:
         line["dense"] = densew
+    if learnedw is not None:
+        line["learned_vs_uniform"] = learnedw
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -473,6 +476,77 @@ def dense_workload(args, torch):
         out["cpu_baseline"] = {"value": N * P * steps * cores / wall, "unit": "updates/s", "cores": cores,
                                "kind": "reference",
                                "sample": "%d processes x QuantumAnneal_dense N=512 P=32 x %d field steps" % (cores, steps)}
+    return out
+
+
+def learned_vs_plain(args, torch, prob_big, R=1024, every=20):
+    """80x80 P=20 anneal with a world-line move pass every `every` steps: uniform (plain) vs learned.
+
+    The network is first trained on moves recorded from plain 32x32 P=20 runs (J ~ U[-2, 2]).  Both forms
+    run the same local sweeps; the learned one replaces the uniform pass (every spin tried) with the
+    network's MH-corrected proposals.  Residual energy per spin = best-slice energy minus the best
+    energy found by either form, divided by n."""
+    import scipy.sparse as sps
+    from piqmc import fast, learned, tools
+    P = P_SLICES
+    g = np.random.default_rng(11)
+    L = 32
+    J = sps.dok_matrix((L * L, L * L))
+    for y in range(L):
+        for x in range(L):
+            i = y * L + x
+            J[i, y * L + (x + 1) % L] = float(np.float32(g.uniform(-2, 2)))
+            J[i, ((y + 1) % L) * L + x] = float(np.float32(g.uniform(-2, 2)))
+    small = fast.Problem(tools.GenerateNeighbors(L * L, J, 4))
+    Rs = 64
+    sched_s = schedule(200)
+    jp_s = fast.jperp_schedule(sched_s, P, TEMP)
+    spins_s = np.repeat(np.where(g.random((Rs, L * L)) < 0.5, -1, 1).astype(np.int8)[:, :, None], P, axis=2)
+    ws = small.pack(torch.from_numpy(spins_s))
+    t0 = time.perf_counter()
+    Xs, ys = [], []
+    for g0 in range(0, len(sched_s), 20):
+        fast.anneal(small, ws, sched_s[g0:g0 + 20], P, TEMP, seed=21, sweep_base=g0,
+                    jperp=torch.from_numpy(jp_s[g0:g0 + 20]).cuda())
+        X, y = learned.record_moves(small, ws, P, 1.0 / TEMP, float(jp_s[g0 + 19]))
+        Xs.append(X)
+        ys.append(y)
+    X, y = torch.cat(Xs), torch.cat(ys)
+    mlp = learned.ProposalMLP(seed=0)
+    hist = mlp.train(X, y, epochs=2, batch=16384, lr=3e-3)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    n = prob_big.n
+    spins = np.repeat(np.where(np.random.default_rng(12).random((R, n)) < 0.5, -1, 1).astype(np.int8)[:, :, None], P,
+                      axis=2)
+    sched = schedule()
+    jp_host = fast.jperp_schedule(sched, P, TEMP)
+    jp = torch.from_numpy(jp_host).cuda()
+    res = {}
+    for kind in ("uniform", "learned"):
+        w = prob_big.pack(torch.from_numpy(spins))
+        cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for g0 in range(0, len(sched), every):
+            g1 = min(len(sched), g0 + every)
+            fast.anneal(prob_big, w, sched[g0:g1], P, TEMP, seed=31, sweep_base=g0, jperp=jp[g0:g1], check=False)
+            learned.learned_pass(prob_big, w, P, mlp, 1.0 / TEMP, float(jp_host[g1 - 1]), seed=32, move=g0,
+                                 counters=cnt, uniform=(kind == "uniform"))
+        e1.record()
+        torch.cuda.synchronize()
+        E = prob_big.energies(w, P).cpu().numpy().min(axis=1)
+        c = cnt.cpu().numpy()
+        res[kind] = {"gpu_s": e0.elapsed_time(e1) * 1e-3, "best": E, "proposed": int(c[0]), "accepted": int(c[1])}
+    e_ref = min(res[k]["best"].min() for k in res)
+    out = {"workload": "80x80 P=20, %d replicas, 2000 steps, world-line pass every %d steps; MLP 8-64-64-1 trained on "
+                       "moves recorded from plain 32x32 P=20 runs" % (R, every),
+           "train_s": train_s, "train_loss_first_last": [hist[0], hist[-1]]}
+    for kind, r in res.items():
+        out[kind] = {"gpu_s": r["gpu_s"], "median_residual_energy_per_spin": float(np.median(r["best"] - e_ref) / n),
+                     "proposed": r["proposed"], "accepted": r["accepted"]}
+    out["learned_time_over_uniform"] = res["learned"]["gpu_s"] / res["uniform"]["gpu_s"]
     return out
 
 
