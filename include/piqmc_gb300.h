@@ -329,6 +329,34 @@ int pq_mlp_head(const float* H2, const float* w3, float b3, float* logit, int64_
 int pq_mlp_propose(void* words, int word_bits, int n, int P, int R, int cls, int stride, int csize,
                    const float* logit, const float* dE, int64_t Mpad, float qmin, float beta, uint32_t move,
                    uint64_t seed, int replica_base, unsigned long long* counters, void* stream);
+/* The whole learned move of class cls in one persistent kernel: features, both
+ * MLP layers as tcgen05 MMAs with TMEM accumulators, head, MH decision; the same
+ * moves as pq_mlp_features + two pq_tc_gemm_bf16 + pq_mlp_head + pq_mlp_propose.
+ * W1, W2: BF16 [64][64] row-major, 16-byte aligned (W1 columns >= 8 zero).
+ * logit_out (nullable, FP32 [2][R*csize]): logits of the current and flipped
+ * world-lines.  counters (nullable): [proposed, accepted] added to. */
+int pq_mlp_learned_move(void* words, int word_bits, int n, int P, int R, int maxdeg, const int32_t* nbr,
+                        const float* cpl, const float* field, int cls, int stride, int csize, float beta, float jp,
+                        const void* W1, const void* W2, const float* b1, const float* b2, const float* w3, float b3,
+                        float qmin, uint32_t move, uint64_t seed, int replica_base, float* logit_out,
+                        unsigned long long* counters, int32_t* status, void* stream);
+/* Uniform world-line move of every spin of class cls (the plain global move):
+ * flip spin i in every slice with probability min(1, exp(-beta dE)); the same
+ * uniforms and decision as the learned move with q = q' = 1. */
+int pq_worldline_move(void* words, int word_bits, int n, int P, int R, int maxdeg, const int32_t* nbr,
+                      const float* cpl, const float* field, int cls, int stride, int csize, float beta, uint32_t move,
+                      uint64_t seed, int replica_base, unsigned long long* counters, void* stream);
+/* A whole pass: the two moves above for classes 0..nclass-1 in order, one
+ * launch per class on `stream` (class_size: host array of nclass sizes). */
+int pq_mlp_learned_pass(void* words, int word_bits, int n, int P, int R, int maxdeg, const int32_t* nbr,
+                        const float* cpl, const float* field, int nclass, int stride, const int32_t* class_size,
+                        float beta, float jp, const void* W1, const void* W2, const float* b1, const float* b2,
+                        const float* w3, float b3, float qmin, uint32_t move, uint64_t seed, int replica_base,
+                        unsigned long long* counters, int32_t* status, void* stream);
+int pq_worldline_pass(void* words, int word_bits, int n, int P, int R, int maxdeg, const int32_t* nbr,
+                      const float* cpl, const float* field, int nclass, int stride, const int32_t* class_size,
+                      float beta, uint32_t move, uint64_t seed, int replica_base, unsigned long long* counters,
+                      void* stream);
 /* Training (BCE with soft targets y, mean over the batch B): head backward
  * (dH2 row-major and transposed, grads of w3, b3, loss), hidden backward
  * (mask by relu'(H1), transposed BF16 dH1, grad of b1), column sums, BF16

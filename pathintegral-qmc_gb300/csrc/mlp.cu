@@ -2,9 +2,9 @@
 // parts (the 64 x 64 layers run on the tensor cores through pq_tc_gemm_bf16),
 // the Metropolis-Hastings world-line move, and the training kernels.
 //
-// Features of spin i of a replica (P slices, local fields f^k = h_i + sum_j J_ij
-// s_j^k from its neighbours, which belong to other update classes):
-//   x0 = mean_k f^k / (1 + sum_m |J_im| + |h_i|)   (normalised local field)
+// Features of spin i of a replica (P slices, local fields f^k = h_i + sum_m J_m t_m^k
+// from its neighbours m, which belong to other update classes; s^k, t_m^k = +-1):
+//   x0 = mean_k f^k / (1 + sum_m |J_m| + |h_i|)   (normalised local field)
 //   x1 = std_k f^k / (same scale)
 //   x2 = mean_k s^k                                (world-line magnetisation)
 //   x3 = #{k : s^k != s^{k+1}} / P                 (slice disagreements, periodic)
@@ -12,12 +12,17 @@
 //   x5 = beta * (classical flip cost) / P, clipped to [-8, 8]
 //   x6 = J-perp * beta / P, clipped to [0, 8]      (how stiff the world-lines are)
 //   x7 = 1                                         (bias input)
+// The slice sums come from popcounts of the packed world-lines (exact integers),
+// combined in FP32 in the order spin_features writes them:
+//   sum_k t_m^k = P - 2 popc(w_m),  sum_k s^k t_m^k = P - 2 popc(w_i ^ w_m),
+//   sum_k t_m^k t_l^k = P - 2 popc(w_m ^ w_l).
 // The flipped world-line (s -> -s in every slice) has x2, x4, x5 negated and the
-// rest unchanged; both versions are scored in one pass (rows i and M + i).
+// rest unchanged; both versions are scored in one pass.
 #include <cuda_bf16.h>
 
 #include "common.cuh"
 #include "sweep_core.cuh"
+#include "tc_gemm.cuh"
 
 namespace {
 
@@ -26,53 +31,96 @@ using namespace pq;
 constexpr int kFeat = 8;
 constexpr int kLd = 64;  // padded feature / hidden width of the GEMM operands
 
+__device__ __forceinline__ int popc_(uint32_t x) { return __popc(x); }
+__device__ __forceinline__ int popc_(uint64_t x) { return __popcll(x); }
+
 template <typename W>
-__device__ void spin_features(const W* __restrict__ words_r, int i, int n, int P, int maxdeg,
+__device__ __forceinline__ W slice_mask(int P) {
+    return P >= (int)(8 * sizeof(W)) ? ~(W)0 : (((W)1 << P) - 1);
+}
+
+// Neighbour world-lines and couplings of spin i (padding entries point at i with coupling 0).
+// Entries m >= maxdeg are zero couplings to i itself, so every loop below runs over all MAXD
+// (>= maxdeg) entries, unrolled into registers.
+template <typename W, int MAXD>
+__device__ __forceinline__ void load_neighbourhood(const W* __restrict__ words_r, int i, int n, int maxdeg,
+                                                   const int32_t* __restrict__ nbr, const float* __restrict__ cpl,
+                                                   W (&nbw)[MAXD], float (&J)[MAXD]) {
+#pragma unroll
+    for (int m = 0; m < MAXD; ++m) {
+        J[m] = 0.0f;
+        nbw[m] = words_r[i];
+        if (m < maxdeg) {
+            const int j = __ldg(nbr + (int64_t)m * n + i);
+            J[m] = __ldg(cpl + (int64_t)m * n + i);
+            nbw[m] = words_r[(unsigned)j < (unsigned)n ? j : i];
+        }
+    }
+}
+
+// sum_k s^k f^k of spin i's world-line: h (P - 2 popc(w_i)), then + J_m (P - 2 popc(w_i ^ w_m)) for m in order.
+// Flipping every slice changes the classical energy by 2 * this.
+template <typename W, int MAXD>
+__device__ __forceinline__ float worldline_align(W wi, const W (&nbw)[MAXD], const float (&J)[MAXD], int deg,
+                                                 float h, int P, W mask) {
+    float sa = __fmul_rn(h, (float)(P - 2 * popc_(wi & mask)));
+#pragma unroll
+    for (int m = 0; m < MAXD; ++m)
+        if (m < deg)
+        sa = __fadd_rn(sa, __fmul_rn(J[m], (float)(P - 2 * popc_((wi ^ nbw[m]) & mask))));
+    return sa;
+}
+
+template <typename W, int MAXD>
+__device__ __forceinline__ void spin_features(const W* __restrict__ words_r, int i, int n, int P, int maxdeg,
                               const int32_t* __restrict__ nbr, const float* __restrict__ cpl, float h, float beta,
                               float jp, float (&x)[kFeat], float& dE) {
-    const W wi = words_r[i];
-    float scale = 1.0f + fabsf(h);
-    float fsum = 0.0f, fsq = 0.0f, align = 0.0f;
-    W nbw[16];
-    float J[16];
-    for (int m = 0; m < maxdeg && m < 16; ++m) {
-        const int j = __ldg(nbr + (int64_t)m * n + i);
-        J[m] = __ldg(cpl + (int64_t)m * n + i);
-        nbw[m] = words_r[(unsigned)j < (unsigned)n ? j : i];
-        scale += fabsf(J[m]);
+    const W mask = slice_mask<W>(P);
+    const W wi = words_r[i] & mask;
+    W nbw[MAXD];
+    float J[MAXD];
+    load_neighbourhood<W, MAXD>(words_r, i, n, maxdeg, nbr, cpl, nbw, J);
+    const int deg = maxdeg;
+    const float Pf = (float)P;
+    float scale = __fadd_rn(1.0f, fabsf(h));
+    float s1 = __fmul_rn(Pf, h);                  // sum_k f^k
+    float s2 = __fmul_rn(Pf, __fmul_rn(h, h));    // sum_k (f^k)^2
+    const float h2 = __fmul_rn(2.0f, h);
+#pragma unroll
+    for (int m = 0; m < MAXD; ++m) {
+        if (m >= deg) break;
+        scale = __fadd_rn(scale, fabsf(J[m]));
+        const float tm = (float)(P - 2 * popc_(nbw[m] & mask));
+        s1 = __fadd_rn(s1, __fmul_rn(J[m], tm));
+        s2 = __fadd_rn(s2, __fmul_rn(__fmul_rn(h2, J[m]), tm));
+        s2 = __fadd_rn(s2, __fmul_rn(__fmul_rn(J[m], J[m]), Pf));
+#pragma unroll
+        for (int l = 0; l < MAXD; ++l) {
+            if (l >= m) break;
+            const float tml = (float)(P - 2 * popc_((nbw[m] ^ nbw[l]) & mask));
+            s2 = __fadd_rn(s2, __fmul_rn(__fmul_rn(2.0f, __fmul_rn(J[m], J[l])), tml));
+        }
     }
-    for (int k = 0; k < P; ++k) {
-        float f = h;
-        for (int m = 0; m < maxdeg && m < 16; ++m) f += ((nbw[m] >> k) & 1) ? -J[m] : J[m];
-        const float s = ((wi >> k) & 1) ? -1.0f : 1.0f;
-        fsum += f;
-        fsq += f * f;
-        align += s * f;
-    }
-    const float inv = 1.0f / (float)P;
-    const float mean = fsum * inv;
-    const float var = fmaxf(fsq * inv - mean * mean, 0.0f);
-    int mag = 0, dis = 0;
-    for (int k = 0; k < P; ++k) {
-        mag += ((wi >> k) & 1) ? -1 : 1;
-        const int kn = k + 1 == P ? 0 : k + 1;
-        dis += (int)(((wi >> k) ^ (wi >> kn)) & 1);
-    }
-    dE = 2.0f * align;  // classical energy change of flipping the whole world-line
-    x[0] = mean / scale;
-    x[1] = sqrtf(var) / scale;
-    x[2] = (float)mag * inv;
-    x[3] = (float)dis * inv;
-    x[4] = align * inv / scale;
-    x[5] = fminf(fmaxf(beta * dE * inv, -8.0f), 8.0f);
-    x[6] = fminf(fmaxf(jp * beta * inv, 0.0f), 8.0f);
+    const float sa = worldline_align<W, MAXD>(wi, nbw, J, deg, h, P, mask);
+    const float inv = __fdiv_rn(1.0f, Pf);
+    const float mean = __fmul_rn(s1, inv);
+    const float var = fmaxf(__fsub_rn(__fmul_rn(s2, inv), __fmul_rn(mean, mean)), 0.0f);
+    const W rot = ((wi >> 1) | (wi << (P - 1))) & mask;   // bit k = slice k + 1 (periodic)
+    dE = __fmul_rn(2.0f, sa);
+    x[0] = __fdiv_rn(mean, scale);
+    x[1] = __fdiv_rn(__fsqrt_rn(var), scale);
+    x[2] = __fmul_rn((float)(P - 2 * popc_(wi)), inv);
+    x[3] = __fmul_rn((float)popc_(wi ^ rot), inv);
+    x[4] = __fdiv_rn(__fmul_rn(sa, inv), scale);
+    x[5] = fminf(fmaxf(__fmul_rn(__fmul_rn(beta, dE), inv), -8.0f), 8.0f);
+    x[6] = fminf(fmaxf(__fmul_rn(__fmul_rn(jp, beta), inv), 0.0f), 8.0f);
     x[7] = 1.0f;
 }
 
 // Rows [0, M): features of the current world-lines of class `cls` (all replicas,
 // row = r * csize + s); rows [M, 2M): the flipped versions.  dE[row] = classical
 // flip cost of the current world-line.
-template <typename W>
+template <typename W, int MAXD>
 __global__ void features_kernel(const W* __restrict__ words, int n, int P, int R, int maxdeg,
                                 const int32_t* __restrict__ nbr, const float* __restrict__ cpl,
                                 const float* __restrict__ field, int cls, int stride, int csize, float beta, float jp,
@@ -83,7 +131,7 @@ __global__ void features_kernel(const W* __restrict__ words, int n, int P, int R
     const int r = (int)(t / csize), s = (int)(t % csize);
     const int i = cls * stride + s;
     float x[kFeat], de;
-    spin_features<W>(words + (int64_t)r * n, i, n, P, maxdeg, nbr, cpl, __ldg(field + i), beta, jp, x, de);
+    spin_features<W, MAXD>(words + (int64_t)r * n, i, n, P, maxdeg, nbr, cpl, __ldg(field + i), beta, jp, x, de);
     dE[t] = de;
     __nv_bfloat16* row = X + t * kLd;
     __nv_bfloat16* rowf = X + (Mpad + t) * kLd;
@@ -247,7 +295,308 @@ __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, 
     p[t] -= lr * (mt / c1) / (sqrtf(vt / c2) + eps);
 }
 
+
+// ---------------------------------------------------------------------------
+// Fused learned move.  A persistent CTA of 4 warps takes tiles of 128 spins of
+// the class; thread t owns spin t of the tile and TMEM lane t.  Per tile:
+//   features of the current and flipped world-lines -> X, Xf (BF16, K = 16,
+//   columns 8..15 zero) in shared memory;
+//   layer 1: two tcgen05 MMAs (M = 128, N = 64, K = 16) into TMEM columns 0..63
+//   (current) and 64..127 (flipped); bias + ReLU -> H, Hf (BF16) in shared memory;
+//   layer 2: 2 x 4 MMAs (K = 64) into the same columns; bias + ReLU + head in
+//   registers, so each thread holds both logits of its spin;
+//   the MH decision as propose_kernel makes it.
+// The epilogues round exactly as the unfused path does (relu(acc + b1) to
+// BF16; head acc = b3 + sum_c relu(acc_c + b2) w3_c in column order), and the
+// K = 16 layer 1 equals the unfused K = 64 one whose extra columns are zero.
+// ---------------------------------------------------------------------------
+constexpr int kTile = 128;
+constexpr int kK1 = 16;
+constexpr int kOffX = 0;                              // X, Xf: 2 x [128][16] BF16
+constexpr int kOffH = kOffX + 2 * kTile * kK1 * 2;    // H, Hf: 2 x [128][64] BF16
+constexpr int kOffW1 = kOffH + 2 * kTile * kLd * 2;   // W1: [64][16] BF16
+constexpr int kOffW2 = kOffW1 + kLd * kK1 * 2;        // W2: [64][64] BF16
+constexpr int kOffB = kOffW2 + kLd * kLd * 2;         // b1, b2, w3: 3 x 64 FP32
+constexpr int kOffBar = kOffB + 3 * kLd * 4;          // mbarrier, TMEM slot
+constexpr int kSmemMove = kOffBar + 16;
+constexpr long long kMmaWait = 1ll << 24;
+static_assert(kOffH % 16 == 0 && kOffW1 % 16 == 0 && kOffW2 % 16 == 0 && kOffBar % 8 == 0, "alignment");
+
+struct MoveArgs {
+    int n, P, R, maxdeg, cls, stride, csize;
+    float beta, jp, qmin, b3;
+    uint32_t move, key0, key1, replica_base;
+    int64_t ntiles;
+};
+
+// Two floats rounded to BF16 (nearest even), the first in the low half (the lower address).
+__device__ __forceinline__ uint32_t bf16x2_bits(float lo, float hi) {
+    const __nv_bfloat162 b = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&b);
+}
+
+__device__ __forceinline__ float sigmoid_clamped(float z, float qmin) {
+    return fminf(fmaxf(1.0f / (1.0f + expf(-z)), qmin), 1.0f);
+}
+
+template <typename W, int MAXD>
+__global__ void __launch_bounds__(128) learned_move_kernel(W* __restrict__ words, const int32_t* __restrict__ nbr,
+                                                          const float* __restrict__ cpl,
+                                                          const float* __restrict__ field,
+                                                          const __nv_bfloat16* __restrict__ W1,
+                                                          const __nv_bfloat16* __restrict__ W2,
+                                                          const float* __restrict__ b1, const float* __restrict__ b2,
+                                                          const float* __restrict__ w3, MoveArgs a,
+                                                          float* __restrict__ logit_out,
+                                                          unsigned long long* __restrict__ counters,
+                                                          int32_t* __restrict__ status) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    unsigned char* sX = smem + kOffX;
+    unsigned char* sXf = sX + kTile * kK1 * 2;
+    unsigned char* sH = smem + kOffH;
+    unsigned char* sHf = sH + kTile * kLd * 2;
+    unsigned char* sW1 = smem + kOffW1;
+    unsigned char* sW2 = smem + kOffW2;
+    float* sb1 = reinterpret_cast<float*>(smem + kOffB);
+    float* sb2 = sb1 + kLd;
+    float* sw3 = sb2 + kLd;
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + kOffBar);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + kOffBar + 8);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t M = (int64_t)a.R * a.csize;
+
+    // weights (W1 columns 0..15 of its padded 64) and the zero K padding of X, Xf
+    for (int c = tid; c < kLd * (kK1 / 8); c += 128) {
+        const int r = c / (kK1 / 8), kk = (c % (kK1 / 8)) * 8;
+        *reinterpret_cast<uint4*>(sW1 + tc::tile_off(r, kk, kK1)) =
+            *reinterpret_cast<const uint4*>(W1 + r * kLd + kk);
+    }
+    for (int c = tid; c < kLd * (kLd / 8); c += 128) {
+        const int r = c / (kLd / 8), kk = (c % (kLd / 8)) * 8;
+        *reinterpret_cast<uint4*>(sW2 + tc::tile_off(r, kk, kLd)) =
+            *reinterpret_cast<const uint4*>(W2 + r * kLd + kk);
+    }
+    for (int c = tid; c < 2 * kTile * kK1 * 2 / 16; c += 128) reinterpret_cast<uint4*>(sX)[c] = make_uint4(0, 0, 0, 0);
+    if (tid < kLd) { sb1[tid] = b1[tid]; sb2[tid] = b2[tid]; sw3[tid] = w3[tid]; }
+    if (tid == 0) {
+        tc::mbar_init(tc::smem_addr(mbar), 1);
+        tc::mbar_fence_init();
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(tc::smem_addr(tslot), 2 * kLd);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tslot;
+    const uint32_t tlane = tmem + ((uint32_t)(32 * warp) << 16);
+    constexpr uint32_t idesc = tc::idesc_bf16(kTile, kLd);
+    const W mask = slice_mask<W>(a.P);
+    uint32_t phase = 0;
+    bool ok = true;
+
+    for (int64_t tile = blockIdx.x; tile < a.ntiles && ok; tile += gridDim.x) {
+        const int64_t t = tile * kTile + tid;
+        const bool valid = t < M;
+        int r = 0, i = 0;
+        float de = 0.0f;
+        {
+            float x[kFeat] = {0, 0, 0, 0, 0, 0, 0, 0};
+            if (valid) {
+                r = (int)(t / a.csize);
+                i = a.cls * a.stride + (int)(t - (int64_t)r * a.csize);
+                spin_features<W, MAXD>(words + (int64_t)r * a.n, i, a.n, a.P, a.maxdeg, nbr, cpl, __ldg(field + i), a.beta,
+                                 a.jp, x, de);
+            }
+            // one 16-byte core-matrix row each: features 0..7 of the current and the flipped world-line
+            uint32_t pc[4], pf[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int c = 2 * e;
+                const float f0 = (c == 2 || c == 4) ? -x[c] : x[c];
+                const float f1 = (c + 1 == 5) ? -x[c + 1] : x[c + 1];
+                pc[e] = bf16x2_bits(x[c], x[c + 1]);
+                pf[e] = bf16x2_bits(f0, f1);
+            }
+            *reinterpret_cast<uint4*>(sX + tc::tile_off(tid, 0, kK1)) = make_uint4(pc[0], pc[1], pc[2], pc[3]);
+            *reinterpret_cast<uint4*>(sXf + tc::tile_off(tid, 0, kK1)) = make_uint4(pf[0], pf[1], pf[2], pf[3]);
+        }
+        // layer 1
+        tc::fence_async_shared();
+        tc::fence_before_sync();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after_sync();
+            const uint64_t bd = tc::smem_desc(tc::smem_addr(sW1), 128, kK1 * 16);
+            tc::mma_bf16(tmem, tc::smem_desc(tc::smem_addr(sX), 128, kK1 * 16), bd, idesc, 0u);
+            tc::mma_bf16(tmem + kLd, tc::smem_desc(tc::smem_addr(sXf), 128, kK1 * 16), bd, idesc, 0u);
+            tc::mma_commit(tc::smem_addr(mbar));
+        }
+        if (!tc::mbar_wait(tc::smem_addr(mbar), phase, kMmaWait)) { ok = false; break; }
+        phase ^= 1u;
+        tc::fence_after_sync();
+#pragma unroll 1
+        for (int c0 = 0; c0 < 2 * kLd; c0 += 32) {
+            float v[32];
+            tc::tmem_ld32(tlane + (uint32_t)c0, v);
+            unsigned char* dst = c0 < kLd ? sH : sHf;
+            const int cb = c0 & (kLd - 1);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                uint32_t pk[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int j = 8 * q + 2 * e;
+                    pk[e] = bf16x2_bits(fmaxf(__fadd_rn(v[j], sb1[cb + j]), 0.0f),
+                                        fmaxf(__fadd_rn(v[j + 1], sb1[cb + j + 1]), 0.0f));
+                }
+                *reinterpret_cast<uint4*>(dst + tc::tile_off(tid, cb + 8 * q, kLd)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            }
+        }
+        // layer 2
+        tc::fence_async_shared();
+        tc::fence_before_sync();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after_sync();
+#pragma unroll
+            for (int st = 0; st < kLd / 16; ++st) {
+                const uint64_t bd = tc::smem_desc(tc::smem_addr(sW2) + st * 256, 128, kLd * 16);
+                tc::mma_bf16(tmem, tc::smem_desc(tc::smem_addr(sH) + st * 256, 128, kLd * 16), bd, idesc,
+                             st > 0 ? 1u : 0u);
+                tc::mma_bf16(tmem + kLd, tc::smem_desc(tc::smem_addr(sHf) + st * 256, 128, kLd * 16), bd, idesc,
+                             st > 0 ? 1u : 0u);
+            }
+            tc::mma_commit(tc::smem_addr(mbar));
+        }
+        if (!tc::mbar_wait(tc::smem_addr(mbar), phase, kMmaWait)) { ok = false; break; }
+        phase ^= 1u;
+        tc::fence_after_sync();
+        float lg[2];
+#pragma unroll 1
+        for (int half = 0; half < 2; ++half) {
+            float acc = a.b3;
+#pragma unroll 1
+            for (int c0 = 0; c0 < kLd; c0 += 32) {
+                float v[32];
+                tc::tmem_ld32(tlane + (uint32_t)(half * kLd + c0), v);
+#pragma unroll
+                for (int j = 0; j < 32; ++j) acc = __fmaf_rn(fmaxf(__fadd_rn(v[j], sb2[c0 + j]), 0.0f), sw3[c0 + j], acc);
+            }
+            lg[half] = acc;
+        }
+        // MH decision: uniforms Philox(ctr = {i, move, replica, 3 << 24 | cls}) words 0 and 1
+        bool proposed = false, accepted = false;
+        if (valid) {
+            if (logit_out) {
+                logit_out[t] = lg[0];
+                logit_out[M + t] = lg[1];
+            }
+            const pq_u32x4 u = pq_philox(
+                pq_u32x4{(uint32_t)i, a.move, a.replica_base + (uint32_t)r, (3u << 24) | (uint32_t)a.cls}, a.key0,
+                a.key1);
+            const float q = sigmoid_clamped(lg[0], a.qmin), qf = sigmoid_clamped(lg[1], a.qmin);
+            proposed = pq_u01(u.x) < q;
+            if (proposed) {
+                const float lr = -a.beta * de + logf(qf) - logf(q);
+                accepted = lr >= 0.0f || pq_u01(u.y) < expf(lr);
+                if (accepted) words[(int64_t)r * a.n + i] ^= mask;
+            }
+        }
+        const unsigned bp = __ballot_sync(0xffffffffu, proposed), ba = __ballot_sync(0xffffffffu, accepted);
+        if (counters && lane == 0) {
+            if (bp) atomicAdd(counters, (unsigned long long)__popc(bp));
+            if (ba) atomicAdd(counters + 1, (unsigned long long)__popc(ba));
+        }
+        tc::fence_before_sync();
+    }
+    if (!ok) {
+        pq_set_status(status, PQ_ERR_TIMEOUT);
+        // the MMAs of the phase that timed out get one more bounded chance to land before TMEM is freed
+        tc::mbar_wait(tc::smem_addr(mbar), phase, kMmaWait);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(tmem, 2 * kLd);
+}
+
+// Uniform world-line move of every spin of class `cls` (the plain form the
+// learned one is judged against): proposed always, accepted with
+// min(1, exp(-beta dE)), dE = 2 worldline_align; the same uniforms and the same
+// decision arithmetic as the learned move with q = q' = 1.
+template <typename W, int MAXD>
+__global__ void uniform_move_kernel(W* __restrict__ words, const int32_t* __restrict__ nbr,
+                                    const float* __restrict__ cpl, const float* __restrict__ field, MoveArgs a,
+                                    unsigned long long* __restrict__ counters) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t M = (int64_t)a.R * a.csize;
+    bool accepted = false;
+    if (t < M) {
+        const int r = (int)(t / a.csize);
+        const int i = a.cls * a.stride + (int)(t - (int64_t)r * a.csize);
+        const W* wr = words + (int64_t)r * a.n;
+        const W mask = slice_mask<W>(a.P);
+        W nbw[MAXD];
+        float J[MAXD];
+        load_neighbourhood<W, MAXD>(wr, i, a.n, a.maxdeg, nbr, cpl, nbw, J);
+        const W wi = wr[i] & mask;
+        const float de = __fmul_rn(2.0f, worldline_align<W, MAXD>(wi, nbw, J, a.maxdeg, __ldg(field + i), a.P, mask));
+        const pq_u32x4 u = pq_philox(
+            pq_u32x4{(uint32_t)i, a.move, a.replica_base + (uint32_t)r, (3u << 24) | (uint32_t)a.cls}, a.key0, a.key1);
+        const float lr = -a.beta * de;
+        accepted = lr >= 0.0f || pq_u01(u.y) < expf(lr);
+        if (accepted) words[(int64_t)r * a.n + i] ^= mask;
+    }
+    const unsigned ba = __ballot_sync(0xffffffffu, accepted);
+    const unsigned bp = __ballot_sync(0xffffffffu, t < M);
+    if (counters && (threadIdx.x & 31) == 0) {
+        if (bp) atomicAdd(counters, (unsigned long long)__popc(bp));
+        if (ba) atomicAdd(counters + 1, (unsigned long long)__popc(ba));
+    }
+}
+
+template <typename W, int MAXD>
+int move_grid(int64_t ntiles) {
+    static int occ = 0, nsm = 0;
+    if (!occ) {
+        auto kernel = learned_move_kernel<W, MAXD>;
+        int dev = 0;
+        PQ_CUDA_TRY(cudaGetDevice(&dev));
+        PQ_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        PQ_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemMove));
+        PQ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, 128, kSmemMove));
+        // four CTAs of 128 TMEM columns fill an SM's 512
+        occ = occ < 1 ? 1 : (occ > 4 ? 4 : occ);
+    }
+    const int64_t g = (int64_t)nsm * occ;
+    return (int)(ntiles < g ? ntiles : g);
+}
+
 inline unsigned blocks_for(int64_t n, int b = 256) { return (unsigned)((n + b - 1) / b); }
+
+// Runs the statement given with W = the word type and D = the unrolled neighbour count (4 or 16).
+#define PQ_WORD_DEG_DISPATCH(word_bits, maxdeg, ...)                  \
+    if ((word_bits) == 32 && (maxdeg) <= 4) {                          \
+        using W = uint32_t;                                            \
+        constexpr int D = 4;                                           \
+        __VA_ARGS__;                                                   \
+    } else if ((word_bits) == 32) {                                    \
+        using W = uint32_t;                                            \
+        constexpr int D = 16;                                          \
+        __VA_ARGS__;                                                   \
+    } else if ((word_bits) == 64 && (maxdeg) <= 4) {                   \
+        using W = uint64_t;                                            \
+        constexpr int D = 4;                                           \
+        __VA_ARGS__;                                                   \
+    } else if ((word_bits) == 64) {                                    \
+        using W = uint64_t;                                            \
+        constexpr int D = 16;                                          \
+        __VA_ARGS__;                                                   \
+    } else {                                                           \
+        return PQ_ERR_INVALID_ARG;                                     \
+    }
 
 }  // namespace
 
@@ -262,16 +611,10 @@ int pq_mlp_features(const void* words, int word_bits, int n, int P, int R, int m
     const int64_t M = (int64_t)R * csize;
     if (M == 0) return PQ_OK;
     cudaStream_t st = (cudaStream_t)stream;
-    if (word_bits == 32)
-        features_kernel<uint32_t><<<blocks_for(M), 256, 0, st>>>((const uint32_t*)words, n, P, R, maxdeg, nbr, cpl,
-                                                                 field, cls, stride, csize, beta, jp,
-                                                                 (__nv_bfloat16*)X, dE, Mpad);
-    else if (word_bits == 64)
-        features_kernel<uint64_t><<<blocks_for(M), 256, 0, st>>>((const uint64_t*)words, n, P, R, maxdeg, nbr, cpl,
-                                                                 field, cls, stride, csize, beta, jp,
-                                                                 (__nv_bfloat16*)X, dE, Mpad);
-    else
-        return PQ_ERR_INVALID_ARG;
+    PQ_WORD_DEG_DISPATCH(word_bits, maxdeg,
+                         (features_kernel<W, D><<<blocks_for(M), 256, 0, st>>>((const W*)words, n, P, R, maxdeg, nbr,
+                                                                               cpl, field, cls, stride, csize, beta,
+                                                                               jp, (__nv_bfloat16*)X, dE, Mpad)));
     return pq_launch_status();
 }
 
@@ -310,6 +653,76 @@ int pq_mlp_propose(void* words, int word_bits, int n, int P, int R, int cls, int
     else
         return PQ_ERR_INVALID_ARG;
     return pq_launch_status();
+}
+
+int pq_mlp_learned_move(void* words, int word_bits, int n, int P, int R, int maxdeg, const int32_t* nbr,
+                        const float* cpl, const float* field, int cls, int stride, int csize, float beta, float jp,
+                        const void* W1, const void* W2, const float* b1, const float* b2, const float* w3, float b3,
+                        float qmin, uint32_t move, uint64_t seed, int replica_base, float* logit_out,
+                        unsigned long long* counters, int32_t* status, void* stream) {
+    if (!words || !nbr || !cpl || !field || !W1 || !W2 || !b1 || !b2 || !w3 || n <= 0 || P < 1 || R <= 0 ||
+        csize < 0 || maxdeg < 0 || maxdeg > 16 || !(qmin > 0.0f) || qmin > 1.0f || ((uintptr_t)W1 & 15) ||
+        ((uintptr_t)W2 & 15) || (word_bits == 32 && P > 32) || P > 64)
+        return PQ_ERR_INVALID_ARG;
+    const int64_t M = (int64_t)R * csize;
+    if (M == 0) return PQ_OK;
+    MoveArgs a{n, P, R, maxdeg, cls, stride, csize, beta, jp, qmin, b3, move, (uint32_t)seed,
+               (uint32_t)(seed >> 32), (uint32_t)replica_base, (M + kTile - 1) / kTile};
+    cudaStream_t st = (cudaStream_t)stream;
+    const __nv_bfloat16* w1 = (const __nv_bfloat16*)W1;
+    const __nv_bfloat16* w2 = (const __nv_bfloat16*)W2;
+    PQ_WORD_DEG_DISPATCH(word_bits, maxdeg, {
+        const int grid = move_grid<W, D>(a.ntiles);
+        if (grid <= 0) return grid;   // a CUDA error, negated
+        learned_move_kernel<W, D><<<grid, 128, kSmemMove, st>>>((W*)words, nbr, cpl, field, w1, w2, b1, b2, w3, a,
+                                                                logit_out, counters, status);
+    });
+    return pq_launch_status();
+}
+
+int pq_worldline_move(void* words, int word_bits, int n, int P, int R, int maxdeg, const int32_t* nbr,
+                      const float* cpl, const float* field, int cls, int stride, int csize, float beta, uint32_t move,
+                      uint64_t seed, int replica_base, unsigned long long* counters, void* stream) {
+    if (!words || !nbr || !cpl || !field || n <= 0 || P < 1 || R <= 0 || csize < 0 || maxdeg < 0 || maxdeg > 16 ||
+        (word_bits == 32 && P > 32) || P > 64)
+        return PQ_ERR_INVALID_ARG;
+    const int64_t M = (int64_t)R * csize;
+    if (M == 0) return PQ_OK;
+    MoveArgs a{n, P, R, maxdeg, cls, stride, csize, beta, 0.0f, 1.0f, 0.0f, move, (uint32_t)seed,
+               (uint32_t)(seed >> 32), (uint32_t)replica_base, 0};
+    cudaStream_t st = (cudaStream_t)stream;
+    PQ_WORD_DEG_DISPATCH(word_bits, maxdeg,
+                         (uniform_move_kernel<W, D><<<blocks_for(M), 256, 0, st>>>((W*)words, nbr, cpl, field, a,
+                                                                                   counters)));
+    return pq_launch_status();
+}
+
+int pq_mlp_learned_pass(void* words, int word_bits, int n, int P, int R, int maxdeg, const int32_t* nbr,
+                        const float* cpl, const float* field, int nclass, int stride, const int32_t* class_size,
+                        float beta, float jp, const void* W1, const void* W2, const float* b1, const float* b2,
+                        const float* w3, float b3, float qmin, uint32_t move, uint64_t seed, int replica_base,
+                        unsigned long long* counters, int32_t* status, void* stream) {
+    if (!class_size || nclass < 0 || nclass > PQ_MAX_CLASSES) return PQ_ERR_INVALID_ARG;
+    for (int c = 0; c < nclass; ++c) {
+        const int rc = pq_mlp_learned_move(words, word_bits, n, P, R, maxdeg, nbr, cpl, field, c, stride, class_size[c],
+                                           beta, jp, W1, W2, b1, b2, w3, b3, qmin, move, seed, replica_base, nullptr,
+                                           counters, status, stream);
+        if (rc != PQ_OK) return rc;
+    }
+    return PQ_OK;
+}
+
+int pq_worldline_pass(void* words, int word_bits, int n, int P, int R, int maxdeg, const int32_t* nbr,
+                      const float* cpl, const float* field, int nclass, int stride, const int32_t* class_size,
+                      float beta, uint32_t move, uint64_t seed, int replica_base, unsigned long long* counters,
+                      void* stream) {
+    if (!class_size || nclass < 0 || nclass > PQ_MAX_CLASSES) return PQ_ERR_INVALID_ARG;
+    for (int c = 0; c < nclass; ++c) {
+        const int rc = pq_worldline_move(words, word_bits, n, P, R, maxdeg, nbr, cpl, field, c, stride, class_size[c],
+                                         beta, move, seed, replica_base, counters, stream);
+        if (rc != PQ_OK) return rc;
+    }
+    return PQ_OK;
 }
 
 int pq_mlp_head_backward(const float* H2, const float* logit, const float* y, const float* w3, int B, void* dH2,

@@ -11,19 +11,25 @@ FP32 (the trained parameters) and used as BF16 copies by the tensor-core GEMMs
   Adam updates the FP32 parameters.
 
 ``learned_pass`` runs one world-line move per spin with the network choosing
-which spins to try.  Update classes are visited in order; for every spin of a
+which spins to try; by default every class is one launch of the fused kernel
+(features, both layers as tcgen05 MMAs with TMEM accumulators, head and MH
+decision without leaving the SM), the unfused path (feature kernel, two GEMMs,
+head, propose) giving the same moves.  Update classes are visited in order; for every spin of a
 class, the features of its current world-line and of the flipped one are scored,
 the flip is proposed with q = clamp(sigmoid(logit), qmin, 1) and accepted with
 min(1, exp(-beta dE) q'/q).  Spins of one class share no coupling, so a flip
 never changes another class member's features during the phase: the reverse
 proposal probability q' is exactly what the network would give in the new
 state, and detailed balance holds.  ``uniform_pass`` is the same move with
-q = 1 (every spin tried), the plain form the learned one is judged against.
+q = 1 (every spin tried), the plain form the learned one is judged against;
+its default kernel computes only the flip cost.
 
 Training data: ``record_moves`` scores the moves the plain method tries at
 snapshots of plain anneals -- features and their Metropolis acceptance
 probabilities min(1, exp(-beta dE)) -- and ``train`` fits the network to them.
 """
+import ctypes
+
 import numpy as np
 import torch
 
@@ -65,6 +71,7 @@ class ProposalMLP:
         self.W1b = W1p.to(torch.bfloat16).contiguous()
         self.W2b = self.params["W2"].to(torch.bfloat16).contiguous()
         self.W2Tb = self.params["W2"].t().contiguous().to(torch.bfloat16)
+        self.b3_host = float(self.params["b3"][0].item())
 
     def state_dict(self):
         return {k: v.detach().cpu().numpy().copy() for k, v in self.params.items()}
@@ -171,11 +178,53 @@ def _features(problem, words, P, cls, beta, jp, X, dE, Mpad):
         _device.stream_handle()), "pq_mlp_features")
 
 
-def learned_pass(problem, words, P, mlp, beta, jp, seed, move, qmin=0.05, counters=None, uniform=False):
-    """One world-line move per spin, class by class (see module docstring); in place on ``words``."""
+_status = {}
+
+
+def _status_buffer(dev):
+    buf = _status.get(dev)
+    if buf is None:
+        buf = _status[dev] = torch.zeros(1, dtype=torch.int32, device=dev)
+    return buf
+
+
+def check_status(device=None):
+    """Raise if a fused learned move gave up on a tensor-core wait since the last check."""
+    buf = _status_buffer(device or _device.device())
+    code = int(buf.item())
+    if code:
+        buf.zero_()
+        raise _native.PiqmcError(code, "pq_mlp_learned_move")
+
+
+def learned_pass(problem, words, P, mlp, beta, jp, seed, move, qmin=0.05, counters=None, uniform=False, fused=True,
+                 check=True):
+    """One world-line move per spin, class by class (see module docstring); in place on ``words``.
+
+    ``check=False`` leaves the device status unread (no host sync); ``check_status`` reads it later.
+    """
     R = words.shape[0]
     bits = 32 if P <= 32 else 64
     lib = _native.lib()
+    st = _device.stream_handle()
+    key = int(seed) & 0xFFFFFFFFFFFFFFFF
+    mv = int(move) & 0xFFFFFFFF
+    if fused:
+        sizes = problem.class_size.ctypes.data_as(ctypes.c_void_p)
+        args = (_device.ptr(words), bits, problem.nslots, P, R, problem.maxdeg, _device.ptr(problem.nbr),
+                _device.ptr(problem.cpl), _device.ptr(problem.field), problem.nclass, problem.class_stride, sizes)
+        if uniform:
+            _native.check(lib.pq_worldline_pass(*args, float(beta), mv, key, 0, _device.ptr(counters), st),
+                          "pq_worldline_pass")
+            return
+        status = _status_buffer(words.device)
+        _native.check(lib.pq_mlp_learned_pass(
+            *args, float(beta), float(jp), _device.ptr(mlp.W1b), _device.ptr(mlp.W2b), _device.ptr(mlp.params["b1"]),
+            _device.ptr(mlp.params["b2"]), _device.ptr(mlp.params["w3"]), mlp.b3_host, float(qmin), mv, key, 0,
+            _device.ptr(counters), _device.ptr(status), st), "pq_mlp_learned_pass")
+        if check:
+            check_status(words.device)
+        return
     for cls in range(problem.nclass):
         csize = int(problem.class_size[cls])
         M = R * csize
@@ -188,12 +237,11 @@ def learned_pass(problem, words, P, mlp, beta, jp, seed, move, qmin=0.05, counte
             logit = mlp.forward(X)
         _native.check(lib.pq_mlp_propose(
             _device.ptr(words), bits, problem.nslots, P, R, cls, problem.class_stride, csize, _device.ptr(logit),
-            _device.ptr(dE), Mpad, float(qmin), float(beta), int(move) & 0xFFFFFFFF, int(seed) & 0xFFFFFFFFFFFFFFFF,
-            0, _device.ptr(counters), _device.stream_handle()), "pq_mlp_propose")
+            _device.ptr(dE), Mpad, float(qmin), float(beta), mv, key, 0, _device.ptr(counters), st), "pq_mlp_propose")
 
 
-def uniform_pass(problem, words, P, beta, jp, seed, move, counters=None):
-    learned_pass(problem, words, P, None, beta, jp, seed, move, counters=counters, uniform=True)
+def uniform_pass(problem, words, P, beta, jp, seed, move, counters=None, fused=True):
+    learned_pass(problem, words, P, None, beta, jp, seed, move, counters=counters, uniform=True, fused=fused)
 
 
 def record_moves(problem, words, P, beta, jp, max_rows=None):

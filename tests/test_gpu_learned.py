@@ -39,6 +39,125 @@ def test_forward_and_gradients_match_cpu_oracle():
         assert rel < 1e-2, (k, rel)
 
 
+def _random_mlp(seed):
+    from piqmc import learned
+    mlp = learned.ProposalMLP(seed=seed)
+    g = np.random.default_rng(seed)
+    with torch.no_grad():
+        for k in ("b1", "b2", "b3"):
+            mlp.params[k].copy_(torch.tensor(g.normal(0, 0.3, mlp.params[k].shape), dtype=torch.float32))
+    mlp.refresh()
+    return mlp
+
+
+def _feature_problem(kind, seed):
+    """A periodic 10x10 lattice with fields (degree 4) or a random graph with degrees up to 9."""
+    import scipy.sparse as sps
+    from piqmc import fast, tools
+    g = np.random.default_rng(seed)
+    if kind == "lattice":
+        J = lattice(10, True, g, dist=lambda r: r.normal(), fields=lambda r: r.normal(0, 0.3))
+        n = 100
+    else:
+        n = 90
+        J = sps.dok_matrix((n, n))
+        for a in range(n):
+            for b in g.choice(n, size=3, replace=False):
+                if a != b:
+                    J[min(a, b), max(a, b)] = float(np.float32(g.uniform(-1.5, 1.5)))
+            J[a, a] = float(np.float32(g.normal(0, 0.2)))
+    return fast.Problem(tools.GenerateNeighbors(n, J, 12))
+
+
+def _random_words(prob, P, R, seed):
+    g = np.random.default_rng(seed)
+    if P <= 32:
+        w = (g.integers(0, 2 ** 32, size=(R, prob.nslots), dtype=np.uint64) & ((1 << P) - 1)).astype(np.uint32)
+        return torch.from_numpy(w.view(np.int32)).cuda()
+    return torch.from_numpy(g.integers(0, 2 ** 64, size=(R, prob.nslots), dtype=np.uint64).view(np.int64)).cuda()
+
+
+@pytest.mark.parametrize("kind", ["lattice", "graph"])
+@pytest.mark.parametrize("P", [20, 64])
+def test_features_match_oracle_bit_exact(kind, P):
+    from piqmc import learned
+    prob = _feature_problem(kind, 3)
+    R, beta, jp = 6, 20.0, 0.37
+    w = _random_words(prob, P, R, 4)
+    D = prob.maxdeg
+    for cls in range(prob.nclass):
+        csize = int(prob.class_size[cls])
+        M = R * csize
+        Mpad = (M + 127) // 128 * 128
+        X = torch.zeros((2 * Mpad, 64), dtype=torch.bfloat16, device="cuda")
+        dE = torch.empty(Mpad, dtype=torch.float32, device="cuda")
+        learned._features(prob, w, P, cls, beta, jp, X, dE, Mpad)
+        Xo, dEo = mlp_oracle.features(w.cpu().numpy(), P, prob.nbr_host[:D], prob.cpl_host[:D], prob.field_host,
+                                      cls, prob.class_stride, csize, beta, jp)
+        got = X[:M, :8].float().cpu().numpy()
+        assert np.array_equal(got, mlp_oracle.bf16(Xo).astype(np.float32)), (cls, np.abs(got - Xo).max())
+        flipped = Xo.copy()
+        flipped[:, [2, 4, 5]] *= -1
+        assert np.array_equal(X[Mpad:Mpad + M, :8].float().cpu().numpy(), mlp_oracle.bf16(flipped).astype(np.float32))
+        assert np.array_equal(dE[:M].cpu().numpy(), dEo), cls
+
+
+@pytest.mark.parametrize("P", [20, 64])
+def test_fused_learned_move_matches_unfused_path(P):
+    """One kernel per class (features, tcgen05 layers, head, MH) against features + GEMMs + head + propose."""
+    from piqmc import _device, _native, learned
+    prob = _feature_problem("lattice", 5)
+    mlp = _random_mlp(7)
+    R, beta, jp = 24, 4.0, 0.2
+    w0 = _random_words(prob, P, R, 6)
+    # logits of one class against the unfused forward
+    cls, csize = 0, int(prob.class_size[0])
+    M = R * csize
+    Mpad = (M + 127) // 128 * 128
+    X = torch.zeros((2 * Mpad, 64), dtype=torch.bfloat16, device="cuda")
+    dE = torch.empty(Mpad, dtype=torch.float32, device="cuda")
+    learned._features(prob, w0, P, cls, beta, jp, X, dE, Mpad)
+    ref = mlp.forward(X)
+    logits = torch.full((2, M), float("nan"), dtype=torch.float32, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    wt = w0.clone()
+    _native.check(_native.lib().pq_mlp_learned_move(
+        _device.ptr(wt), 32 if P <= 32 else 64, prob.nslots, P, R, prob.maxdeg, _device.ptr(prob.nbr),
+        _device.ptr(prob.cpl), _device.ptr(prob.field), cls, prob.class_stride, csize, beta, jp,
+        _device.ptr(mlp.W1b), _device.ptr(mlp.W2b), _device.ptr(mlp.params["b1"]), _device.ptr(mlp.params["b2"]),
+        _device.ptr(mlp.params["w3"]), mlp.b3_host, 0.05, 0, 11, 0, _device.ptr(logits), None, _device.ptr(status),
+        _device.stream_handle()), "pq_mlp_learned_move")
+    assert int(status.item()) == 0
+    assert torch.equal(logits[0], ref[:M]) and torch.equal(logits[1], ref[Mpad:Mpad + M])
+    # whole passes, every class
+    out = {}
+    for fused in (True, False):
+        w = w0.clone()
+        cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
+        for move in range(3):
+            learned.learned_pass(prob, w, P, mlp, beta, jp, seed=11, move=move, counters=cnt, fused=fused)
+        out[fused] = (w, cnt.cpu().numpy())
+    assert torch.equal(out[True][0], out[False][0])
+    assert np.array_equal(out[True][1], out[False][1]) and out[True][1][1] > 0
+
+
+@pytest.mark.parametrize("P", [20, 64])
+def test_uniform_move_kernel_matches_q1_path(P):
+    from piqmc import learned
+    prob = _feature_problem("graph", 8)
+    R, beta = 16, 1.5
+    w0 = _random_words(prob, P, R, 9)
+    out = {}
+    for fused in (True, False):
+        w = w0.clone()
+        cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
+        for move in range(3):
+            learned.uniform_pass(prob, w, P, beta, 0.1, seed=12, move=move, counters=cnt, fused=fused)
+        out[fused] = (w, cnt.cpu().numpy())
+    assert torch.equal(out[True][0], out[False][0])
+    assert np.array_equal(out[True][1], out[False][1]) and out[True][1][1] > 0
+
+
 def _problem(L, seed):
     from piqmc import fast, tools
     J = lattice(L, True, np.random.default_rng(seed), dist=lambda r: r.normal())
