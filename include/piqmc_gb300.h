@@ -85,6 +85,13 @@ int pq_sa_sparse_reforder(int8_t* spins, const int32_t* nb_idx, const float* nb_
                           const int32_t* perms, const int32_t* rands, int64_t rand_stride,
                           int64_t* rand_used, int32_t* status, void* stream);
 
+/* Replaces sa.Anneal_dense (reference piqmc/sa.pyx:126-187): dense float64 J
+ * [n][n] (upper triangle + diagonal read), temps[g] = (float)sched[g], spins int8
+ * [R][n], perms int32 [R][nsched*mcsteps][n]. */
+int pq_sa_dense_reforder(int8_t* spins, const double* J, int n, int R, const float* temps, int nsched, int mcsteps,
+                         const int32_t* perms, const int32_t* rands, int64_t rand_stride, int64_t* rand_used,
+                         int32_t* status, void* stream);
+
 /* The same three sweeps with the exp-parity hooks.  ov_x/ov_y (device, may be
  * NULL): sorted FP32 bit patterns x and the host libm's exp((double)x), used in
  * place of the device exp for "close calls" (exp(x) within ~4.5 ulp of the
@@ -111,6 +118,20 @@ int pq_sa_sparse_reforder_ex(int8_t* spins, const int32_t* nb_idx, const float* 
                              int64_t* rand_used, int flags, const uint32_t* ov_x, const double* ov_y, int ov_n,
                              uint32_t* close_x, double* close_y, int close_cap, int* close_cnt,
                              int32_t* status, void* stream);
+
+int pq_sa_dense_reforder_ex(int8_t* spins, const double* J, int n, int R, const float* temps, int nsched,
+                            int mcsteps, const int32_t* perms, const int32_t* rands, int64_t rand_stride,
+                            int64_t* rand_used, const uint32_t* ov_x, const double* ov_y, int ov_n,
+                            uint32_t* close_x, double* close_y, int close_cap, int* close_cnt, int32_t* status,
+                            void* stream);
+/* Replaces sa.Anneal_bipartite (reference piqmc/sa.pyx:411-500): spins int8
+ * [R][nl + nr] (left then right), J float64 [nl][nr], biases float64; spins are
+ * visited in index order (the reference draws no permutation). */
+int pq_sa_bipartite_reforder_ex(int8_t* spins, const double* J, int nl, int nr, const double* lbias,
+                                const double* rbias, int R, const float* temps, int nsched, int mcsteps,
+                                const int32_t* rands, int64_t rand_stride, int64_t* rand_used, const uint32_t* ov_x,
+                                const double* ov_y, int ov_n, uint32_t* close_x, double* close_y, int close_cap,
+                                int* close_cnt, int32_t* status, void* stream);
 
 /* Device exp((double)x) exactly as the reference-order kernels evaluate it
  * (diagnostic for the libm parity scan): y[i] = exp(x[i]), and the range form

@@ -61,6 +61,10 @@ def lib():
         L.orc_qa_dense.restype = i64
         L.orc_sa_sparse.argtypes = [i32, i32, P, P, P, i32, i32, P, P, i64, P]
         L.orc_sa_sparse.restype = i64
+        L.orc_sa_dense.argtypes = [i32, P, P, i32, i32, P, P, i64, P]
+        L.orc_sa_dense.restype = i64
+        L.orc_sa_bipartite.argtypes = [i32, i32, P, P, P, P, i32, i32, P, i64, P, P]
+        L.orc_sa_bipartite.restype = i64
         L.orc_jperp.argtypes = [P, i32, i32, f32, P]
         L.orc_jperp.restype = None
         L.orc_libc_rand.argtypes = [P, i64]
@@ -185,6 +189,29 @@ def sa_sparse(spins, nbs, sched, mcsteps, perms, rands):
     rands = np.ascontiguousarray(rands, dtype=np.int32)
     return lib().orc_sa_sparse(n, idx.shape[1], _p(idx), _p(jv), _p(temps), len(temps), mcsteps,
                                _p(perms), _p(rands), len(rands), _p(spins))
+
+
+def sa_dense(spins, J, sched, mcsteps, perms, rands):
+    """sa.Anneal_dense of one int8 spin vector in place; returns the rand() count consumed."""
+    n = spins.shape[0]
+    assert spins.dtype == np.int8 and spins.flags.c_contiguous
+    J = np.ascontiguousarray(J, dtype=np.float64)
+    temps = np.ascontiguousarray(np.asarray(sched, dtype=np.float64).astype(np.float32))
+    perms = np.ascontiguousarray(perms, dtype=np.int64)
+    rands = np.ascontiguousarray(rands, dtype=np.int32)
+    return lib().orc_sa_dense(n, _p(J), _p(temps), len(temps), mcsteps, _p(perms), _p(rands), len(rands), _p(spins))
+
+
+def sa_bipartite(lv, rv, J, lbias, rbias, sched, mcsteps, rands):
+    """sa.Anneal_bipartite of int8 left / right spin vectors in place; returns the rand() count consumed."""
+    assert lv.dtype == np.int8 and rv.dtype == np.int8
+    J = np.ascontiguousarray(J, dtype=np.float64)
+    lb = np.ascontiguousarray(lbias, dtype=np.float64)
+    rb = np.ascontiguousarray(rbias, dtype=np.float64)
+    temps = np.ascontiguousarray(np.asarray(sched, dtype=np.float64).astype(np.float32))
+    rands = np.ascontiguousarray(rands, dtype=np.int32)
+    return lib().orc_sa_bipartite(lv.shape[0], rv.shape[0], _p(J), _p(lb), _p(rb), _p(temps), len(temps), mcsteps,
+                                  _p(rands), len(rands), _p(lv), _p(rv))
 
 
 # ----------------------------------------------------------------------------------------

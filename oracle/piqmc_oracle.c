@@ -158,6 +158,75 @@ int64_t orc_sa_sparse(int n, int maxnb, const int32_t* nb_idx, const float* nb_j
 /* J-perp schedule of reference piqmc/qmc.pyx:95 in the generated C's types
  * (piqmc/qmc.c:2063-2075): slices*temp is an FP32 product, the quotient and
  * log/tanh are double, the result is stored to FP32. */
+/* sa.Anneal_dense, reference piqmc/sa.pyx:126-187: dense float64 J, upper
+ * triangle for pairs and the diagonal as field (:170-179), ediff reset per spin
+ * (:186), deterministic accept on ediff > 0 (:181). */
+int64_t orc_sa_dense(int n, const double* J, const float* temps, int nsched, int mcsteps, const int64_t* perms,
+                     const int32_t* rands, int64_t nrand, int8_t* s) {
+    int64_t used = 0;
+    int exhausted = 0;
+    for (int g = 0; g < nsched; ++g) {
+        const float temp = temps[g];
+        for (int step = 0; step < mcsteps; ++step) {
+            const int64_t* perm = perms + (int64_t)(g * mcsteps + step) * n;
+            for (int t = 0; t < n; ++t) {
+                const int i = (int)perm[t];
+                const double si = (double)s[i];
+                float ediff = 0.0f;
+                for (int j = 0; j < n; ++j) {
+                    if (j == i) {
+                        ediff = acc(ediff, -2.0 * si * J[(int64_t)i * n + i]);
+                    } else {
+                        const double jv = i < j ? J[(int64_t)i * n + j] : J[(int64_t)j * n + i];
+                        ediff = acc(ediff, -2.0 * si * (jv * (double)s[j]));
+                    }
+                }
+                if (metropolis(ediff, temp, 0, rands, nrand, &used, &exhausted)) s[i] = (int8_t)-s[i];
+                if (exhausted) return -1;
+            }
+        }
+    }
+    return used;
+}
+
+/* sa.Anneal_bipartite, reference piqmc/sa.pyx:411-500: left spins in index
+ * order then right spins; ediff -= 2 l_i J_ij r_j + lb_i l_i + rb_j r_j over the
+ * other side (:466-468, :478-480), FP64 terms into the FP32 accumulator. */
+int64_t orc_sa_bipartite(int nl, int nr, const double* J, const double* lbias, const double* rbias,
+                         const float* temps, int nsched, int mcsteps, const int32_t* rands, int64_t nrand,
+                         int8_t* lv, int8_t* rv) {
+    int64_t used = 0;
+    int exhausted = 0;
+    for (int g = 0; g < nsched; ++g) {
+        const float temp = temps[g];
+        for (int step = 0; step < mcsteps; ++step) {
+            for (int i = 0; i < nl; ++i) {
+                const double li = (double)lv[i];
+                float ediff = 0.0f;
+                for (int j = 0; j < nr; ++j) {
+                    const double rj = (double)rv[j];
+                    ediff = (float)((double)ediff - (2.0 * li * J[(int64_t)i * nr + j] * rj + lbias[i] * li +
+                                                     rbias[j] * rj));
+                }
+                if (metropolis(ediff, temp, 0, rands, nrand, &used, &exhausted)) lv[i] = (int8_t)-lv[i];
+                if (exhausted) return -1;
+            }
+            for (int i = 0; i < nr; ++i) {
+                const double ri = (double)rv[i];
+                float ediff = 0.0f;
+                for (int j = 0; j < nl; ++j) {
+                    const double lj = (double)lv[j];
+                    ediff = (float)((double)ediff - (2.0 * ri * J[(int64_t)j * nr + i] * lj + lbias[j] * lj +
+                                                     rbias[i] * ri));
+                }
+                if (metropolis(ediff, temp, 0, rands, nrand, &used, &exhausted)) rv[i] = (int8_t)-rv[i];
+                if (exhausted) return -1;
+            }
+        }
+    }
+    return used;
+}
+
 void orc_jperp(const double* sched, int nsched, int P, float temp, float* out) {
     for (int g = 0; g < nsched; ++g) {
         const float pt = (float)P * temp;

@@ -66,7 +66,7 @@ def build(force=False, verbose=False, extra=()):
         objs = list(ex.map(lambda s: _compile(s, force, verbose, list(extra)), srcs))
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
         tmp = LIB + ".tmp%d" % os.getpid()
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcuda"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError("link failed:\n%s%s" % (res.stdout, res.stderr))

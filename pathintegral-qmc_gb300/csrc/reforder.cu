@@ -285,6 +285,91 @@ __global__ void sa_sparse_reforder_kernel(int8_t* __restrict__ spins, const int3
     rand_used[r] = rng.used;
 }
 
+// sa.Anneal_dense (reference piqmc/sa.pyx:126-187): one thread per replica walks
+// the spins in the supplied order; ediff sums every term of the spin's row in the
+// FP32 accumulator (upper triangle for off-diagonal pairs, the diagonal as the
+// field, :170-179), is reset per spin (:186), and the deterministic branch
+// accepts on ediff > 0 (:181).
+__global__ void sa_dense_reforder_kernel(int8_t* __restrict__ spins, const double* __restrict__ J, int n, int R,
+                                         const float* __restrict__ temps, int nsched, int mcsteps,
+                                         const int32_t* __restrict__ perms, const int32_t* __restrict__ rands,
+                                         int64_t rand_stride, int64_t* __restrict__ rand_used, ExpPatch ep,
+                                         int32_t* status) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    int8_t* s = spins + (int64_t)r * n;
+    const int32_t* pr = perms + (int64_t)r * nsched * mcsteps * n;
+    RefRng rng{rands + (int64_t)r * rand_stride, rand_stride, 0, false};
+    for (int g = 0; g < nsched; ++g) {
+        const float temp = temps[g];
+        for (int step = 0; step < mcsteps; ++step) {
+            const int32_t* perm = pr + (int64_t)(g * mcsteps + step) * n;
+            for (int t = 0; t < n; ++t) {
+                const int i = perm[t];
+                if ((unsigned)i >= (unsigned)n) { pq_set_status(status, PQ_ERR_BAD_INDEX); rand_used[r] = -1; return; }
+                const double si = (double)s[i];
+                float ediff = 0.0f;
+                for (int j = 0; j < n; ++j) {
+                    if (j == i) {
+                        ediff = acc(ediff, -2.0 * si * J[(int64_t)i * n + i]);
+                    } else {
+                        const double jv = i < j ? J[(int64_t)i * n + j] : J[(int64_t)j * n + i];
+                        ediff = acc(ediff, -2.0 * si * (jv * (double)s[j]));
+                    }
+                }
+                if (ref_accept(ediff, temp, false, rng, ep, status)) s[i] = (int8_t)-s[i];
+                if (rng.dead) { rand_used[r] = -1; return; }
+            }
+        }
+    }
+    rand_used[r] = rng.used;
+}
+
+// sa.Anneal_bipartite (reference piqmc/sa.pyx:411-500): left spins in index
+// order, then right spins, every step; for left spin i the accumulator takes,
+// for every right spin j, ediff - (2 l_i J_ij r_j + lb_i l_i + rb_j r_j) in FP64
+// rounded to FP32 (:466-468), and symmetrically for right spins (:478-480).
+// spins: int8 [R][nl + nr] (left then right).
+__global__ void sa_bipartite_reforder_kernel(int8_t* __restrict__ spins, const double* __restrict__ J, int nl, int nr,
+                                             const double* __restrict__ lbias, const double* __restrict__ rbias,
+                                             int R, const float* __restrict__ temps, int nsched, int mcsteps,
+                                             const int32_t* __restrict__ rands, int64_t rand_stride,
+                                             int64_t* __restrict__ rand_used, ExpPatch ep, int32_t* status) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    int8_t* lv = spins + (int64_t)r * (nl + nr);
+    int8_t* rv = lv + nl;
+    RefRng rng{rands + (int64_t)r * rand_stride, rand_stride, 0, false};
+    for (int g = 0; g < nsched; ++g) {
+        const float temp = temps[g];
+        for (int step = 0; step < mcsteps; ++step) {
+            for (int i = 0; i < nl; ++i) {
+                const double li = (double)lv[i];
+                float ediff = 0.0f;
+                for (int j = 0; j < nr; ++j) {
+                    const double rj = (double)rv[j];
+                    const double t = 2.0 * li * J[(int64_t)i * nr + j] * rj + lbias[i] * li + rbias[j] * rj;
+                    ediff = __double2float_rn(__dsub_rn((double)ediff, t));
+                }
+                if (ref_accept(ediff, temp, false, rng, ep, status)) lv[i] = (int8_t)-lv[i];
+                if (rng.dead) { rand_used[r] = -1; return; }
+            }
+            for (int i = 0; i < nr; ++i) {
+                const double ri = (double)rv[i];
+                float ediff = 0.0f;
+                for (int j = 0; j < nl; ++j) {
+                    const double lj = (double)lv[j];
+                    const double t = 2.0 * ri * J[(int64_t)j * nr + i] * lj + lbias[j] * lj + rbias[i] * ri;
+                    ediff = __double2float_rn(__dsub_rn((double)ediff, t));
+                }
+                if (ref_accept(ediff, temp, false, rng, ep, status)) rv[i] = (int8_t)-rv[i];
+                if (rng.dead) { rand_used[r] = -1; return; }
+            }
+        }
+    }
+    rand_used[r] = rng.used;
+}
+
 __global__ void exp_probe_kernel(const float* __restrict__ x, double* __restrict__ y, int64_t n) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) y[i] = exp((double)x[i]);
@@ -454,6 +539,43 @@ int pq_sa_sparse_reforder(int8_t* spins, const int32_t* nb_idx, const float* nb_
     return pq_sa_sparse_reforder_ex(spins, nb_idx, nb_j, n, maxnb, R, temps, nsched, mcsteps, perms,
                                     rands, rand_stride, rand_used, 0, nullptr, nullptr, 0, nullptr,
                                     nullptr, 0, nullptr, status, stream);
+}
+
+int pq_sa_dense_reforder_ex(int8_t* spins, const double* J, int n, int R, const float* temps, int nsched,
+                            int mcsteps, const int32_t* perms, const int32_t* rands, int64_t rand_stride,
+                            int64_t* rand_used, const uint32_t* ov_x, const double* ov_y, int ov_n,
+                            uint32_t* close_x, double* close_y, int close_cap, int* close_cnt, int32_t* status,
+                            void* stream) {
+    int st = check_common(n, 1, R, nsched, mcsteps, 1.0f);
+    if (st) return st;
+    if (!spins || !J || !temps || !rand_used || (nsched * mcsteps > 0 && !perms)) return PQ_ERR_INVALID_ARG;
+    if (R == 0) return PQ_OK;
+    ExpPatch ep = make_patch(ov_x, ov_y, ov_n, close_x, close_y, close_cap, close_cnt);
+    sa_dense_reforder_kernel<<<(R + kRefThreads - 1) / kRefThreads, kRefThreads, 0, (cudaStream_t)stream>>>(
+        spins, J, n, R, temps, nsched, mcsteps, perms, rands, rand_stride, rand_used, ep, status);
+    return pq_launch_status();
+}
+
+int pq_sa_dense_reforder(int8_t* spins, const double* J, int n, int R, const float* temps, int nsched, int mcsteps,
+                         const int32_t* perms, const int32_t* rands, int64_t rand_stride, int64_t* rand_used,
+                         int32_t* status, void* stream) {
+    return pq_sa_dense_reforder_ex(spins, J, n, R, temps, nsched, mcsteps, perms, rands, rand_stride, rand_used,
+                                   nullptr, nullptr, 0, nullptr, nullptr, 0, nullptr, status, stream);
+}
+
+int pq_sa_bipartite_reforder_ex(int8_t* spins, const double* J, int nl, int nr, const double* lbias,
+                                const double* rbias, int R, const float* temps, int nsched, int mcsteps,
+                                const int32_t* rands, int64_t rand_stride, int64_t* rand_used, const uint32_t* ov_x,
+                                const double* ov_y, int ov_n, uint32_t* close_x, double* close_y, int close_cap,
+                                int* close_cnt, int32_t* status, void* stream) {
+    if (nl < 0 || nr < 0 || R < 0 || nsched < 0 || mcsteps < 0 || !spins || !temps || !rand_used ||
+        (nl > 0 && nr > 0 && (!J || !lbias || !rbias)))
+        return PQ_ERR_INVALID_ARG;
+    if (R == 0) return PQ_OK;
+    ExpPatch ep = make_patch(ov_x, ov_y, ov_n, close_x, close_y, close_cap, close_cnt);
+    sa_bipartite_reforder_kernel<<<(R + kRefThreads - 1) / kRefThreads, kRefThreads, 0, (cudaStream_t)stream>>>(
+        spins, J, nl, nr, lbias, rbias, R, temps, nsched, mcsteps, rands, rand_stride, rand_used, ep, status);
+    return pq_launch_status();
 }
 
 // Device exp((double)x) exactly as the reference-order kernels evaluate it.

@@ -1,12 +1,27 @@
-// D[M][N] = A[M][K] * B[N][K]^T with BF16 operands and FP32 accumulation on the
-// 5th-generation tensor cores (tcgen05.mma, accumulator in TMEM).
+// D[M][N] = alpha * A[M][K] * B[N][K]^T (+ bias[N]) with BF16 operands and FP32
+// accumulation on the 5th-generation tensor cores.
 //
-// One CTA (4 warps) computes a 128 x BN tile.  For every K chunk of 64 the
-// warps copy the A and B tiles into shared memory in the K-major no-swizzle
-// layout of tc_gemm.cuh, one thread issues four K = 16 MMAs and commits them to
-// an mbarrier, and all threads wait (bounded) before the buffers are reused.
-// The epilogue reads the accumulator with tcgen05.ld (warp w owns rows
-// 32w..32w+31) and applies D = alpha * acc + (bias[col] if bias).
+// One CTA (4 warps) computes a 128 x BN tile through a ring of `kStages` shared-
+// memory stages:
+//  * warp 0 is the TMA producer: per K chunk of 64 it waits for the stage to be
+//    free, arms the stage's "full" mbarrier with the chunk's byte count and issues
+//    one two-dimensional TMA load (cp.async.bulk.tensor) of A (box 64 x 128) and
+//    one of B (box 64 x BN), both with the 128-byte swizzle;
+//  * warp 1 is the MMA issuer: it waits for "full", issues four tcgen05.mma
+//    (K = 16 each, descriptors advanced by 32 B inside the swizzle atom) into the
+//    TMEM accumulator and commits them to the stage's "empty" mbarrier, which hands
+//    the stage back to the producer; a final commit signals "done";
+//  * all four warps then read the accumulator with tcgen05.ld (warp w owns rows
+//    32w..32w+31) and write D = alpha * acc + bias.
+// Stage layout: A then B, each [rows][64] BF16 as the TMA swizzle writes it (rows
+// of 128 B, 8-row atoms of 1024 B), every stage 1024-byte aligned.
+//
+// Every wait is bounded: a wait that gives up sets PQ_ERR_TIMEOUT in `status`,
+// stops the producer and the MMA issuer, waits (bounded) for the copies and MMAs
+// already issued and frees TMEM before returning.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "common.cuh"
 #include "tc_gemm.cuh"
 
@@ -17,20 +32,41 @@ constexpr int KC = 64;
 constexpr long long kWaitIters = 1ll << 24;
 
 template <int BN>
-__global__ void __launch_bounds__(128) tc_gemm_kernel(const __nv_bfloat16* __restrict__ A, int lda,
-                                                      const __nv_bfloat16* __restrict__ B, int ldb,
-                                                      float* __restrict__ D, int ldd, int K, float alpha,
-                                                      const float* __restrict__ bias, int32_t* status) {
-    extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char* sA = smem;
-    unsigned char* sB = smem + BM * KC * 2;
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(sB + BN * KC * 2);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
+struct Cfg {
+    static constexpr int kStages = BN == 256 ? 4 : 6;
+    static constexpr int kStageA = BM * KC * 2;
+    static constexpr int kStageB = BN * KC * 2;
+    static constexpr int kStage = kStageA + kStageB;
+    static constexpr int kBarOff = kStages * kStage;
+    // + 1 KB so the ring can start on a 1024-byte boundary whatever the base alignment
+    static constexpr int kSmem = kBarOff + (2 * kStages + 1) * 8 + 16 + 1024;
+};
+
+template <int BN>
+__global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA,
+                                                         const __grid_constant__ CUtensorMap tmB,
+                                                         float* __restrict__ D, int ldd, int K, float alpha,
+                                                         const float* __restrict__ bias, int32_t* status) {
+    using C = Cfg<BN>;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* smem = smem_raw + ((1024u - (tc::smem_addr(smem_raw) & 1023u)) & 1023u);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + C::kBarOff);
+    uint64_t* empty = full + C::kStages;
+    uint64_t* done = empty + C::kStages;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+    const int nk = K / KC;
+    const uint32_t base = tc::smem_addr(smem);
 
     if (threadIdx.x == 0) {
-        tc::mbar_init(tc::smem_addr(mbar), 1);
+        for (int s = 0; s < C::kStages; ++s) {
+            tc::mbar_init(tc::smem_addr(full + s), 1);
+            tc::mbar_init(tc::smem_addr(empty + s), 1);
+        }
+        tc::mbar_init(tc::smem_addr(done), 1);
+        *abort_flag = 0;
         tc::mbar_fence_init();
     }
     if (warp == 0) {
@@ -41,38 +77,67 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(const __nv_bfloat16* __res
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = *tslot;
-    constexpr uint32_t idesc = tc::idesc_bf16(BM, BN);
 
-    uint32_t phase = 0;
-    bool ok = true;
-    for (int k0 = 0; k0 < K && ok; k0 += KC) {
-        for (int c = threadIdx.x; c < BM * (KC / 8); c += blockDim.x) {
-            const int r = c / (KC / 8), kk = (c % (KC / 8)) * 8;
-            const uint4 v = *reinterpret_cast<const uint4*>(A + (size_t)(m0 + r) * lda + k0 + kk);
-            *reinterpret_cast<uint4*>(sA + tc::tile_off(r, kk, KC)) = v;
-        }
-        for (int c = threadIdx.x; c < BN * (KC / 8); c += blockDim.x) {
-            const int r = c / (KC / 8), kk = (c % (KC / 8)) * 8;
-            const uint4 v = *reinterpret_cast<const uint4*>(B + (size_t)(n0 + r) * ldb + k0 + kk);
-            *reinterpret_cast<uint4*>(sB + tc::tile_off(r, kk, KC)) = v;
-        }
-        tc::fence_async_shared();
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            tc::fence_after_sync();
-#pragma unroll
-            for (int s = 0; s < KC / 16; ++s) {
-                const uint64_t ad = tc::smem_desc(tc::smem_addr(sA) + s * 256, 128, KC * 16);
-                const uint64_t bd = tc::smem_desc(tc::smem_addr(sB) + s * 256, 128, KC * 16);
-                tc::mma_bf16(tmem, ad, bd, idesc, (k0 > 0 || s > 0) ? 1u : 0u);
+    if (warp == 0) {
+        // TMA producer
+        int issued = 0;
+        for (int c = 0; c < nk; ++c) {
+            const int s = c % C::kStages;
+            const uint32_t round = (uint32_t)(c / C::kStages);
+            if (c >= C::kStages && !tc::mbar_wait(tc::smem_addr(empty + s), (round - 1) & 1u, kWaitIters)) {
+                if (lane == 0) { *abort_flag = 1; pq_set_status(status, PQ_ERR_TIMEOUT); }
+                break;
             }
-            tc::mma_commit(tc::smem_addr(mbar));
+            if (*abort_flag) break;
+            if (lane == 0) {
+                const uint32_t sa = base + s * C::kStage, sb = sa + C::kStageA, fb = tc::smem_addr(full + s);
+                tc::mbar_arrive_expect_tx(fb, C::kStage);
+                tc::tma_load_2d(sa, &tmA, c * KC, m0, fb);
+                tc::tma_load_2d(sb, &tmB, c * KC, n0, fb);
+            }
+            issued = c + 1;
+            __syncwarp();
         }
-        if (!tc::mbar_wait(tc::smem_addr(mbar), phase, kWaitIters)) ok = false;
-        phase ^= 1u;
-        tc::fence_after_sync();
+        if (*abort_flag && lane == 0) {
+            // copies already issued land before the CTA lets go of its shared memory
+            for (int c = issued - C::kStages < 0 ? 0 : issued - C::kStages; c < issued; ++c)
+                tc::mbar_wait(tc::smem_addr(full + c % C::kStages), (uint32_t)(c / C::kStages) & 1u, kWaitIters);
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        // MMA issuer
+        constexpr uint32_t idesc = tc::idesc_bf16(BM, BN);
+        for (int c = 0; c < nk; ++c) {
+            const int s = c % C::kStages;
+            const uint32_t round = (uint32_t)(c / C::kStages);
+            if (!tc::mbar_wait(tc::smem_addr(full + s), round & 1u, kWaitIters)) {
+                if (lane == 0) { *abort_flag = 1; pq_set_status(status, PQ_ERR_TIMEOUT); }
+                break;
+            }
+            if (*abort_flag) break;
+            tc::fence_after_sync();
+            if (lane == 0) {
+                const uint32_t sa = base + s * C::kStage, sb = sa + C::kStageA;
+#pragma unroll
+                for (int kk = 0; kk < KC / 16; ++kk) {
+                    const uint64_t ad = tc::smem_desc_sw128(sa + 32 * kk);
+                    const uint64_t bd = tc::smem_desc_sw128(sb + 32 * kk);
+                    tc::mma_bf16(tmem, ad, bd, idesc, (c > 0 || kk > 0) ? 1u : 0u);
+                }
+                tc::mma_commit(tc::smem_addr(empty + s));
+            }
+            __syncwarp();
+        }
+        // every MMA issued above completes before "done" (also on the abort path)
+        if (lane == 0) tc::mma_commit(tc::smem_addr(done));
+        __syncwarp();
     }
-    if (ok) {
+
+    const bool waited = tc::mbar_wait(tc::smem_addr(done), 0u, kWaitIters);
+    tc::fence_after_sync();
+    __syncthreads();
+    if (!waited && threadIdx.x == 0) pq_set_status(status, PQ_ERR_TIMEOUT);
+    if (waited && !*abort_flag && nk > 0) {
         const int row = m0 + 32 * warp + lane;
 #pragma unroll 1
         for (int c0 = 0; c0 < BN; c0 += 32) {
@@ -89,10 +154,6 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(const __nv_bfloat16* __res
                 *reinterpret_cast<float4*>(dst + j) = o;
             }
         }
-    } else {
-        pq_set_status(status, PQ_ERR_TIMEOUT);
-        // give the MMAs in flight one more bounded chance to land before freeing TMEM
-        tc::mbar_wait(tc::smem_addr(mbar), phase ^ 1u, kWaitIters);
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -100,21 +161,44 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(const __nv_bfloat16* __res
     if (warp == 0) tc::tmem_dealloc(tmem, BN);
 }
 
+// Row-major BF16 [rows][ld] matrix of which the first `cols` columns are used, as a
+// 2-D tensor map with a 64-column (128-byte) x box_rows box and the 128-byte swizzle.
+int encode_map(CUtensorMap* map, const void* ptr, int rows, int cols, int ld, int box_rows) {
+    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)KC, (cuuint32_t)box_rows};
+    const cuuint32_t estr[2] = {1u, 1u};
+    // the driver's encoder, looked up through the runtime so the library does not link libcuda
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        PQ_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+        if (q != cudaDriverEntryPointSuccess || !fn) return PQ_ERR_NO_DEVICE;
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims, strides, box,
+                              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? PQ_OK : PQ_ERR_INVALID_ARG;
+}
+
 template <int BN>
 int launch_gemm(const void* A, int lda, const void* B, int ldb, float* D, int ldd, int M, int N, int K, float alpha,
                 const float* bias, int32_t* status, cudaStream_t stream) {
-    // shared memory sized so that at most 512 / BN CTAs share an SM's TMEM
-    size_t smem = (size_t)(BM + BN) * KC * 2 + 16;
-    const size_t floor_bytes = BN == 256 ? 80 * 1024 : (BN == 128 ? 60 * 1024 : 29 * 1024);
-    if (smem < floor_bytes) smem = floor_bytes;
+    using C = Cfg<BN>;
+    CUtensorMap ta, tb;
+    int rc = encode_map(&ta, A, M, K, lda, BM);
+    if (rc != PQ_OK) return rc;
+    rc = encode_map(&tb, B, N, K, ldb, BN);
+    if (rc != PQ_OK) return rc;
     static bool attr = false;
     if (!attr) {
-        PQ_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+        PQ_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::kSmem));
         attr = true;
     }
     dim3 grid(M / BM, N / BN);
-    tc_gemm_kernel<BN><<<grid, 128, smem, stream>>>((const __nv_bfloat16*)A, lda, (const __nv_bfloat16*)B, ldb, D,
-                                                    ldd, K, alpha, bias, status);
+    tc_gemm_kernel<BN><<<grid, 128, C::kSmem, stream>>>(ta, tb, D, ldd, K, alpha, bias, status);
     return pq_launch_status();
 }
 
@@ -129,8 +213,11 @@ int pq_tc_gemm_bf16(const void* A, int lda, const void* B, int ldb, float* D, in
         return PQ_ERR_INVALID_ARG;
     if (((uintptr_t)A | (uintptr_t)B) & 15 || ((uintptr_t)D & 15)) return PQ_ERR_INVALID_ARG;
     cudaStream_t st = (cudaStream_t)stream;
-    if (N % 256 == 0) return launch_gemm<256>(A, lda, B, ldb, D, ldd, M, N, K, alpha, bias, status, st);
-    if (N % 128 == 0) return launch_gemm<128>(A, lda, B, ldb, D, ldd, M, N, K, alpha, bias, status, st);
+    // the widest tile that divides N and still gives the SMs something to do
+    const int tiles256 = (N % 256 == 0) ? (M / BM) * (N / 256) : 0;
+    if (tiles256 >= 128) return launch_gemm<256>(A, lda, B, ldb, D, ldd, M, N, K, alpha, bias, status, st);
+    const int tiles128 = (N % 128 == 0) ? (M / BM) * (N / 128) : 0;
+    if (tiles128 >= 128) return launch_gemm<128>(A, lda, B, ldb, D, ldd, M, N, K, alpha, bias, status, st);
     return launch_gemm<64>(A, lda, B, ldb, D, ldd, M, N, K, alpha, bias, status, st);
 }
 

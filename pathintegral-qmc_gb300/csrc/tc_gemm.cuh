@@ -27,6 +27,16 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
            ((uint64_t)((sbo & 0x3FFFFu) >> 4) << 32) | (1ull << 46);
 }
 
+// Descriptor of a K-major operand in the 128-byte swizzle layout that a TMA load with
+// CU_TENSOR_MAP_SWIZZLE_128B writes: rows of 64 BF16 (128 B) with the 16-byte chunks
+// of row r permuted by chunk ^ (r % 8), 8-row groups 1024 B apart (SBO); the start
+// address must lie in a 1024-byte-aligned atom (K steps of 16 elements advance it by
+// 32 B); swizzle mode 2 (128 B) in bits 61-63; LBO unused for this layout (1).
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) | (1ull << 46) |
+           (2ull << 61);
+}
+
 // Instruction descriptor of kind::f16: D = FP32, A = B = BF16, both K-major,
 // N >> 3 at bit 17, M >> 4 at bit 24.
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
@@ -107,6 +117,21 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
     for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// mbarrier arrival that also expects `bytes` of asynchronous (TMA) transactions.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
+// 2-D TMA tile load (tensor map in kernel-parameter space) into shared memory at
+// `dst`, completing `bytes` on the mbarrier.  x is the innermost coordinate: it
+// must be a multiple of 16 bytes / element size.
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const void* tmap, int x, int y, uint32_t mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+            "r"(dst), "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(mbar)
+        : "memory");
 }
 
 // Byte offset of element (r, k) in a K-major no-swizzle tile with KC columns.

@@ -73,6 +73,11 @@ SIGNATURES = {
                                      _V]),
     "pq_sa_sparse_reforder_ex": (_I32, [_V, _V, _V, _I32, _I32, _I32, _V, _I32, _I32, _V, _V, _I64, _V, _I32,
                                         _V, _V, _I32, _V, _V, _I32, _V, _V, _V]),
+    "pq_sa_dense_reforder": (_I32, [_V, _V, _I32, _I32, _V, _I32, _I32, _V, _V, _I64, _V, _V, _V]),
+    "pq_sa_dense_reforder_ex": (_I32, [_V, _V, _I32, _I32, _V, _I32, _I32, _V, _V, _I64, _V, _V, _V, _I32, _V, _V,
+                                       _I32, _V, _V, _V]),
+    "pq_sa_bipartite_reforder_ex": (_I32, [_V, _V, _I32, _I32, _V, _V, _I32, _V, _I32, _I32, _V, _I64, _V, _V, _V,
+                                           _I32, _V, _V, _I32, _V, _V, _V]),
     "pq_exp_probe": (_I32, [_V, _V, _I64, _V]),
     "pq_exp_probe_range": (_I32, [_U32, _I64, _V, _V]),
     "pq_jperp_schedule": (_I32, [_V, _I32, _I32, _F32, _V]),

@@ -113,11 +113,16 @@ def _qa_fast(sched, mcsteps, slices, temp, nspins, confs, nbs, rng, seed, global
     return None
 
 
-def QuantumAnneal_dense(sched, mcsteps, slices, temp, nspins, confs, J, rng, *, mode="reference"):
+def QuantumAnneal_dense(sched, mcsteps, slices, temp, nspins, confs, J, rng, *, mode="reference", seed=None,
+                        recompute_every=50):
     """Dense-J path-integral quantum annealing of ``confs`` in place.
 
     Reference: piqmc/qmc.pyx:141-242.  ``J`` is a dense float64 matrix whose upper
     triangle holds the couplings and whose diagonal holds the fields.
+    ``mode="fast"`` runs the dense fast path (``piqmc.dense``: local fields kept
+    in shared memory with rank-1 updates, recomputed every ``recompute_every``
+    field steps by the split-BF16 tensor-core GEMM; both reference quirks
+    corrected; slices <= 32; Philox key ``seed`` or drawn from ``rng``).
     """
     sched = _buffers.float64_buffer(sched, 1, "sched")
     mcsteps = _buffers.as_c_int(mcsteps, "mcsteps")
@@ -126,11 +131,13 @@ def QuantumAnneal_dense(sched, mcsteps, slices, temp, nspins, confs, J, rng, *, 
     nspins = _buffers.as_c_int(nspins, "nspins")
     confs = _buffers.float64_buffer(confs, 2, "confs", writable=True)
     J = _buffers.float64_buffer(J, 2, "J")
-    if mode != "reference":
-        raise ValueError("QuantumAnneal_dense supports mode='reference'")
+    if mode not in ("reference", "fast"):
+        raise ValueError("mode must be 'reference' or 'fast'")
     _validate(sched, mcsteps, slices, nspins, confs)
     if J.shape[0] < nspins or J.shape[1] < nspins:
         raise ValueError("J must be at least nspins x nspins")
+    if mode == "fast":
+        return _qa_dense_fast(sched, mcsteps, slices, temp, nspins, confs, J, rng, seed, recompute_every)
     cur = rng.permutation(range(nspins))
     nsched = sched.size
     if nsched == 0:
@@ -155,3 +162,36 @@ def QuantumAnneal_dense(sched, mcsteps, slices, temp, nspins, confs, J, rng, *, 
         reforder.libc_skip(int(used[0]))
     confs[:nspins, :slices] = spins[0].cpu().numpy()
     return None
+
+
+def _qa_dense_fast(sched, mcsteps, slices, temp, nspins, confs, J, rng, seed, recompute_every):
+    from . import dense
+    if nspins != confs.shape[0]:
+        raise ValueError("mode='fast' updates every row: nspins must equal confs.shape[0]")
+    if slices < 1 or slices > 32:
+        raise ValueError("mode='fast' needs 1 <= slices <= 32")
+    if temp <= 0:
+        raise ValueError("mode='fast' needs temp > 0")
+    if nspins == 0 or sched.size == 0 or mcsteps == 0:
+        return None
+    _buffers.check_pm1(confs[:, :slices], "confs")
+    if seed is None:
+        seed = _buffers.seed_from_rng(rng)
+    prob = dense.DenseProblem(np.ascontiguousarray(J[:nspins, :nspins]))
+    words = prob.pack(torch.from_numpy(np.ascontiguousarray(confs[:, :slices]).astype(np.int8)[None]))
+    prob.anneal(words, sched, slices, float(temp), seed=seed, mcsteps=mcsteps, recompute_every=recompute_every)
+    confs[:, :slices] = prob.unpack(words, slices)[0].cpu().numpy()
+    return None
+
+
+def QuantumAnneal_parallel(sched, mcsteps, slices, temp, nspins, confs, nbs, nthreads, *, seed=0, global_moves=0):
+    """The reference's OpenMP variant (piqmc/qmc.pyx:247-340) on the GPU: the packed kernel.
+
+    The reference threads race on shared spins (its results are not
+    reproducible) and it takes no ``rng``; this runs ``QuantumAnneal(...,
+    mode="fast")`` with Philox key ``seed``.  ``nthreads`` is accepted for
+    compatibility and unused.
+    """
+    _buffers.as_c_int(nthreads, "nthreads")
+    return QuantumAnneal(sched, mcsteps, slices, temp, nspins, confs, nbs, None, mode="fast", seed=seed,
+                         global_moves=global_moves)

@@ -236,6 +236,58 @@ def anneal(spins, nb_idx, nb_j, sched, mcsteps, perms, rands):
     return sp, used.cpu().numpy()
 
 
+def anneal_dense(spins, J, sched, mcsteps, perms, rands):
+    """Reference-order sa.Anneal_dense of R replicas (spins int8 (R, n), J dense float64 (n, n))."""
+    dev = _device.device()
+    sp = torch.as_tensor(spins).to(dev, torch.int8).contiguous()
+    R, n = sp.shape
+    nsched = len(sched)
+    perms = _as_perms(perms, R, nsched * mcsteps, n)
+    rands = _as_rands(rands, R)
+    d_J = _device.to_device(np.ascontiguousarray(np.asarray(J, dtype=np.float64)[:n, :n]))
+    d_t = _device.to_device(np.asarray(sched, dtype=np.float64).astype(np.float32))
+    d_perm = _device.to_device(perms)
+    d_rand = _device.to_device(rands)
+    used = torch.zeros(R, dtype=torch.int64, device=dev)
+    L = _native.lib()
+
+    def launch(ov_x, ov_y, ov_n, cx, cy, cap, ccnt, status):
+        return L.pq_sa_dense_reforder_ex(
+            _device.ptr(sp), _device.ptr(d_J), n, R, _device.ptr(d_t), nsched, int(mcsteps), _device.ptr(d_perm),
+            _device.ptr(d_rand), rands.shape[1], _device.ptr(used), _device.ptr(ov_x), _device.ptr(ov_y), ov_n,
+            _device.ptr(cx), _device.ptr(cy), cap, _device.ptr(ccnt), status.ptr, _device.stream_handle())
+
+    _run_with_exp_check(launch, sp, "pq_sa_dense_reforder")
+    return sp, used.cpu().numpy()
+
+
+def anneal_bipartite(spins, nl, J, lbias, rbias, sched, mcsteps, rands):
+    """Reference-order sa.Anneal_bipartite of R replicas (spins int8 (R, nl + nr): left then right)."""
+    dev = _device.device()
+    sp = torch.as_tensor(spins).to(dev, torch.int8).contiguous()
+    R, ntot = sp.shape
+    nr = ntot - nl
+    nsched = len(sched)
+    rands = _as_rands(rands, R)
+    d_J = _device.to_device(np.ascontiguousarray(np.asarray(J, dtype=np.float64).reshape(nl, nr)))
+    d_lb = _device.to_device(np.ascontiguousarray(lbias, dtype=np.float64))
+    d_rb = _device.to_device(np.ascontiguousarray(rbias, dtype=np.float64))
+    d_t = _device.to_device(np.asarray(sched, dtype=np.float64).astype(np.float32))
+    d_rand = _device.to_device(rands)
+    used = torch.zeros(R, dtype=torch.int64, device=dev)
+    L = _native.lib()
+
+    def launch(ov_x, ov_y, ov_n, cx, cy, cap, ccnt, status):
+        return L.pq_sa_bipartite_reforder_ex(
+            _device.ptr(sp), _device.ptr(d_J), nl, nr, _device.ptr(d_lb), _device.ptr(d_rb), R, _device.ptr(d_t),
+            nsched, int(mcsteps), _device.ptr(d_rand), rands.shape[1], _device.ptr(used), _device.ptr(ov_x),
+            _device.ptr(ov_y), ov_n, _device.ptr(cx), _device.ptr(cy), cap, _device.ptr(ccnt), status.ptr,
+            _device.stream_handle())
+
+    _run_with_exp_check(launch, sp, "pq_sa_bipartite_reforder")
+    return sp, used.cpu().numpy()
+
+
 # ------------------------------------------------------------------------------------------
 # libc rand() stream of this process
 # ------------------------------------------------------------------------------------------

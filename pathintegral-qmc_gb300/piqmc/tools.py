@@ -1,7 +1,9 @@
-"""Drop-in for ``piqmc.tools`` (reference piqmc/tools.pyx): spin/bit conversion and the neighbour table."""
+"""Drop-in for ``piqmc.tools`` (reference piqmc/tools.pyx): spin/bit conversion, the neighbour
+table, the instance generators, and instance / neighbour-table file I/O."""
 import ctypes
 
 import numpy as np
+import scipy.sparse as sps
 
 from . import _native
 
@@ -52,3 +54,172 @@ def GenerateNeighbors(nspins, J, maxnb, savepath=None):
     if savepath is not None:
         np.save(savepath, out)
     return out
+
+
+# ------------------------------------------------------------------------------------------
+# instance generators (reference piqmc/tools.pyx:98-273)
+#
+# Each generator first lists the (row, column) assignments the reference makes, in
+# the order it makes them, then draws all their values with one vectorised
+# ``rng.uniform`` call (the same MT19937 doubles, in the same order, as one scalar
+# draw per assignment), then replays the assignments into a DOK matrix with the
+# DOK's own semantics (a later assignment overwrites the value and keeps the key's
+# position; an exact zero removes the key).  So the matrix, its key order (which
+# ``GenerateNeighbors`` follows) and the state ``rng`` is left in match the
+# reference's, in O(assignments) instead of the reference's O(nspins^2) scan.
+# ------------------------------------------------------------------------------------------
+
+def _replay(n, rows, cols, vals):
+    d = {}
+    for i, j, v in zip(rows, cols, vals.tolist()):
+        if v == 0.0:
+            d.pop((i, j), None)
+        else:
+            d[(i, j)] = v
+    J = sps.dok_matrix((n, n), dtype=np.float64)
+    for (i, j), v in d.items():
+        J[i, j] = v
+    return J
+
+
+def Generate2DIsingInstance(nRows, rng):
+    """Periodic nRows x nRows lattice, couplings U[-2, 2] (reference piqmc/tools.pyx:98-131).
+
+    Assignment order of the reference, per spin ``row`` (n = nRows^2): the
+    vertical wrap bond (row, row + nRows (nRows - 1)) for the first lattice row;
+    then, for every column index ``col`` from ``row`` to n - 1: the horizontal
+    wrap bond (row, row + nRows - 1) when ``row`` starts a lattice row (so that
+    bond is drawn n - row times, the last draw kept), the right bond at
+    col = row + 1 unless ``row`` ends a lattice row, and the down bond at
+    col = row + nRows.
+    """
+    nRows = int(nRows)
+    n = nRows * nRows
+    rows, cols = [], []
+    for row in range(n):
+        if row < nRows:
+            rows.append(row)
+            cols.append(row + nRows * (nRows - 1))
+        right = row % nRows != nRows - 1 and row + 1 < n
+        down = row + nRows < n
+        if row % nRows == 0:
+            wrap = row + nRows - 1
+            for col in range(row, n):
+                rows.append(row)
+                cols.append(wrap)
+                if right and col == row + 1:
+                    rows.append(row)
+                    cols.append(col)
+                if down and col == row + nRows:
+                    rows.append(row)
+                    cols.append(col)
+        else:
+            if right:
+                rows.append(row)
+                cols.append(row + 1)
+            if down:
+                rows.append(row)
+                cols.append(row + nRows)
+    vals = rng.uniform(low=-2, high=2, size=len(rows)) if rows else np.zeros(0)
+    return _replay(n, rows, cols, vals)
+
+
+def Generate2DLattice(nrows, ncols, rng, periodic=0):
+    """nrows x ncols lattice, couplings U[-1e-8, 1e-8] (reference piqmc/tools.pyx:133-175).
+
+    Per spin: the vertical wrap bond (first lattice row, periodic only), the
+    horizontal wrap bond (first lattice column, periodic only), the right bond
+    (unless last lattice column), the down bond (unless last lattice row).
+    """
+    nrows, ncols, periodic = int(nrows), int(ncols), int(periodic)
+    n = nrows * ncols
+    rows, cols = [], []
+    for j in range(n):
+        if periodic and j < ncols:
+            rows.append(j)
+            cols.append(j + ncols * (nrows - 1))
+        if periodic and j % ncols == 0:
+            rows.append(j)
+            cols.append(j + ncols - 1)
+        if j + 1 < n and j % ncols != ncols - 1:
+            rows.append(j)
+            cols.append(j + 1)
+        if j + ncols < n:
+            rows.append(j)
+            cols.append(j + ncols)
+    vals = rng.uniform(low=-1e-8, high=1e-8, size=len(rows)) if rows else np.zeros(0)
+    return _replay(n, rows, cols, vals)
+
+
+def GenerateKblockLattice(nrows, ncols, rng, k=1):
+    """Every spin coupled to the spins on the rings of radius 1..k around it (reference piqmc/tools.pyx:177-273).
+
+    For spin i and radius q, the ring is clipped to the lattice (q' = min(q,
+    distance to each edge)); its top-left corner is tlc = i - up' ncols - left'.
+    The reference assigns, in this order, the top side (tlc + r, r = 0..w - 1),
+    the bottom side (same, plus up' + down' rows), the left side (tlc + r ncols)
+    and the right side (tlc + w - 1 + r ncols), r = 1..up' + down' for the sides,
+    w = left' + right' + 1 -- keeping only entries above the diagonal (i < idx).
+    Couplings U[-1e-8, 1e-8].
+    """
+    nrows, ncols, k = int(nrows), int(ncols), int(k)
+    n = nrows * ncols
+    rows, cols = [], []
+    for i in range(n):
+        c = i % ncols
+        to_right = (ncols - (i + 1) % ncols) if (i + 1) % ncols else 0
+        for q in range(1, k + 1):
+            left = min(c, q)
+            right = min(to_right, q)
+            up = q
+            while i - up * ncols < 0:
+                up -= 1
+            down = q
+            while i + down * ncols >= n:
+                down -= 1
+            tlc = max(i - up * ncols - left, 0)
+            w = left + right + 1
+            h = up + down
+            ring = np.concatenate([tlc + np.arange(w), tlc + h * ncols + np.arange(w),
+                                   tlc + ncols * np.arange(1, h + 1), tlc + w - 1 + ncols * np.arange(1, h + 1)])
+            ring = ring[ring > i].tolist()
+            rows.extend([i] * len(ring))
+            cols.extend(ring)
+    vals = rng.uniform(low=-1e-8, high=1e-8, size=len(rows)) if rows else np.zeros(0)
+    return _replay(n, rows, cols, vals)
+
+
+# ------------------------------------------------------------------------------------------
+# instance and neighbour-table files
+# ------------------------------------------------------------------------------------------
+
+def LoadIsingInstance(fname, nspins=None):
+    """An instance text file of ``i j J`` lines with 1-based spin indices, as a DOK matrix.
+
+    The format of the reference's instance files, read as its examples do
+    (examples/santoro80.py:265-268): entry (i - 1, j - 1) = J, file order is DOK
+    key order (a repeated pair keeps its first position and its last value).
+    ``nspins`` defaults to the largest index in the file.
+    """
+    data = np.loadtxt(fname, ndmin=2)
+    if data.size == 0:
+        return sps.dok_matrix((int(nspins or 0), int(nspins or 0)), dtype=np.float64)
+    if data.shape[1] != 3:
+        raise ValueError("%s: expected 3 columns (i j J), got %d" % (fname, data.shape[1]))
+    ij = data[:, :2]
+    if np.any(ij != np.round(ij)) or np.any(ij < 1):
+        raise ValueError("%s: spin indices must be integers >= 1" % fname)
+    ii = ij.astype(np.int64) - 1
+    n = int(nspins) if nspins is not None else int(ii.max()) + 1
+    if ii.max() >= n:
+        raise ValueError("%s: spin index %d > nspins=%d" % (fname, int(ii.max()) + 1, n))
+    return _replay(n, ii[:, 0].tolist(), ii[:, 1].tolist(), data[:, 2].copy())
+
+
+def LoadNeighbors(path):
+    """A neighbour table saved by ``GenerateNeighbors(..., savepath)`` (``np.save`` of the
+    float64 (nspins, maxnb, 2) table, reference piqmc/tools.pyx:94-95)."""
+    nbs = np.load(path)
+    if nbs.dtype != np.float64 or nbs.ndim != 3 or nbs.shape[2] != 2:
+        raise ValueError("%s: not a neighbour table (float64, shape (nspins, maxnb, 2))" % path)
+    return nbs

@@ -146,6 +146,44 @@ def main():
     E = np.array([sa.ClassicalIsingEnergy(s, J) for s in S])
     r, c, v = dok_arrays(J)
     np.savez_compressed(os.path.join(HERE, "energy_16x16.npz"), rows=r, cols=c, vals=v, spins=S, energies=E)
+    # 8. sa.Anneal_dense, N=48 (upper triangle + fields), 30 temperatures x 2 sweeps
+    N = 48
+    Jd = np.triu(g.normal(0.0, 1.0 / np.sqrt(N), (N, N)), 1) + np.diag(g.normal(0.0, np.sqrt(0.1), N))
+    sv0 = np.where(g.random(N) < 0.5, -1.0, 1.0)
+    sv = sv0.copy()
+    tsched = np.linspace(3.0, 0.05, 30)
+    libc.srand(41)
+    rng = np.random.RandomState(42)
+    sa.Anneal_dense(tsched, 2, sv, Jd, rng)
+    np.savez_compressed(os.path.join(HERE, "sa_dense_48.npz"), J=Jd, sched=tsched, mcsteps=2, sv0=sv0,
+                        final=sv.astype(np.int8), cseed=41, rseed=42, next_rand=libc.rand(),
+                        next_rng=rng.randint(2 ** 31))
+    # 9. sa.Anneal_bipartite, 12 left x 20 right spins with biases, 25 temperatures x 2 sweeps
+    Jb = g.normal(0.0, 0.5, (12, 20))
+    lb, rb = g.normal(0.0, 0.2, 12), g.normal(0.0, 0.2, 20)
+    l0, r0 = np.where(g.random(12) < 0.5, -1.0, 1.0), np.where(g.random(20) < 0.5, -1.0, 1.0)
+    lv, rv = l0.copy(), r0.copy()
+    tsched = np.linspace(4.0, 0.1, 25)
+    libc.srand(51)
+    rng = np.random.RandomState(52)
+    sa.Anneal_bipartite(tsched, 2, lv, rv, Jb, lb, rb, rng)
+    np.savez_compressed(os.path.join(HERE, "sa_bipartite.npz"), J=Jb, lbias=lb, rbias=rb, sched=tsched, mcsteps=2,
+                        l0=l0, r0=r0, lfinal=lv.astype(np.int8), rfinal=rv.astype(np.int8), cseed=51,
+                        next_rand=libc.rand(), next_rng=rng.randint(2 ** 31))
+    # 10. instance generators: DOK key order, values and the rng state they leave
+    gen = {}
+    for name, call, seed in [("ising2d_5", lambda rs: tools.Generate2DIsingInstance(5, rs), 61),
+                             ("ising2d_2", lambda rs: tools.Generate2DIsingInstance(2, rs), 62),
+                             ("lattice_4x5_periodic", lambda rs: tools.Generate2DLattice(4, 5, rs, 1), 63),
+                             ("lattice_4x5_open", lambda rs: tools.Generate2DLattice(4, 5, rs, 0), 64),
+                             ("kblock_5x6_k2", lambda rs: tools.GenerateKblockLattice(5, 6, rs, 2), 65),
+                             ("kblock_4x4_k1", lambda rs: tools.GenerateKblockLattice(4, 4, rs, 1), 66)]:
+        rs = np.random.RandomState(seed)
+        r, c, v = dok_arrays(call(rs))
+        gen[name + "_rows"], gen[name + "_cols"], gen[name + "_vals"] = r, c, v
+        gen[name + "_seed"] = seed
+        gen[name + "_next_rng"] = rs.randint(2 ** 31)
+    np.savez_compressed(os.path.join(HERE, "generators.npz"), **gen)
     print("golden vectors written to", HERE)
 
 

@@ -57,6 +57,66 @@ def test_dropin_qa_dense_48(piqmc):
     assert rng.randint(2 ** 31) == g["next_rng"]
 
 
+def test_dropin_sa_dense_48(piqmc):
+    g = golden("sa_dense_48")
+    sv = g["sv0"].copy()
+    oracle.libc_srand(int(g["cseed"]))
+    rng = np.random.RandomState(int(g["rseed"]))
+    piqmc.sa.Anneal_dense(g["sched"], int(g["mcsteps"]), sv, g["J"], rng)
+    np.testing.assert_array_equal(sv.astype(np.int8), g["final"])
+    assert oracle.libc_rand(1)[0] == g["next_rand"]
+    assert rng.randint(2 ** 31) == g["next_rng"]
+
+
+def test_dropin_sa_bipartite(piqmc):
+    g = golden("sa_bipartite")
+    lv, rv = g["l0"].copy(), g["r0"].copy()
+    oracle.libc_srand(int(g["cseed"]))
+    rng = np.random.RandomState(0)
+    piqmc.sa.Anneal_bipartite(g["sched"], int(g["mcsteps"]), lv, rv, g["J"], g["lbias"], g["rbias"], rng)
+    np.testing.assert_array_equal(lv.astype(np.int8), g["lfinal"])
+    np.testing.assert_array_equal(rv.astype(np.int8), g["rfinal"])
+    assert oracle.libc_rand(1)[0] == g["next_rand"]
+
+
+def test_parallel_and_multispin_aliases_run_the_packed_kernel(piqmc):
+    """QuantumAnneal_parallel / Anneal_parallel / Anneal_multispin: the packed kernel with a fixed key."""
+    from piqmc import tools
+    J = tools.Generate2DIsingInstance(8, np.random.RandomState(1))
+    nbs = tools.GenerateNeighbors(64, J, 4)
+    g = np.random.default_rng(2)
+    confs = np.tile(np.where(g.random(64) < 0.5, -1.0, 1.0), (8, 1)).T.copy()
+    c2 = confs.copy()
+    sched = np.linspace(3.0, 1e-8, 50)
+    piqmc.qmc.QuantumAnneal_parallel(sched, 1, 8, 0.05, 64, confs, nbs, 4)
+    piqmc.qmc.QuantumAnneal(sched, 1, 8, 0.05, 64, c2, nbs, None, mode="fast", seed=0)
+    np.testing.assert_array_equal(confs, c2)
+    sv = np.where(g.random(64) < 0.5, -1.0, 1.0)
+    sv2 = sv.copy()
+    tsched = np.linspace(3.0, 0.05, 40)
+    piqmc.sa.Anneal_parallel(tsched, 1, sv, nbs, 8, seed=5)
+    piqmc.sa.Anneal(tsched, 1, sv2, nbs, None, mode="fast", seed=5)
+    np.testing.assert_array_equal(sv, sv2)
+    mat = np.where(g.random((64, 64)) < 0.5, -1.0, 1.0)
+    e0 = piqmc.sa.ClassicalIsingEnergy(mat.T, J)
+    piqmc.sa.Anneal_multispin(tsched, 2, mat, nbs, np.random.RandomState(4))
+    assert set(np.unique(mat)) <= {-1.0, 1.0}
+    assert np.all(piqmc.sa.ClassicalIsingEnergy(mat.T, J) <= e0.max()) and np.median(
+        piqmc.sa.ClassicalIsingEnergy(mat.T, J)) < np.median(e0)
+
+
+def test_dense_fast_mode_anneals_like_the_reference_semantics(piqmc):
+    """QuantumAnneal_dense(mode='fast') runs the dense fast path in place."""
+    g = golden("qa_dense_48")
+    J, P = g["J"], int(g["P"])
+    confs = np.tile(g["conf0"], (P, 1)).T.copy()
+    e0 = piqmc.sa.ClassicalIsingEnergy(confs[:, 0], J)
+    piqmc.qmc.QuantumAnneal_dense(np.linspace(3.0, 1e-8, 200), 1, P, 0.05, J.shape[0], confs, J,
+                                  np.random.RandomState(1), mode="fast")
+    assert set(np.unique(confs)) <= {-1.0, 1.0}
+    assert min(piqmc.sa.ClassicalIsingEnergy(confs[:, k], J) for k in range(P)) < e0
+
+
 def test_dropin_boixo8(piqmc):
     """The reference's own diamond-graph test (testing/test_boixo.py:90-114), bit-exact."""
     g = golden("boixo8")

@@ -147,3 +147,45 @@ def test_greedy_colouring(native):
     assert nc >= 3
     for (a, b) in J.keys():
         assert col[a] != col[b]
+
+
+GENERATORS = {
+    "ising2d_5": lambda t, rs: t.Generate2DIsingInstance(5, rs),
+    "ising2d_2": lambda t, rs: t.Generate2DIsingInstance(2, rs),
+    "lattice_4x5_periodic": lambda t, rs: t.Generate2DLattice(4, 5, rs, 1),
+    "lattice_4x5_open": lambda t, rs: t.Generate2DLattice(4, 5, rs, 0),
+    "kblock_5x6_k2": lambda t, rs: t.GenerateKblockLattice(5, 6, rs, 2),
+    "kblock_4x4_k1": lambda t, rs: t.GenerateKblockLattice(4, 4, rs, 1),
+}
+
+
+@pytest.mark.parametrize("name", sorted(GENERATORS))
+def test_instance_generators_match_reference(name):
+    """Key order, values and the rng state left behind, against the compiled reference's outputs."""
+    from piqmc import tools
+    g = golden("generators")
+    rs = np.random.RandomState(int(g[name + "_seed"]))
+    J = GENERATORS[name](tools, rs)
+    items = list(J.items())
+    np.testing.assert_array_equal([k[0] for k, _ in items], g[name + "_rows"])
+    np.testing.assert_array_equal([k[1] for k, _ in items], g[name + "_cols"])
+    np.testing.assert_array_equal([v for _, v in items], g[name + "_vals"])
+    assert rs.randint(2 ** 31) == g[name + "_next_rng"]
+
+
+def test_instance_file_and_neighbor_cache_round_trip(tmp_path):
+    from piqmc import tools
+    J = tools.Generate2DIsingInstance(6, np.random.RandomState(3))
+    path = tmp_path / "inst.txt"
+    with open(path, "w") as f:
+        for (i, j), v in J.items():
+            f.write("%d %d %.17g\n" % (i + 1, j + 1, v))
+    K = tools.LoadIsingInstance(str(path))
+    assert list(K.keys()) == list(J.keys())
+    assert all(K[k] == v for k, v in J.items())
+    nbs = tools.GenerateNeighbors(36, K, 4, str(tmp_path / "nbs.npy"))
+    np.testing.assert_array_equal(tools.LoadNeighbors(str(tmp_path / "nbs.npy")), nbs)
+    with pytest.raises(ValueError):
+        bad = tmp_path / "bad.txt"
+        bad.write_text("0 1 0.5\n")
+        tools.LoadIsingInstance(str(bad))

@@ -70,6 +70,31 @@ def test_qa_dense_48():
     assert rng.randint(2 ** 31) == g["next_rng"]
 
 
+def test_sa_dense_48():
+    g = golden("sa_dense_48")
+    J, sched, mcsteps = g["J"], g["sched"], int(g["mcsteps"])
+    n = J.shape[0]
+    rng = np.random.RandomState(int(g["rseed"]))
+    perms = oracle.reference_perms(rng, n, len(sched) * mcsteps)
+    rands = oracle.libc_stream(int(g["cseed"]), n * len(sched) * mcsteps + 1)
+    s = g["sv0"].astype(np.int8).copy()
+    used = oracle.sa_dense(s, J, sched, mcsteps, perms, rands)
+    np.testing.assert_array_equal(s, g["final"])
+    assert rands[used] == g["next_rand"]
+    assert rng.randint(2 ** 31) == g["next_rng"]
+
+
+def test_sa_bipartite():
+    g = golden("sa_bipartite")
+    sched, mcsteps = g["sched"], int(g["mcsteps"])
+    lv, rv = g["l0"].astype(np.int8).copy(), g["r0"].astype(np.int8).copy()
+    rands = oracle.libc_stream(int(g["cseed"]), (lv.size + rv.size) * len(sched) * mcsteps + 1)
+    used = oracle.sa_bipartite(lv, rv, g["J"], g["lbias"], g["rbias"], sched, mcsteps, rands)
+    np.testing.assert_array_equal(lv, g["lfinal"])
+    np.testing.assert_array_equal(rv, g["rfinal"])
+    assert rands[used] == g["next_rand"]
+
+
 def test_boixo8_qa_and_energies():
     g = golden("boixo8")
     J = dok_from(g["rows"], g["cols"], g["vals"], 8)
