@@ -44,6 +44,46 @@ def schedule(nsched=NSCHED):
     return np.linspace(3.0, 1e-8, nsched)
 
 
+# ------------------------------------------------------------------------------------------
+# sharding over ranks: replicas only, no data-path collective
+# ------------------------------------------------------------------------------------------
+
+BENCH_SEED = 7
+
+
+def rank_plan(rank, world, R):
+    """Rank `rank` of `world` anneals the global replicas [rank R, (rank + 1) R) with the job's Philox key.
+
+    A replica's stream depends only on (key, global replica id, sweep), so the
+    union of the ranks' results equals one process annealing all world x R
+    replicas; the only collective is the max-over-ranks timing reduction."""
+    if not 0 <= rank < world or R <= 0:
+        raise ValueError("bad rank plan: rank %d of %d, %d replicas" % (rank, world, R))
+    return {"replica_base": rank * R, "replicas": R, "seed": BENCH_SEED, "total_replicas": world * R}
+
+
+def initial_spins(replica_base, R, n, seed=1234):
+    """+-1 start vectors of global replicas replica_base .. replica_base + R - 1 (the same on any rank layout)."""
+    out = np.empty((R, n), dtype=np.int8)
+    for j in range(R):
+        g = np.random.default_rng([seed, replica_base + j])
+        out[j] = np.where(g.random(n) < 0.5, -1, 1)
+    return out
+
+
+def max_over_ranks(x, dist, device):
+    """The largest of the ranks' values of x (the job's time is its slowest rank's)."""
+    import torch
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank_step, steps, world, total_s):
+    """Units all ranks processed / the slowest rank's time."""
+    return units_per_rank_step * steps * world / total_s
+
+
 def instance_arrays(seed=2026):
     """Seeded 80x80 periodic N(0,1) instance: DOK keys in insertion order (right, down per spin)."""
     g = np.random.default_rng(seed)
@@ -254,20 +294,20 @@ def gpu_arm(args):
     nbs = tools.GenerateNeighbors(n, J, 4)
     prob = fast.Problem(nbs)
     sched = schedule(args.nsched)
-    g = np.random.default_rng(1234 + rank)
-    conf0 = np.where(g.random((R, n)) < 0.5, -1, 1).astype(np.int8)
+    plan = rank_plan(rank, world, R)
+    conf0 = initial_spins(plan["replica_base"], R, n)
     confs = np.ascontiguousarray(np.repeat(conf0[:, :, None], P, axis=2))
     words0 = prob.pack(torch.from_numpy(confs))
     words = words0.clone()
     jp = torch.from_numpy(fast.jperp_schedule(sched, P, TEMP)).cuda()
     status = fast._device.Status()
     l2_flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    seed0 = 7 + 1000 * rank
+    seed0 = plan["seed"]
     updates = float(n) * P * R * len(sched)
 
     def one_step(it):
         fast.anneal(prob, words, sched, P, TEMP, seed=seed0 + it, jperp=jp, status=status, check=False,
-                    threads=args.threads, replicas_per_cta=args.rpc, replica_base=rank * R)
+                    threads=args.threads, replicas_per_cta=args.rpc, replica_base=plan["replica_base"])
 
     for it in range(args.warmup):
         words.copy_(words0)
@@ -293,10 +333,8 @@ def gpu_arm(args):
     step_ms = [a.elapsed_time(b) for a, b in times]
     total_s = sum(step_ms) * 1e-3
     if world > 1:
-        t = torch.tensor([total_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
-    value = updates * args.steps * world / total_s
+        total_s = max_over_ranks(total_s, dist, "cuda")
+    value = whole_job_rate(updates, args.steps, world, total_s)
     # energies of the last anneal: residual-energy summary (per spin, best slice)
     E = prob.energies(words, P).cpu().numpy()
     best = E.min(axis=1) / n
@@ -305,23 +343,23 @@ def gpu_arm(args):
     pinned_in = torch.from_numpy(confs).pin_memory()
     out_c = torch.empty((R, n, P), dtype=torch.int8, pin_memory=True)
     out_e = torch.empty((R, P), dtype=torch.float64, pin_memory=True)
-    fast.anneal_replicas(prob, pinned_in, sched, P, TEMP, seed=seed0, out=out_c, energies_out=out_e)
+    fast.anneal_replicas(prob, pinned_in, sched, P, TEMP, seed=seed0, out=out_c, energies_out=out_e,
+                         replica_base=plan["replica_base"])
     e2e_ms = []
     for it in range(max(1, min(args.steps, 3))):
         l2_flush.fill_(float(it))
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        fast.anneal_replicas(prob, pinned_in, sched, P, TEMP, seed=seed0 + 100 + it, out=out_c, energies_out=out_e)
+        fast.anneal_replicas(prob, pinned_in, sched, P, TEMP, seed=seed0 + 100 + it, out=out_c, energies_out=out_e,
+                             replica_base=plan["replica_base"])
         e1.record()
         torch.cuda.synchronize()
         e2e_ms.append(e0.elapsed_time(e1))
     e2e_s = sum(e2e_ms) * 1e-3
     if world > 1:
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = updates * len(e2e_ms) * world / e2e_s
+        e2e_s = max_over_ranks(e2e_s, dist, "cuda")
+    e2e_value = whole_job_rate(updates, len(e2e_ms), world, e2e_s)
 
     batched = densew = learnedw = None
     if not args.no_batched and rank == 0:
@@ -594,7 +632,8 @@ def reference_arm(args):
     if rank != 0:
         return
     base = cpu_baseline(steps=args.steps, warmup=args.warmup)
-    line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": "updates/s", "n_gpus": 0,
+    # n_gpus mirrors the GPU arm's launch; the work itself runs on the host cores (cpu_baseline.cores)
+    line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": "updates/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp32/fp64", "data": "synthetic",
             "config": {"workload": "80x80 periodic lattice, J~N(0,1) fp32, P=20, T=0.05, G linear 3.0->1e-8 "

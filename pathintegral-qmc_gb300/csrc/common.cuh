@@ -40,6 +40,43 @@ __device__ __forceinline__ pq_u32x4 pq_philox(pq_u32x4 c, uint32_t k0, uint32_t 
     return c;
 }
 
+// Round keys of Philox4x32-10: round r uses (k0 + r * 0x9E3779B9, k1 + r * 0xBB67AE85).
+// PhiloxKeysReg derives them from the key pair in registers; PhiloxKeysTab reads a
+// precomputed table (placed in kernel-parameter space it folds into the XORs as
+// constant operands).  Both give pq_philox's values.
+struct PhiloxKeyTable {
+    uint32_t a[10], b[10];
+};
+struct PhiloxKeysReg {
+    uint32_t k0, k1;
+    __device__ __forceinline__ uint32_t ka(int r) const { return k0 + (uint32_t)r * 0x9E3779B9u; }
+    __device__ __forceinline__ uint32_t kb(int r) const { return k1 + (uint32_t)r * 0xBB67AE85u; }
+};
+struct PhiloxKeysTab {
+    const PhiloxKeyTable& t;
+    __device__ __forceinline__ uint32_t ka(int r) const { return t.a[r]; }
+    __device__ __forceinline__ uint32_t kb(int r) const { return t.b[r]; }
+};
+inline PhiloxKeyTable pq_philox_key_table(uint32_t k0, uint32_t k1) {
+    PhiloxKeyTable t;
+    for (int r = 0; r < 10; ++r) {
+        t.a[r] = k0 + (uint32_t)r * 0x9E3779B9u;
+        t.b[r] = k1 + (uint32_t)r * 0xBB67AE85u;
+    }
+    return t;
+}
+
+template <typename KS>
+__device__ __forceinline__ pq_u32x4 pq_philox_ks(pq_u32x4 c, const KS& ks) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = pq_u32x4{hi1 ^ c.y ^ ks.ka(r), lo1, hi0 ^ c.w ^ ks.kb(r), lo0};
+    }
+    return c;
+}
+
 // Uniform in [0, 1) with 23 random bits: (1 + (r >> 9) * 2^-23) - 1 = (r >> 9) * 2^-23, exact.
 __device__ __forceinline__ float pq_u01(uint32_t r) {
     return __fsub_rn(__uint_as_float((r >> 9) | 0x3f800000u), 1.0f);

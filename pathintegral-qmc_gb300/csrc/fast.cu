@@ -18,6 +18,7 @@ struct FastArgs {
     int64_t sweep_base;
     int replica_base;
     int rpc;  // replicas per CTA
+    PhiloxKeyTable keys;  // round keys of (key0, key1), read as constant operands
 };
 
 template <typename W, int MAXDEG, int NQC>
@@ -25,7 +26,8 @@ __global__ void __launch_bounds__(512) qa_fast_kernel(W* __restrict__ words, con
                                                       const float* __restrict__ cpl,
                                                       const float* __restrict__ field,
                                                       const float* __restrict__ jperp,
-                                                      const float* __restrict__ betas, FastArgs a,
+                                                      const float* __restrict__ betas,
+                                                      const __grid_constant__ FastArgs a,
                                                       unsigned long long* __restrict__ accepts,
                                                       int32_t* __restrict__ status) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -52,7 +54,7 @@ __global__ void __launch_bounds__(512) qa_fast_kernel(W* __restrict__ words, con
     bool bad = false;
     unsigned long long nacc = 0;
     stage_in<W>(it, sw, g);   // also publishes csize
-    run_item<W, MAXDEG, NQC>(it, sw, order, parity, g, bad, nacc);
+    run_item<W, MAXDEG, NQC>(it, a.keys, sw, order, parity, g, bad, nacc);
     stage_out<W>(it, sw, g);
     if (bad) pq_set_status(status, PQ_ERR_BAD_INDEX);
     if (accepts) {
@@ -227,6 +229,7 @@ int pq_qa_fast_ex(void* words, const int32_t* nbr, const float* cpl, const float
     a.beta = p.beta;
     a.key0 = (uint32_t)(p.seed & 0xffffffffu);
     a.key1 = (uint32_t)(p.seed >> 32);
+    a.keys = pq_philox_key_table(a.key0, a.key1);
     a.sweep_base = p.sweep_base;
     a.replica_base = p.replica_base;
     int threads = p.threads > 0 ? p.threads : 0;

@@ -71,15 +71,31 @@ __device__ __forceinline__ float worldline_align(W wi, const W (&nbw)[MAXD], con
     return sa;
 }
 
+// What the features of spin i read from memory: its world-line, its neighbours'
+// world-lines and couplings, its field.
 template <typename W, int MAXD>
-__device__ __forceinline__ void spin_features(const W* __restrict__ words_r, int i, int n, int P, int maxdeg,
-                              const int32_t* __restrict__ nbr, const float* __restrict__ cpl, float h, float beta,
-                              float jp, float (&x)[kFeat], float& dE) {
-    const W mask = slice_mask<W>(P);
-    const W wi = words_r[i] & mask;
+struct SiteIn {
+    W wi;
     W nbw[MAXD];
     float J[MAXD];
-    load_neighbourhood<W, MAXD>(words_r, i, n, maxdeg, nbr, cpl, nbw, J);
+    float h;
+};
+
+template <typename W, int MAXD>
+__device__ __forceinline__ void load_site_in(const W* __restrict__ words_r, int i, int n, int maxdeg,
+                                             const int32_t* __restrict__ nbr, const float* __restrict__ cpl,
+                                             const float* __restrict__ field, SiteIn<W, MAXD>& s) {
+    s.wi = words_r[i];
+    s.h = __ldg(field + i);
+    load_neighbourhood<W, MAXD>(words_r, i, n, maxdeg, nbr, cpl, s.nbw, s.J);
+}
+
+template <typename W, int MAXD>
+__device__ __forceinline__ void site_features(const SiteIn<W, MAXD>& st, int P, int maxdeg, float beta, float jp,
+                                              float (&x)[kFeat], float& dE) {
+    const W mask = slice_mask<W>(P);
+    const W wi = st.wi & mask;
+    const float h = st.h;
     const int deg = maxdeg;
     const float Pf = (float)P;
     float scale = __fadd_rn(1.0f, fabsf(h));
@@ -89,19 +105,19 @@ __device__ __forceinline__ void spin_features(const W* __restrict__ words_r, int
 #pragma unroll
     for (int m = 0; m < MAXD; ++m) {
         if (m >= deg) break;
-        scale = __fadd_rn(scale, fabsf(J[m]));
-        const float tm = (float)(P - 2 * popc_(nbw[m] & mask));
-        s1 = __fadd_rn(s1, __fmul_rn(J[m], tm));
-        s2 = __fadd_rn(s2, __fmul_rn(__fmul_rn(h2, J[m]), tm));
-        s2 = __fadd_rn(s2, __fmul_rn(__fmul_rn(J[m], J[m]), Pf));
+        scale = __fadd_rn(scale, fabsf(st.J[m]));
+        const float tm = (float)(P - 2 * popc_(st.nbw[m] & mask));
+        s1 = __fadd_rn(s1, __fmul_rn(st.J[m], tm));
+        s2 = __fadd_rn(s2, __fmul_rn(__fmul_rn(h2, st.J[m]), tm));
+        s2 = __fadd_rn(s2, __fmul_rn(__fmul_rn(st.J[m], st.J[m]), Pf));
 #pragma unroll
         for (int l = 0; l < MAXD; ++l) {
             if (l >= m) break;
-            const float tml = (float)(P - 2 * popc_((nbw[m] ^ nbw[l]) & mask));
-            s2 = __fadd_rn(s2, __fmul_rn(__fmul_rn(2.0f, __fmul_rn(J[m], J[l])), tml));
+            const float tml = (float)(P - 2 * popc_((st.nbw[m] ^ st.nbw[l]) & mask));
+            s2 = __fadd_rn(s2, __fmul_rn(__fmul_rn(2.0f, __fmul_rn(st.J[m], st.J[l])), tml));
         }
     }
-    const float sa = worldline_align<W, MAXD>(wi, nbw, J, deg, h, P, mask);
+    const float sa = worldline_align<W, MAXD>(wi, st.nbw, st.J, deg, h, P, mask);
     const float inv = __fdiv_rn(1.0f, Pf);
     const float mean = __fmul_rn(s1, inv);
     const float var = fmaxf(__fsub_rn(__fmul_rn(s2, inv), __fmul_rn(mean, mean)), 0.0f);
@@ -115,6 +131,16 @@ __device__ __forceinline__ void spin_features(const W* __restrict__ words_r, int
     x[5] = fminf(fmaxf(__fmul_rn(__fmul_rn(beta, dE), inv), -8.0f), 8.0f);
     x[6] = fminf(fmaxf(__fmul_rn(__fmul_rn(jp, beta), inv), 0.0f), 8.0f);
     x[7] = 1.0f;
+}
+
+template <typename W, int MAXD>
+__device__ __forceinline__ void spin_features(const W* __restrict__ words_r, int i, int n, int P, int maxdeg,
+                                              const int32_t* __restrict__ nbr, const float* __restrict__ cpl,
+                                              const float* __restrict__ field, float beta, float jp,
+                                              float (&x)[kFeat], float& dE) {
+    SiteIn<W, MAXD> st;
+    load_site_in<W, MAXD>(words_r, i, n, maxdeg, nbr, cpl, field, st);
+    site_features<W, MAXD>(st, P, maxdeg, beta, jp, x, dE);
 }
 
 // Rows [0, M): features of the current world-lines of class `cls` (all replicas,
@@ -131,7 +157,7 @@ __global__ void features_kernel(const W* __restrict__ words, int n, int P, int R
     const int r = (int)(t / csize), s = (int)(t % csize);
     const int i = cls * stride + s;
     float x[kFeat], de;
-    spin_features<W, MAXD>(words + (int64_t)r * n, i, n, P, maxdeg, nbr, cpl, __ldg(field + i), beta, jp, x, de);
+    spin_features<W, MAXD>(words + (int64_t)r * n, i, n, P, maxdeg, nbr, cpl, field, beta, jp, x, de);
     dE[t] = de;
     __nv_bfloat16* row = X + t * kLd;
     __nv_bfloat16* rowf = X + (Mpad + t) * kLd;
@@ -396,6 +422,17 @@ __global__ void __launch_bounds__(128) learned_move_kernel(W* __restrict__ words
     uint32_t phase = 0;
     bool ok = true;
 
+    // the inputs of the next tile's features are loaded while this tile's MMAs run
+    SiteIn<W, MAXD> nxt;
+    auto prefetch = [&](int64_t tile) {
+        const int64_t t = tile * kTile + tid;
+        if (tile < a.ntiles && t < M) {
+            const int r = (int)(t / a.csize);
+            const int i = a.cls * a.stride + (int)(t - (int64_t)r * a.csize);
+            load_site_in<W, MAXD>(words + (int64_t)r * a.n, i, a.n, a.maxdeg, nbr, cpl, field, nxt);
+        }
+    };
+    prefetch(blockIdx.x);
     for (int64_t tile = blockIdx.x; tile < a.ntiles && ok; tile += gridDim.x) {
         const int64_t t = tile * kTile + tid;
         const bool valid = t < M;
@@ -406,8 +443,7 @@ __global__ void __launch_bounds__(128) learned_move_kernel(W* __restrict__ words
             if (valid) {
                 r = (int)(t / a.csize);
                 i = a.cls * a.stride + (int)(t - (int64_t)r * a.csize);
-                spin_features<W, MAXD>(words + (int64_t)r * a.n, i, a.n, a.P, a.maxdeg, nbr, cpl, __ldg(field + i), a.beta,
-                                 a.jp, x, de);
+                site_features<W, MAXD>(nxt, a.P, a.maxdeg, a.beta, a.jp, x, de);
             }
             // one 16-byte core-matrix row each: features 0..7 of the current and the flipped world-line
             uint32_t pc[4], pf[4];
@@ -433,25 +469,29 @@ __global__ void __launch_bounds__(128) learned_move_kernel(W* __restrict__ words
             tc::mma_bf16(tmem + kLd, tc::smem_desc(tc::smem_addr(sXf), 128, kK1 * 16), bd, idesc, 0u);
             tc::mma_commit(tc::smem_addr(mbar));
         }
+        // spins of the next tile are not touched by this tile's moves (one thread per spin)
+        prefetch(tile + gridDim.x);
         if (!tc::mbar_wait(tc::smem_addr(mbar), phase, kMmaWait)) { ok = false; break; }
         phase ^= 1u;
         tc::fence_after_sync();
 #pragma unroll 1
-        for (int c0 = 0; c0 < 2 * kLd; c0 += 32) {
-            float v[32];
-            tc::tmem_ld32(tlane + (uint32_t)c0, v);
-            unsigned char* dst = c0 < kLd ? sH : sHf;
-            const int cb = c0 & (kLd - 1);
+        for (int half = 0; half < 2; ++half) {
+            uint32_t u0[32], u1[32];
+            tc::tmem_ld32_async(tlane + (uint32_t)(half * kLd), u0);
+            tc::tmem_ld32_async(tlane + (uint32_t)(half * kLd + 32), u1);
+            tc::tmem_wait_ld();
+            unsigned char* dst = half ? sHf : sH;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
+            for (int q = 0; q < 8; ++q) {
                 uint32_t pk[4];
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
                     const int j = 8 * q + 2 * e;
-                    pk[e] = bf16x2_bits(fmaxf(__fadd_rn(v[j], sb1[cb + j]), 0.0f),
-                                        fmaxf(__fadd_rn(v[j + 1], sb1[cb + j + 1]), 0.0f));
+                    const float v0 = __uint_as_float(j < 32 ? u0[j & 31] : u1[j & 31]);
+                    const float v1 = __uint_as_float(j + 1 < 32 ? u0[(j + 1) & 31] : u1[(j + 1) & 31]);
+                    pk[e] = bf16x2_bits(fmaxf(__fadd_rn(v0, sb1[j]), 0.0f), fmaxf(__fadd_rn(v1, sb1[j + 1]), 0.0f));
                 }
-                *reinterpret_cast<uint4*>(dst + tc::tile_off(tid, cb + 8 * q, kLd)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                *reinterpret_cast<uint4*>(dst + tc::tile_off(tid, 8 * q, kLd)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
             }
         }
         // layer 2
@@ -473,19 +513,23 @@ __global__ void __launch_bounds__(128) learned_move_kernel(W* __restrict__ words
         if (!tc::mbar_wait(tc::smem_addr(mbar), phase, kMmaWait)) { ok = false; break; }
         phase ^= 1u;
         tc::fence_after_sync();
-        float lg[2];
-#pragma unroll 1
-        for (int half = 0; half < 2; ++half) {
-            float acc = a.b3;
-#pragma unroll 1
-            for (int c0 = 0; c0 < kLd; c0 += 32) {
-                float v[32];
-                tc::tmem_ld32(tlane + (uint32_t)(half * kLd + c0), v);
+        float lg0 = a.b3, lg1 = a.b3;
 #pragma unroll
-                for (int j = 0; j < 32; ++j) acc = __fmaf_rn(fmaxf(__fadd_rn(v[j], sb2[c0 + j]), 0.0f), sw3[c0 + j], acc);
-            }
-            lg[half] = acc;
+        for (int half = 0; half < 2; ++half) {
+            uint32_t u0[32], u1[32];
+            tc::tmem_ld32_async(tlane + (uint32_t)(half * kLd), u0);
+            tc::tmem_ld32_async(tlane + (uint32_t)(half * kLd + 32), u1);
+            tc::tmem_wait_ld();
+            float acc = a.b3;
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                acc = __fmaf_rn(fmaxf(__fadd_rn(__uint_as_float(u0[j]), sb2[j]), 0.0f), sw3[j], acc);
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                acc = __fmaf_rn(fmaxf(__fadd_rn(__uint_as_float(u1[j]), sb2[32 + j]), 0.0f), sw3[32 + j], acc);
+            if (half == 0) lg0 = acc; else lg1 = acc;
         }
+        const float lg[2] = {lg0, lg1};
         // MH decision: uniforms Philox(ctr = {i, move, replica, 3 << 24 | cls}) words 0 and 1
         bool proposed = false, accepted = false;
         if (valid) {

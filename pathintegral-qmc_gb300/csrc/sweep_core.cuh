@@ -101,15 +101,16 @@ __device__ __forceinline__ int slice_count(int P, int q) {
 __device__ __forceinline__ int slice_of(int P, int q, int m) { return q == 2 ? P - 1 : 2 * m + q; }
 
 // Class visiting order of one (replica, sweep) and the slice-class parity word.
-__device__ inline void class_order(int M, int order_mode, uint32_t key0, uint32_t key1, uint32_t sweep,
-                                   uint32_t replica, uint8_t* order, uint32_t* parity) {
+template <typename KS>
+__device__ inline void class_order(int M, int order_mode, const KS& ks, uint32_t sweep, uint32_t replica,
+                                   uint8_t* order, uint32_t* parity) {
     for (int c = 0; c < M; ++c) order[c] = (uint8_t)c;
     if (order_mode == 0) { *parity = 0; return; }
     uint32_t w[4] = {0, 0, 0, 0};
     int used = 4, blk = 0;
     for (int j = M - 1; j >= 0; --j) {
         if (used == 4) {
-            const pq_u32x4 r = pq_philox(pq_u32x4{0xFFFFFFFFu, sweep, replica, (2u << 24) | (uint32_t)blk++}, key0, key1);
+            const pq_u32x4 r = pq_philox_ks(pq_u32x4{0xFFFFFFFFu, sweep, replica, (2u << 24) | (uint32_t)blk++}, ks);
             w[0] = r.x; w[1] = r.y; w[2] = r.z; w[3] = r.w;
             used = 0;
         }
@@ -155,15 +156,15 @@ __device__ __forceinline__ bool decide(float sum, float u, float m2beta, float m
 // Core of the compile-time path: NQH slices m = 0..NQH-1 whose bits sit at
 // positions 2m of the 32-bit (q-shifted) words wq, dq, dl, dr; the m-th uses
 // word m & 3 of Philox block blk0 + (m >> 2).  Returns the flips at bits 2m.
-template <int NQH, int DEG>
+template <int NQH, int DEG, typename KS>
 __device__ __forceinline__ uint32_t update_half(uint32_t wq, const uint32_t (&dq)[DEG], uint32_t dl, uint32_t dr,
                                                 const float (&J)[DEG], float h, float jp, int q, int blk0, uint32_t i,
-                                                uint32_t sweep, uint32_t rep, uint32_t key0, uint32_t key1,
-                                                float m2beta, float m2blog2e) {
+                                                uint32_t sweep, uint32_t rep, const KS& ks, float m2beta,
+                                                float m2blog2e) {
     uint32_t flips = 0;
 #pragma unroll
     for (int blk = 0; blk < (NQH + 3) / 4; ++blk) {
-        const pq_u32x4 rnd = pq_philox(pq_u32x4{i, sweep, rep, (uint32_t)((q << 16) | (blk0 + blk))}, key0, key1);
+        const pq_u32x4 rnd = pq_philox_ks(pq_u32x4{i, sweep, rep, (uint32_t)((q << 16) | (blk0 + blk))}, ks);
         const uint32_t rw4[4] = {rnd.x, rnd.y, rnd.z, rnd.w};
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
@@ -186,10 +187,10 @@ __device__ __forceinline__ uint32_t update_half(uint32_t wq, const uint32_t (&dq
 // fixed at compile time (NQ <= 16 with 32-bit words, NQ = 32 with 64-bit words
 // as two 32-bit halves), DEG couplings.  Same arithmetic and uniforms as the
 // generic path.
-template <int NQ, int DEG, typename W>
+template <int NQ, int DEG, typename W, typename KS>
 __device__ __forceinline__ W update_fixed(W wi, const W (&d)[DEG], const float (&J)[DEG], float h, float jp, int q,
-                                          uint32_t i, uint32_t sweep, uint32_t rep, uint32_t key0, uint32_t key1,
-                                          float m2beta, float m2blog2e) {
+                                          uint32_t i, uint32_t sweep, uint32_t rep, const KS& ks, float m2beta,
+                                          float m2blog2e) {
     constexpr int P = 2 * NQ;
     constexpr int BITS = 8 * sizeof(W);
     constexpr W MASK = P >= BITS ? ~(W)0 : (((W)1 << P) - 1);
@@ -203,9 +204,10 @@ __device__ __forceinline__ W update_fixed(W wi, const W (&d)[DEG], const float (
         uint32_t dq[DEG];
 #pragma unroll
         for (int m = 0; m < DEG; ++m) dq[m] = (uint32_t)(d[m] >> (32 * half)) >> q;
-        const uint32_t f = update_half<NQH, DEG>((uint32_t)(wi >> (32 * half)) >> q, dq,
-                                                 (uint32_t)(dlw >> (32 * half)) >> q, (uint32_t)(drw >> (32 * half)) >> q,
-                                                 J, h, jp, q, 4 * half, i, sweep, rep, key0, key1, m2beta, m2blog2e);
+        const uint32_t f = update_half<NQH, DEG, KS>((uint32_t)(wi >> (32 * half)) >> q, dq,
+                                                     (uint32_t)(dlw >> (32 * half)) >> q,
+                                                     (uint32_t)(drw >> (32 * half)) >> q, J, h, jp, q, 4 * half, i,
+                                                     sweep, rep, ks, m2beta, m2blog2e);
         flips |= (W)f << (32 * half);
     }
     return flips << q;
@@ -215,27 +217,28 @@ __device__ __forceinline__ W update_fixed(W wi, const W (&d)[DEG], const float (
 // nrep x n words (staged by the caller); order: nrep x kMaxClasses bytes;
 // parity: nrep words.  Counts accepted local flips into nacc and out-of-range
 // indices into bad.
-template <typename W, int MAXDEG, int NQC, bool INLINE>
-__device__ __forceinline__ void run_item_body(const Item& it, W* sw, uint8_t* order, uint32_t* parity, const Group& g,
-                                              bool& bad, unsigned long long& nacc);
+template <typename W, int MAXDEG, int NQC, bool INLINE, typename KS>
+__device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* sw, uint8_t* order, uint32_t* parity,
+                                              const Group& g, bool& bad, unsigned long long& nacc);
 
 // The single-instance kernel inlines the item loop; the batched kernel calls one
 // out-of-line copy per variant, so each variant keeps its own register budget.
 template <typename W, int MAXDEG, int NQC>
-__device__ __forceinline__ void run_item(const Item& it, W* sw, uint8_t* order, uint32_t* parity, const Group& g,
-                                         bool& bad, unsigned long long& nacc) {
-    run_item_body<W, MAXDEG, NQC, true>(it, sw, order, parity, g, bad, nacc);
+__device__ __forceinline__ void run_item(const Item& it, const PhiloxKeyTable& keys, W* sw, uint8_t* order,
+                                         uint32_t* parity, const Group& g, bool& bad, unsigned long long& nacc) {
+    run_item_body<W, MAXDEG, NQC, true, PhiloxKeysTab>(it, PhiloxKeysTab{keys}, sw, order, parity, g, bad, nacc);
 }
 
 template <typename W, int MAXDEG, int NQC>
 __device__ __noinline__ void run_item_call(const Item& it, W* sw, uint8_t* order, uint32_t* parity, const Group& g,
                                            bool& bad, unsigned long long& nacc) {
-    run_item_body<W, MAXDEG, NQC, false>(it, sw, order, parity, g, bad, nacc);
+    run_item_body<W, MAXDEG, NQC, false, PhiloxKeysReg>(it, PhiloxKeysReg{it.key0, it.key1}, sw, order, parity, g,
+                                                        bad, nacc);
 }
 
-template <typename W, int MAXDEG, int NQC, bool INLINE>
-__device__ __forceinline__ void run_item_body(const Item& it, W* sw, uint8_t* order, uint32_t* parity, const Group& g,
-                                              bool& bad, unsigned long long& nacc) {
+template <typename W, int MAXDEG, int NQC, bool INLINE, typename KS>
+__device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* sw, uint8_t* order, uint32_t* parity,
+                                              const Group& g, bool& bad, unsigned long long& nacc) {
     const int n = it.n, P = it.P, S = it.stride, nrep = it.nrep;
     const W mask = full_mask<W>(P);
     const int nclass_q = P == 1 ? 1 : ((P & 1) ? 3 : 2);
@@ -247,8 +250,8 @@ __device__ __forceinline__ void run_item_body(const Item& it, W* sw, uint8_t* or
         for (int step = 0; step < it.mcsteps; ++step) {
             const uint32_t sweep = (uint32_t)(it.sweep_base + (int64_t)gs * it.mcsteps + step);
             if (g.tid < nrep)
-                class_order(it.nclass, it.order_mode, it.key0, it.key1, sweep, it.replica0 + g.tid,
-                            order + g.tid * kMaxClasses, parity + g.tid);
+                class_order<KS>(it.nclass, it.order_mode, ks, sweep, it.replica0 + g.tid,
+                                order + g.tid * kMaxClasses, parity + g.tid);
             group_sync(g);
             for (int p = 0; p < it.nclass; ++p) {
                 for (int qq = 0; qq < nclass_q; ++qq) {
@@ -267,8 +270,8 @@ __device__ __forceinline__ void run_item_body(const Item& it, W* sw, uint8_t* or
                             const float h = __ldg(it.field + i);
                             const uint32_t rep = it.replica0 + rl;
                             if constexpr (NQC > 0) {
-                                const W fl = update_fixed<NQC, MAXDEG, W>(wi, d, J, h, jp, q, (uint32_t)i, sweep, rep,
-                                                                          it.key0, it.key1, m2beta, m2blog2e);
+                                const W fl = update_fixed<NQC, MAXDEG, W, KS>(wi, d, J, h, jp, q, (uint32_t)i, sweep,
+                                                                              rep, ks, m2beta, m2blog2e);
                                 rw[i] = wi ^ fl;
                                 nacc += sizeof(W) == 8 ? __popcll((unsigned long long)fl) : __popc((uint32_t)fl);
                             } else {
@@ -277,8 +280,8 @@ __device__ __forceinline__ void run_item_body(const Item& it, W* sw, uint8_t* or
                                 W flips = 0;
                                 const int nq = slice_count(P, q);
                                 for (int mb = 0; mb * 4 < nq; ++mb) {
-                                    const pq_u32x4 rnd = pq_philox(
-                                        pq_u32x4{(uint32_t)i, sweep, rep, (uint32_t)((q << 16) | mb)}, it.key0, it.key1);
+                                    const pq_u32x4 rnd = pq_philox_ks(
+                                        pq_u32x4{(uint32_t)i, sweep, rep, (uint32_t)((q << 16) | mb)}, ks);
                                     const uint32_t rw4[4] = {rnd.x, rnd.y, rnd.z, rnd.w};
 #pragma unroll
                                     for (int jj = 0; jj < 4; ++jj) {
@@ -331,10 +334,10 @@ __device__ __forceinline__ void run_item_body(const Item& it, W* sw, uint8_t* or
                                 if (m < it.maxdeg) e = __fadd_rn(e, flip_sign(J[m], bit_to_sign<W>(d[m], k)));
                             E = __fadd_rn(E, e);
                         }
-                        const pq_u32x4 rnd = pq_philox(
+                        const pq_u32x4 rnd = pq_philox_ks(
                             pq_u32x4{(uint32_t)i, sweep, it.replica0 + rl,
                                      (uint32_t)((1u << 24) | ((uint32_t)gm << 16) | (uint32_t)cls)},
-                            it.key0, it.key1);
+                            ks);
                         if (decide(E, pq_u01(rnd.x), m2beta, m2blog2e)) rw[i] = wi ^ mask;
                     }
                     s += g.nthr;

@@ -248,7 +248,7 @@ def anneal(problem, words, sched, P, temp, mcsteps=1, seed=0, global_moves=0, sw
 
 
 def anneal_replicas(problem, confs, sched, P, temp, mcsteps=1, seed=0, global_moves=0, order_mode=1,
-                    out=None, energies_out=None, stream=None):
+                    out=None, energies_out=None, stream=None, replica_base=0):
     """Host-buffer entry point: anneal R replicas given as int8 (R, n, P) +-1 host arrays.
 
     Copies the configurations to the device, packs them, anneals, computes the
@@ -263,7 +263,7 @@ def anneal_replicas(problem, confs, sched, P, temp, mcsteps=1, seed=0, global_mo
     d_spins = src.to(dev, non_blocking=True)
     words = problem.pack(d_spins)
     anneal(problem, words, sched, P, temp, mcsteps=mcsteps, seed=seed, global_moves=global_moves,
-           order_mode=order_mode, stream=stream)
+           order_mode=order_mode, stream=stream, replica_base=replica_base)
     E = problem.energies(words, P)
     fin = problem.unpack(words, P)
     if out is None:
