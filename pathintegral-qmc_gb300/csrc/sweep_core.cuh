@@ -253,31 +253,35 @@ __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* s
                 class_order<KS>(it.nclass, it.order_mode, ks, sweep, it.replica0 + g.tid,
                                 order + g.tid * kMaxClasses, parity + g.tid);
             group_sync(g);
+            // Phase = one update class.  Its spins share no coupling, so each thread takes
+            // its spins one at a time through every slice class (in the replica's parity
+            // order): the same result as slice class by slice class over all spins, with
+            // one barrier and one load of the neighbourhood per spin and class.
             for (int p = 0; p < it.nclass; ++p) {
-                for (int qq = 0; qq < nclass_q; ++qq) {
-                    int rl = 0, s = g.tid;
-                    while (s >= S) { s -= S; ++rl; }
-                    for (; rl < nrep;) {
-                        const int cls = order[rl * kMaxClasses + p];
-                        const int q = nclass_q == 2 ? (qq ^ (int)((parity[rl] >> p) & 1u)) : qq;
-                        if (s < it.csize[cls]) {
-                            const int i = cls * S + s;
-                            W* rw = sw + rl * n;
-                            const W wi = rw[i];
-                            W d[MAXDEG];
-                            float J[MAXDEG];
-                            load_site<W, MAXDEG>(rw, i, n, it.maxdeg, it.nbr, it.cpl, wi, d, J, bad);
-                            const float h = __ldg(it.field + i);
-                            const uint32_t rep = it.replica0 + rl;
+                int rl = 0, s = g.tid;
+                while (s >= S) { s -= S; ++rl; }
+                for (; rl < nrep;) {
+                    const int cls = order[rl * kMaxClasses + p];
+                    if (s < it.csize[cls]) {
+                        const int i = cls * S + s;
+                        W* rw = sw + rl * n;
+                        W wi = rw[i];
+                        W d[MAXDEG];
+                        float J[MAXDEG];
+                        load_site<W, MAXDEG>(rw, i, n, it.maxdeg, it.nbr, it.cpl, wi, d, J, bad);
+                        const float h = __ldg(it.field + i);
+                        const uint32_t rep = it.replica0 + rl;
+                        const uint32_t first = nclass_q == 2 ? (parity[rl] >> p) & 1u : 0u;
+                        for (int qq = 0; qq < nclass_q; ++qq) {
+                            const int q = nclass_q == 2 ? (qq ^ (int)first) : qq;
+                            W fl;
                             if constexpr (NQC > 0) {
-                                const W fl = update_fixed<NQC, MAXDEG, W, KS>(wi, d, J, h, jp, q, (uint32_t)i, sweep,
-                                                                              rep, ks, m2beta, m2blog2e);
-                                rw[i] = wi ^ fl;
-                                nacc += sizeof(W) == 8 ? __popcll((unsigned long long)fl) : __popc((uint32_t)fl);
+                                fl = update_fixed<NQC, MAXDEG, W, KS>(wi, d, J, h, jp, q, (uint32_t)i, sweep, rep, ks,
+                                                                      m2beta, m2blog2e);
                             } else {
                                 W dl, dr;
                                 trotter_diffs<W>(wi, P, mask, dl, dr);
-                                W flips = 0;
+                                fl = 0;
                                 const int nq = slice_count(P, q);
                                 for (int mb = 0; mb * 4 < nq; ++mb) {
                                     const pq_u32x4 rnd = pq_philox_ks(
@@ -295,19 +299,23 @@ __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* s
                                             const float t = __fadd_rn(flip_sign(jp, bit_to_sign<W>(dl, k)),
                                                                       flip_sign(jp, bit_to_sign<W>(dr, k)));
                                             const bool acc = decide(__fadd_rn(e, t), pq_u01(rw4[jj]), m2beta, m2blog2e);
-                                            flips |= (W)acc << k;
-                                            nacc += acc;
+                                            fl |= (W)acc << k;
                                         }
                                     }
                                 }
-                                rw[i] = wi ^ flips;
                             }
+                            // the neighbours are unchanged in this phase: only the spin's own bits move
+                            wi ^= fl;
+#pragma unroll
+                            for (int m = 0; m < MAXDEG; ++m) d[m] ^= fl;
+                            nacc += sizeof(W) == 8 ? __popcll((unsigned long long)fl) : __popc((uint32_t)fl);
                         }
-                        s += g.nthr;
-                        while (s >= S) { s -= S; ++rl; }
+                        rw[i] = wi;
                     }
-                    group_sync(g);
+                    s += g.nthr;
+                    while (s >= S) { s -= S; ++rl; }
                 }
+                group_sync(g);
             }
         }
         // world-line moves: flip spin i in every slice at once, classes in order
