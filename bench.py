@@ -361,21 +361,24 @@ def gpu_arm(args):
         e2e_s = max_over_ranks(e2e_s, dist, "cuda")
     e2e_value = whole_job_rate(updates, len(e2e_ms), world, e2e_s)
 
-    batched = densew = learnedw = None
+    batched = densew = learnedw = reforderw = None
     if not args.no_batched and rank == 0:
         batched = batched_workload(args, torch)
         densew = dense_workload(args, torch)
         learnedw = learned_vs_plain(args, torch, prob, R=args.learned_replicas)
+        reforderw = reforder_workload(args, torch)
 
     peak = measured_fp32_peak(lib, torch)
     achieved_tflops = value / world * FLOP_PER_UPDATE / 1e12
     ms_per_step = total_s / args.steps * 1e3
-    traffic = None
+    traffic, issue = None, None
     prof = os.path.join(ROOT, "profiles", "qa_fast_kernel_80x80_P20.traffic.json")
     if os.path.exists(prof):
         try:
             with open(prof) as f:
-                traffic = json.load(f).get("dram_bytes_per_launch")
+                pj = json.load(f)
+            traffic = pj.get("dram_bytes_per_launch")
+            issue = pj.get("issue")
         except (OSError, ValueError):
             traffic = None
     line = {
@@ -395,7 +398,8 @@ def gpu_arm(args):
                      "frac": achieved_tflops / peak, "traffic": traffic,
                      "note": "achieved = %d FP32 flop per spin-slice update x updates/s of the packed sweep "
                              "(qa_fast_kernel, one launch per step, CUDA events); peak = in-run FP32 FMA probe "
-                             "(no FP32 figure in the measured-peaks file)" % FLOP_PER_UPDATE},
+                             "(no FP32 figure in the measured-peaks file)" % FLOP_PER_UPDATE,
+                     "binding_unit": issue},
         "clocks": clk.summary(),
         "residual": {"best_slice_energy_per_spin_median": float(np.median(best)),
                      "best_slice_energy_per_spin_min": float(best.min())},
@@ -409,6 +413,8 @@ def gpu_arm(args):
         line["dense"] = densew
     if learnedw is not None:
         line["learned_vs_uniform"] = learnedw
+    if reforderw is not None:
+        line["reference_order"] = reforderw
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -606,6 +612,85 @@ def learned_vs_plain(args, torch, prob_big, R=1024, every=20):
     return out
 
 
+def reforder_workload(args, torch):
+    """Reference-order sweeps (the drop-in's bit-exact mode) on the 32x32 periodic P=20 lattice.
+
+    8 replicas (and 1) with synthetic permutations and uniform streams in the
+    reference's formats, one launch each, timed with CUDA events; the same kernel
+    the drop-in QuantumAnneal runs (exp close calls are not resolved here)."""
+    from piqmc import _device, _native, reforder, tools
+    import scipy.sparse as sps
+    L, P, steps = 32, 20, args.reforder_steps
+    n = L * L
+    g = np.random.default_rng(17)
+    J = sps.dok_matrix((n, n))
+    for y in range(L):
+        for x in range(L):
+            i = y * L + x
+            J[i, y * L + (x + 1) % L] = float(np.float32(g.uniform(-2, 2)))
+            J[i, ((y + 1) % L) * L + x] = float(np.float32(g.uniform(-2, 2)))
+    nbs = tools.GenerateNeighbors(n, J, 4)
+    idx, jv = reforder.split_neighbors(nbs)
+    sched = schedule(steps)
+    jp = torch.from_numpy(reforder.jperp_schedule(sched, P, TEMP)).cuda()
+    lib = _native.lib()
+    out = {"workload": "32x32 periodic, J~U[-2,2] fp32, P=20, T=0.05, %d steps, reference order (bit-exact mode), "
+                       "synthetic permutations and uniform streams" % steps}
+    for R in (1, 8):
+        perms = torch.from_numpy(np.stack([np.stack([g.permutation(n) for _ in range(steps)]) for _ in range(R)])
+                                 .astype(np.int32)).cuda()
+        cap = n * P * steps
+        rands = torch.from_numpy(g.integers(0, 2 ** 31 - 1, size=(R, cap), dtype=np.int64).astype(np.int32)).cuda()
+        spins0 = torch.from_numpy(np.repeat(np.where(g.random((R, n)) < 0.5, -1, 1).astype(np.int8)[:, :, None], P,
+                                            axis=2)).cuda()
+        d_idx, d_j = torch.from_numpy(idx).cuda(), torch.from_numpy(jv).cuda()
+        used = torch.zeros(R, dtype=torch.int64, device="cuda")
+        status = torch.zeros(1, dtype=torch.int32, device="cuda")
+        times = []
+        for it in range(3):
+            sp = spins0.clone()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            rc = lib.pq_qa_sparse_reforder(_device.ptr(sp), _device.ptr(d_idx), _device.ptr(d_j), n, n, idx.shape[1],
+                                           P, R, _device.ptr(jp), steps, 1, float(np.float32(TEMP)),
+                                           _device.ptr(perms), _device.ptr(rands), cap, _device.ptr(used), 0,
+                                           _device.ptr(status), _device.stream_handle())
+            e1.record()
+            torch.cuda.synchronize()
+            _native.check(rc, "pq_qa_sparse_reforder")
+            if int(status.item()) or int(used.min().item()) < 0:
+                raise RuntimeError("reference-order bench: status %d" % int(status.item()))
+            times.append(e0.elapsed_time(e1) * 1e-3)
+        out["replicas_%d" % R] = {"value": float(n) * P * steps * R / min(times), "unit": "updates/s",
+                                  "ms": 1e3 * min(times)}
+    # sa.Anneal's reference-order sweep, one replica, 100 temperatures 5 -> 0.05
+    temps = torch.from_numpy(np.linspace(5.0, 0.05, steps).astype(np.float32)).cuda()
+    perms = torch.from_numpy(np.stack([g.permutation(n) for _ in range(steps)])[None].astype(np.int32)).cuda()
+    rands = torch.from_numpy(g.integers(0, 2 ** 31 - 1, size=(1, n * steps), dtype=np.int64).astype(np.int32)).cuda()
+    s0 = torch.from_numpy(np.where(g.random((1, n)) < 0.5, -1, 1).astype(np.int8)).cuda()
+    d_idx, d_j = torch.from_numpy(idx).cuda(), torch.from_numpy(jv).cuda()
+    used = torch.zeros(1, dtype=torch.int64, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    times = []
+    for it in range(3):
+        sp = s0.clone()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        rc = lib.pq_sa_sparse_reforder(_device.ptr(sp), _device.ptr(d_idx), _device.ptr(d_j), n, idx.shape[1], 1,
+                                       _device.ptr(temps), steps, 1, _device.ptr(perms), _device.ptr(rands), n * steps,
+                                       _device.ptr(used), _device.ptr(status), _device.stream_handle())
+        e1.record()
+        torch.cuda.synchronize()
+        _native.check(rc, "pq_sa_sparse_reforder")
+        if int(status.item()) or int(used.min().item()) < 0:
+            raise RuntimeError("reference-order SA bench: status %d" % int(status.item()))
+        times.append(e0.elapsed_time(e1) * 1e-3)
+    out["sa_replicas_1"] = {"value": float(n) * steps / min(times), "unit": "updates/s", "ms": 1e3 * min(times)}
+    return out
+
+
 def only_arm(args):
     """One extra workload on its own (profiling entry point)."""
     import torch
@@ -615,6 +700,8 @@ def only_arm(args):
         out = batched_workload(args, torch)
     elif args.only == "dense":
         out = dense_workload(args, torch)
+    elif args.only == "reforder":
+        out = reforder_workload(args, torch)
     else:
         from piqmc import fast, tools
         import scipy.sparse as sps
@@ -656,13 +743,14 @@ def main():
     ap.add_argument("--rpc", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched, dense and learned extras")
-    ap.add_argument("--only", choices=["batched", "dense", "learned"], default=None,
+    ap.add_argument("--only", choices=["batched", "dense", "learned", "reforder"], default=None,
                     help="run one extra workload alone (for profiling) and print its JSON")
     ap.add_argument("--batched-count", type=int, default=256)
     ap.add_argument("--batched-steps", type=int, default=500)
     ap.add_argument("--dense-replicas", type=int, default=256)
     ap.add_argument("--dense-steps", type=int, default=1000)
     ap.add_argument("--learned-replicas", type=int, default=1024)
+    ap.add_argument("--reforder-steps", type=int, default=100)
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)

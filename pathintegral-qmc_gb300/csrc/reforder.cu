@@ -50,7 +50,7 @@ struct ExpPatch {
     int* close_cnt;
 };
 
-__device__ __forceinline__ double patched_exp(float xf, double q, const ExpPatch& ep) {
+__device__ __forceinline__ double patched_exp(float xf, double q, const ExpPatch& ep, bool record = true) {
     double e = exp((double)xf);
     const double d = fabs(e - q);
     const bool close = d <= 1e-15 * fmax(e, q) || (q == 0.0 && e < 1e-300);
@@ -62,7 +62,7 @@ __device__ __forceinline__ double patched_exp(float xf, double q, const ExpPatch
         if (ep.ov_x[mid] < xb) lo = mid + 1; else hi = mid;
     }
     if (lo < ep.ov_n && ep.ov_x[lo] == xb) return ep.ov_y[lo];
-    if (ep.close_cnt) {
+    if (ep.close_cnt && record) {
         const int slot = atomicAdd(ep.close_cnt, 1);
         if (slot < ep.close_cap) { ep.close_x[slot] = xb; ep.close_y[slot] = e; }
     }
@@ -196,6 +196,212 @@ __global__ void __launch_bounds__(32) qa_sparse_reforder_kernel(
         __syncwarp();
         for (int64_t t = threadIdx.x; t < (int64_t)n * P; t += blockDim.x) gs[t] = sh_spins[t];
     }
+}
+
+// The same sweep with the warp sharing the work (replicas whose spins fit in
+// shared memory, maxnb 4 or 5).  The permutation is taken in blocks of 32
+// positions, lane l owning position l:
+//  * each lane loads its spin's neighbour row and couplings (the global loads of
+//    the next block are issued before the current block is resolved) and folds
+//    the current neighbour spins into signed couplings; a neighbour at an earlier
+//    position p of the same block is recorded (its term changes sign if p flips);
+//  * the accumulator is a sequential chain (FP32, one rounding per term, carried
+//    across spins as the reference carries it): all lanes walk the positions in
+//    order computing it -- the sum of position l and the number of uniforms
+//    consumed before it are kept by lane l -- until a position depends on an
+//    earlier position of the block whose decision is still open;
+//  * then the open positions decide in parallel, each lane with its own uniform
+//    (the window of the next 32 values of the stream) and exactly
+//    ref_accept's arithmetic; their flips resolve the pending sign changes and
+//    the walk continues.
+// Flips are written back at the end of the block.  Same results, same uniforms
+// consumed and the same close calls (recorded by the deciding lane) as
+// qa_sparse_reforder_kernel.
+template <bool FP64, int MAXNB>
+struct RefBlockIn {
+    int i;
+    int j[MAXNB];
+    float v[MAXNB];
+};
+
+template <bool FP64, int MAXNB, bool FIXQ2>
+__global__ void __launch_bounds__(32) qa_sparse_reforder_warp_kernel(
+    int8_t* __restrict__ spins, const int32_t* __restrict__ nb_idx, const float* __restrict__ nb_j, int n, int nperm,
+    int maxnb, int P, int R, const float* __restrict__ jperp, int nsched, int mcsteps, float temp,
+    const int32_t* __restrict__ perms, const int32_t* __restrict__ rands, int64_t rand_stride,
+    int64_t* __restrict__ rand_used, int flags, ExpPatch ep, int32_t* status) {
+    static_assert(MAXNB + 3 <= 8, "record holds MAXNB terms, two Trotter terms and s2");
+    extern __shared__ __align__(16) int8_t sh[];
+    int8_t* s = sh;                                                                             // [n][P]
+    uint8_t* pos_of = reinterpret_cast<uint8_t*>(sh + (((size_t)n * P + 15) & ~(size_t)15));   // [n]
+    // records of the block's 32 positions (+ one spare so position l + 1 can be read ahead)
+    float4* rec = reinterpret_cast<float4*>(pos_of + (((size_t)n + 15) & ~(size_t)15));        // [33][2]
+    uint32_t* rec_dep = reinterpret_cast<uint32_t*>(rec + 66);                                  // [36]
+    uint8_t* rec_p = reinterpret_cast<uint8_t*>(rec_dep + 36);                                  // [32][MAXNB]
+    const int r = blockIdx.x;
+    if (r >= R) return;
+    const int lane = threadIdx.x;
+    int8_t* gs = spins + (int64_t)r * n * P;
+    for (int64_t t = lane; t < (int64_t)n * P; t += 32) s[t] = gs[t];
+    for (int t = lane; t < n; t += 32) pos_of[t] = 0xFF;
+    __syncwarp();
+    const int32_t* pr = perms + (int64_t)r * nsched * mcsteps * nperm;
+    const int32_t* rr = rands + (int64_t)r * rand_stride;
+    const int64_t cap = rand_stride;
+    int64_t used = 0;
+    bool bad = false, dead = false;
+    const int nblk = (nperm + 31) / 32;
+    const int64_t total = (int64_t)nsched * mcsteps * P * nblk;   // blocks in the whole run
+
+    // this lane's inputs of block number b (global loads only)
+    auto load_in = [&](int64_t b, RefBlockIn<FP64, MAXNB>& in) {
+        in.i = -1;
+        if (b >= total) return;
+        const int64_t sweep = b / ((int64_t)P * nblk);
+        const int t = (int)(b % nblk) * 32 + lane;
+        if (t >= nperm) return;
+        int i = __ldg(pr + sweep * nperm + t);
+        if ((unsigned)i >= (unsigned)n) { bad = true; i = 0; }
+        in.i = i;
+#pragma unroll
+        for (int m = 0; m < MAXNB; ++m) {
+            in.j[m] = __ldg(nb_idx + (int64_t)i * maxnb + m);
+            in.v[m] = __ldg(nb_j + (int64_t)i * maxnb + m);
+        }
+    };
+    RefBlockIn<FP64, MAXNB> cur, nxt;
+    load_in(0, cur);
+    int64_t b = 0;
+    for (int g = 0; g < nsched && !dead; ++g) {
+        const float jpf = jperp[g];
+        for (int step = 0; step < mcsteps && !dead; ++step) {
+            for (int k = 0; k < P && !dead; ++k) {
+                int tl = P - 1, tr = 1;   // Q1 as shipped (piqmc/qmc.pyx:115-117)
+                if (flags & PQ_FIX_Q1) { tl = k == 0 ? P - 1 : k - 1; tr = k == P - 1 ? 0 : k + 1; }
+                float ediff = 0.0f;       // Q2 as shipped: reset once per slice (piqmc/qmc.pyx:134-135)
+                for (int blk = 0; blk < nblk && !dead; ++blk, ++b) {
+                    load_in(b + 1, nxt);
+                    const int nb = min(32, nperm - blk * 32);
+                    const int i = cur.i;
+                    if (lane < nb) pos_of[i] = (uint8_t)lane;
+                    __syncwarp();
+                    if (lane < nb) {
+                        const int8_t* si_p = s + (int64_t)i * P;
+                        float x[8];
+                        uint32_t dep = 0;
+#pragma unroll
+                        for (int m = 0; m < MAXNB; ++m) {
+                            int j = cur.j[m];
+                            if ((unsigned)j >= (unsigned)n) { bad = true; j = i; }
+                            float v = cur.v[m];
+                            uint8_t pp = 0xFF;
+                            if (j != i) {
+                                if (s[(int64_t)j * P + k] <= 0) v = -v;
+                                const uint8_t q = pos_of[j];
+                                if (q < lane) { pp = q; dep |= 1u << q; }
+                            }
+                            x[m] = v;
+                            rec_p[lane * MAXNB + m] = pp;
+                        }
+                        x[MAXNB] = si_p[tl] > 0 ? jpf : -jpf;
+                        x[MAXNB + 1] = si_p[tr] > 0 ? jpf : -jpf;
+                        x[MAXNB + 2] = -2.0f * (float)si_p[k];
+                        if constexpr (!FP64) {
+                            // the FP32 path stores the terms s2 v themselves (exact: no 2J overflows here)
+#pragma unroll
+                            for (int m = 0; m < MAXNB + 2; ++m) x[m] = __fmul_rn(x[MAXNB + 2], x[m]);
+                        }
+#pragma unroll
+                        for (int m = MAXNB + 3; m < 8; ++m) x[m] = 0.0f;
+                        rec[2 * lane] = make_float4(x[0], x[1], x[2], x[3]);
+                        rec[2 * lane + 1] = make_float4(x[4], x[5], x[6], x[7]);
+                        rec_dep[lane] = dep;
+                    }
+                    const int32_t rwin = used + lane < cap ? __ldg(rr + used + lane) : 0;
+                    __syncwarp();
+                    uint32_t flipmask = 0;
+                    int c = 0;               // uniforms consumed in this block so far
+                    float my_e = 0.0f;       // this lane's position: its sum ...
+                    int my_c = 0;            // ... and the uniforms consumed before it
+                    int l = 0;
+                    while (l < nb) {
+                        const int start = l;
+                        const uint32_t open = ~((1u << start) - 1u);   // positions >= start are undecided
+                        // records of position l + 1 are loaded while position l's sum is chained
+                        uint32_t dep = rec_dep[l];
+                        float4 ra = rec[2 * l], rb = rec[2 * l + 1];
+                        for (; l < nb; ++l) {
+                            if (dep & open) break;
+                            const uint32_t dep_n = rec_dep[l + 1];
+                            const float4 ra_n = rec[2 * l + 2], rb_n = rec[2 * l + 3];
+                            float x[8] = {ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w};
+                            const uint32_t dep_l = dep;
+                            dep = dep_n;
+                            ra = ra_n;
+                            rb = rb_n;
+                            if (dep_l & flipmask) {
+#pragma unroll
+                                for (int m = 0; m < MAXNB; ++m) {
+                                    const uint32_t pp = rec_p[l * MAXNB + m];
+                                    if (pp != 0xFFu && ((flipmask >> pp) & 1u)) x[m] = -x[m];
+                                }
+                            }
+                            if (FIXQ2) ediff = 0.0f;
+                            if constexpr (FP64) {
+                                const float s2 = x[MAXNB + 2];
+#pragma unroll
+                                for (int m = 0; m < MAXNB + 2; ++m) ediff = acc2<true>(ediff, s2, x[m]);
+                            } else {
+#pragma unroll
+                                for (int m = 0; m < MAXNB + 2; ++m) ediff = __fadd_rn(ediff, x[m]);
+                            }
+                            if (lane == l) { my_e = ediff; my_c = c; }
+                            c += ediff > 0.0f ? 0 : 1;
+                        }
+                        // decisions of positions [start, l), one per lane
+                        const int32_t rv = __shfl_sync(0xffffffffu, rwin, my_c & 31);
+                        bool flip = false, out = false;
+                        if (lane >= start && lane < l) {
+                            if (my_e > 0.0f) {
+                                flip = true;
+                            } else if (used + my_c >= cap) {
+                                out = true;
+                            } else {
+                                const float xf = __fdiv_rn(my_e, temp);
+                                const int quick = fp32_decide(xf, rv);
+                                if (quick >= 0) {
+                                    flip = quick != 0;
+                                } else {
+                                    const double q = (double)rv / 2147483647.0;   // glibc RAND_MAX
+                                    flip = patched_exp(xf, q, ep) > q;
+                                }
+                            }
+                        }
+                        if (__any_sync(0xffffffffu, out)) {
+                            if (lane == 0) pq_set_status(status, PQ_ERR_RAND_EXHAUSTED);
+                            dead = true;
+                            break;
+                        }
+                        flipmask |= __ballot_sync(0xffffffffu, flip);
+                    }
+                    used += c;
+                    if (lane < nb) {
+                        if ((flipmask >> lane) & 1u) s[(int64_t)i * P + k] = (int8_t)-s[(int64_t)i * P + k];
+                        pos_of[i] = 0xFF;
+                    }
+                    __syncwarp();
+                    cur = nxt;
+                }
+            }
+        }
+    }
+    bad = __any_sync(0xffffffffu, bad);   // each lane saw its own positions' indices
+    if (lane == 0) {
+        if (bad) pq_set_status(status, PQ_ERR_BAD_INDEX);
+        rand_used[r] = (dead || bad) ? -1 : used;
+    }
+    __syncwarp();
+    for (int64_t t = lane; t < (int64_t)n * P; t += 32) gs[t] = s[t];
 }
 
 __global__ void qa_dense_reforder_kernel(int8_t* __restrict__ spins, const double* __restrict__ J, int n,
@@ -370,6 +576,156 @@ __global__ void sa_bipartite_reforder_kernel(int8_t* __restrict__ spins, const d
     rand_used[r] = rng.used;
 }
 
+// sa.Anneal with the warp sharing the work (spins in shared memory, maxnb <= 8).
+// The energy difference is reset for every spin (piqmc/sa.pyx:119), so the sums
+// of a block's 32 positions are independent except through neighbours flipped
+// earlier in the same block.  Each pass takes the longest run of open positions
+// whose in-block neighbours are all decided: their sums are computed in parallel
+// (each lane its own FP32 chain in the reference's term order), the uniforms they
+// consume are numbered by a ballot prefix count (a position consumes one when
+// ediff < 0, :114-117), and they decide in parallel with ref_accept's arithmetic.
+// Same results, uniforms and close calls as sa_sparse_reforder_kernel.
+template <bool FP64>
+__global__ void __launch_bounds__(32) sa_sparse_reforder_warp_kernel(
+    int8_t* __restrict__ spins, const int32_t* __restrict__ nb_idx, const float* __restrict__ nb_j, int n, int maxnb,
+    int R, const float* __restrict__ temps, int nsched, int mcsteps, const int32_t* __restrict__ perms,
+    const int32_t* __restrict__ rands, int64_t rand_stride, int64_t* __restrict__ rand_used, ExpPatch ep,
+    int32_t* status) {
+    constexpr int MAXNB = 8;
+    extern __shared__ __align__(16) int8_t sh[];
+    int8_t* s = sh;                                                                      // [n]
+    uint8_t* pos_of = reinterpret_cast<uint8_t*>(sh + (((size_t)n + 15) & ~(size_t)15));  // [n]
+    const int r = blockIdx.x;
+    if (r >= R) return;
+    const int lane = threadIdx.x;
+    int8_t* gs = spins + (int64_t)r * n;
+    for (int t = lane; t < n; t += 32) { s[t] = gs[t]; pos_of[t] = 0xFF; }
+    __syncwarp();
+    const int32_t* pr = perms + (int64_t)r * nsched * mcsteps * n;
+    const int32_t* rr = rands + (int64_t)r * rand_stride;
+    const int64_t cap = rand_stride;
+    int64_t used = 0;
+    bool bad = false, dead = false;
+    const int nblk = (n + 31) / 32;
+    const int64_t total = (int64_t)nsched * mcsteps * nblk;
+    struct In { int i; int j[MAXNB]; float v[MAXNB]; };
+    auto load_in = [&](int64_t b, In& in) {
+        in.i = -1;
+        if (b >= total) return;
+        const int64_t sweep = b / nblk;
+        const int t = (int)(b % nblk) * 32 + lane;
+        if (t >= n) return;
+        int i = __ldg(pr + sweep * n + t);
+        if ((unsigned)i >= (unsigned)n) { bad = true; i = 0; }
+        in.i = i;
+#pragma unroll
+        for (int m = 0; m < MAXNB; ++m) {
+            in.j[m] = m < maxnb ? __ldg(nb_idx + (int64_t)i * maxnb + m) : i;
+            in.v[m] = m < maxnb ? __ldg(nb_j + (int64_t)i * maxnb + m) : 0.0f;
+        }
+    };
+    In cur, nxt;
+    load_in(0, cur);
+    int64_t b = 0;
+    for (int g = 0; g < nsched && !dead; ++g) {
+        const float temp = temps[g];
+        for (int step = 0; step < mcsteps && !dead; ++step) {
+            for (int blk = 0; blk < nblk && !dead; ++blk, ++b) {
+                load_in(b + 1, nxt);
+                const int nb = min(32, n - blk * 32);
+                const int i = cur.i;
+                if (lane < nb) pos_of[i] = (uint8_t)lane;
+                __syncwarp();
+                float x[MAXNB];
+                uint8_t pp[MAXNB];
+                uint32_t dep = 0;
+                float s2 = 0.0f;
+                if (lane < nb) {
+                    s2 = -2.0f * (float)s[i];
+#pragma unroll
+                    for (int m = 0; m < MAXNB; ++m) {
+                        int j = cur.j[m];
+                        float v = cur.v[m];
+                        pp[m] = 0xFF;
+                        if (m < maxnb && j != i) {
+                            if ((unsigned)j >= (unsigned)n) { bad = true; j = i; }
+                            else {
+                                if (s[j] <= 0) v = -v;
+                                const uint8_t q = pos_of[j];
+                                if (q < lane) { pp[m] = q; dep |= 1u << q; }
+                            }
+                        }
+                        x[m] = v;
+                    }
+                }
+                const int32_t rwin = used + lane < cap ? __ldg(rr + used + lane) : 0;
+                uint32_t flipmask = 0;
+                int c = 0;
+                int start = 0;
+                while (start < nb) {
+                    const bool ready = (dep & ~((1u << start) - 1u)) == 0;
+                    const uint32_t wait = __ballot_sync(0xffffffffu, lane >= start && lane < nb && !ready);
+                    const int end = wait ? __ffs(wait) - 1 : nb;
+                    const bool mine = lane >= start && lane < end;
+                    float ediff = 0.0f;
+                    if (mine) {
+#pragma unroll
+                        for (int m = 0; m < MAXNB; ++m) {
+                            if (m < maxnb) {
+                                const float v = (pp[m] != 0xFF && ((flipmask >> pp[m]) & 1u)) ? -x[m] : x[m];
+                                ediff = acc2<FP64>(ediff, s2, v);
+                            }
+                        }
+                    }
+                    const bool consume = mine && !(ediff >= 0.0f);
+                    const uint32_t cons = __ballot_sync(0xffffffffu, consume);
+                    const int my_c = c + __popc(cons & ((1u << lane) - 1u));
+                    const int32_t rv = __shfl_sync(0xffffffffu, rwin, my_c & 31);
+                    bool flip = false, out = false;
+                    if (mine) {
+                        if (!consume) {
+                            flip = true;
+                        } else if (used + my_c >= cap) {
+                            out = true;
+                        } else {
+                            const float xf = __fdiv_rn(ediff, temp);
+                            const int quick = fp32_decide(xf, rv);
+                            if (quick >= 0) {
+                                flip = quick != 0;
+                            } else {
+                                const double q = (double)rv / 2147483647.0;   // glibc RAND_MAX
+                                flip = patched_exp(xf, q, ep) > q;
+                            }
+                        }
+                    }
+                    if (__any_sync(0xffffffffu, out)) {
+                        if (lane == 0) pq_set_status(status, PQ_ERR_RAND_EXHAUSTED);
+                        dead = true;
+                        break;
+                    }
+                    flipmask |= __ballot_sync(0xffffffffu, flip);
+                    c += __popc(cons);
+                    start = end;
+                }
+                used += c;
+                if (lane < nb) {
+                    if ((flipmask >> lane) & 1u) s[i] = (int8_t)-s[i];
+                    pos_of[i] = 0xFF;
+                }
+                __syncwarp();
+                cur = nxt;
+            }
+        }
+    }
+    bad = __any_sync(0xffffffffu, bad);
+    if (lane == 0) {
+        if (bad) pq_set_status(status, PQ_ERR_BAD_INDEX);
+        rand_used[r] = (dead || bad) ? -1 : used;
+    }
+    __syncwarp();
+    for (int t = lane; t < n; t += 32) gs[t] = s[t];
+}
+
 __global__ void exp_probe_kernel(const float* __restrict__ x, double* __restrict__ y, int64_t n) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) y[i] = exp((double)x[i]);
@@ -408,10 +764,34 @@ int launch_qa_sparse_t(int8_t* spins, const int32_t* nb_idx, const float* nb_j, 
 }
 
 template <bool FP64, int MAXNB>
+size_t warp_kernel_smem(int n, int P) {
+    return (((size_t)n * P + 15) & ~(size_t)15) + (((size_t)n + 15) & ~(size_t)15) + 33 * 32 + 36 * 4 + 32 * MAXNB;
+}
+
+template <bool FP64, int MAXNB>
 int launch_qa_sparse_s(int8_t* spins, const int32_t* nb_idx, const float* nb_j, int n, int nperm, int maxnb, int P,
                        int R, const float* jperp, int nsched, int mcsteps, float temp, const int32_t* perms,
                        const int32_t* rands, int64_t rand_stride, int64_t* rand_used, int flags, const ExpPatch& ep,
                        int32_t* status, cudaStream_t stream) {
+    if constexpr (MAXNB > 0) {
+        const size_t smem = warp_kernel_smem<FP64, MAXNB>(n, P);
+        if (smem <= kRefSmemMax + 8192) {
+            if (flags & PQ_FIX_Q2) {
+                PQ_CUDA_TRY(cudaFuncSetAttribute(qa_sparse_reforder_warp_kernel<FP64, MAXNB, true>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                qa_sparse_reforder_warp_kernel<FP64, MAXNB, true><<<R, 32, smem, stream>>>(
+                    spins, nb_idx, nb_j, n, nperm, maxnb, P, R, jperp, nsched, mcsteps, temp, perms, rands,
+                    rand_stride, rand_used, flags, ep, status);
+            } else {
+                PQ_CUDA_TRY(cudaFuncSetAttribute(qa_sparse_reforder_warp_kernel<FP64, MAXNB, false>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                qa_sparse_reforder_warp_kernel<FP64, MAXNB, false><<<R, 32, smem, stream>>>(
+                    spins, nb_idx, nb_j, n, nperm, maxnb, P, R, jperp, nsched, mcsteps, temp, perms, rands,
+                    rand_stride, rand_used, flags, ep, status);
+            }
+            return pq_launch_status();
+        }
+    }
     if ((size_t)n * P <= kRefSmemMax)
         return launch_qa_sparse_t<FP64, MAXNB, true>(spins, nb_idx, nb_j, n, nperm, maxnb, P, R, jperp, nsched, mcsteps,
                                                       temp, perms, rands, rand_stride, rand_used, flags, ep, status, stream);
@@ -522,6 +902,24 @@ int pq_sa_sparse_reforder_ex(int8_t* spins, const int32_t* nb_idx, const float* 
     if (maxnb < 0 || !spins || !rand_used || (maxnb > 0 && (!nb_idx || !nb_j))) return PQ_ERR_INVALID_ARG;
     if (R == 0) return PQ_OK;
     ExpPatch ep = make_patch(ov_x, ov_y, ov_n, close_x, close_y, close_cap, close_cnt);
+    const size_t wsmem = (((size_t)n + 15) & ~(size_t)15) * 2;
+    if (maxnb <= 8 && wsmem <= kRefSmemMax) {
+        cudaStream_t st = (cudaStream_t)stream;
+        if (flags & PQ_ACC_FP64) {
+            PQ_CUDA_TRY(cudaFuncSetAttribute(sa_sparse_reforder_warp_kernel<true>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsmem));
+            sa_sparse_reforder_warp_kernel<true><<<R, 32, wsmem, st>>>(spins, nb_idx, nb_j, n, maxnb, R, temps, nsched,
+                                                                       mcsteps, perms, rands, rand_stride, rand_used,
+                                                                       ep, status);
+        } else {
+            PQ_CUDA_TRY(cudaFuncSetAttribute(sa_sparse_reforder_warp_kernel<false>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsmem));
+            sa_sparse_reforder_warp_kernel<false><<<R, 32, wsmem, st>>>(spins, nb_idx, nb_j, n, maxnb, R, temps,
+                                                                        nsched, mcsteps, perms, rands, rand_stride,
+                                                                        rand_used, ep, status);
+        }
+        return pq_launch_status();
+    }
     const dim3 grid((R + kRefThreads - 1) / kRefThreads), block(kRefThreads);
     if (flags & PQ_ACC_FP64)
         sa_sparse_reforder_kernel<true><<<grid, block, 0, (cudaStream_t)stream>>>(

@@ -181,6 +181,61 @@ def test_random_cases_vs_oracle(piqmc, flags):
             assert used[r] == u
 
 
+@pytest.mark.parametrize("seed", [0, 1])
+def test_random_sa_cases_vs_oracle(piqmc, seed):
+    """sa.Anneal's reference-order sweep (several blocks of 32 positions, fields, a hot schedule)."""
+    from piqmc import reforder
+    g = np.random.default_rng(10 + seed)
+    for L, periodic in [(7, True), (5, False), (9, True)]:
+        J = lattice(L, periodic, g, dist=lambda r: r.normal(), fields=lambda r: r.normal(0, 0.5))
+        n = L * L
+        nbs = oracle.generate_neighbors(n, J, 5)
+        idx, jv = reforder.split_neighbors(nbs)
+        sched = np.linspace(3.0, 0.2, 12)
+        R = 3
+        spins = np.where(g.random((R, n)) < 0.5, -1, 1).astype(np.int8)
+        perms = np.array([oracle.reference_perms(np.random.RandomState(r), n, 24) for r in range(R)])
+        rands = g.integers(0, 2 ** 31 - 1, size=(R, n * 24), dtype=np.int64).astype(np.int32)
+        out, used = reforder.anneal(spins, idx, jv, sched, 2, perms, rands)
+        out = out.cpu().numpy()
+        for r in range(R):
+            sp = spins[r].copy()
+            u = oracle.sa_sparse(sp, nbs, sched, 2, perms[r], rands[r])
+            np.testing.assert_array_equal(out[r], sp)
+            assert used[r] == u
+
+
+def test_fp64_accumulator_with_huge_couplings(piqmc):
+    """Couplings near FP32's range switch the sweeps to the FP64 accumulator (2J would overflow)."""
+    from piqmc import reforder
+    g = np.random.default_rng(5)
+    J = lattice(6, True, g, dist=lambda r: float(np.float32(r.choice([-1, 1]) * r.uniform(1.0, 1.6) * 2.0 ** 126)))
+    n = 36
+    nbs = oracle.generate_neighbors(n, J, 4)
+    idx, jv = reforder.split_neighbors(nbs)
+    assert reforder._acc_flag(jv)
+    R, P = 2, 4
+    spins = np.where(g.random((R, n, P)) < 0.5, -1, 1).astype(np.int8)
+    sched = np.linspace(2.0, 0.5, 6)
+    perms = np.array([oracle.reference_perms(np.random.RandomState(r), n, 6) for r in range(R)])
+    rands = g.integers(0, 2 ** 31 - 1, size=(R, n * P * 6), dtype=np.int64).astype(np.int32)
+    out, used = reforder.quantum_anneal(spins, idx, jv, sched, 1, 1e30, perms, rands, flags=3)
+    out = out.cpu().numpy()
+    for r in range(R):
+        sp = spins[r].copy()
+        u = oracle.qa_sparse(sp, nbs, sched, 1, 1e30, perms[r], rands[r], flags=3)
+        np.testing.assert_array_equal(out[r], sp)
+        assert used[r] == u
+    s1 = np.where(g.random((R, n)) < 0.5, -1, 1).astype(np.int8)
+    out, used = reforder.anneal(s1, idx, jv, np.linspace(1e30, 1e29, 6), 1, perms, rands[:, : n * 6])
+    out = out.cpu().numpy()
+    for r in range(R):
+        sp = s1[r].copy()
+        u = oracle.sa_sparse(sp, nbs, np.linspace(1e30, 1e29, 6), 1, perms[r], rands[r, : n * 6])
+        np.testing.assert_array_equal(out[r], sp)
+        assert used[r] == u
+
+
 def test_edge_cases(piqmc):
     g = np.random.default_rng(7)
     J = lattice(4, True, g)
