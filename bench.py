@@ -691,6 +691,41 @@ def reforder_workload(args, torch):
     return out
 
 
+def gemm_workload(args, torch):
+    """The tcgen05/TMA GEMM (pq_tc_gemm_bf16) alone: the dense recompute's shape and two large ones.
+
+    Ten back-to-back calls between CUDA events (the launches queue, so host-side
+    tensor-map encoding is hidden); checked against torch's product of the same BF16
+    operands; cuBLAS timed beside it for reference."""
+    from piqmc.tensor import gemm_bf16
+    torch.manual_seed(0)
+    out = {"workload": "D = A B^T, BF16 operands, FP32 accumulate and output", "shapes": []}
+    for (M, N, K) in [(8192, 512, 1024), (8192, 8192, 8192), (16384, 4096, 4096)]:
+        A = torch.randn(M, K, device="cuda").to(torch.bfloat16)
+        B = torch.randn(N, K, device="cuda").to(torch.bfloat16)
+        D = torch.empty(M, N, device="cuda")
+        for _ in range(3):
+            gemm_bf16(A, B, out=D)
+        torch.cuda.synchronize()
+
+        def timed(fn):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(10):
+                fn()
+            e1.record()
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1) * 1e-3 / 10
+
+        t = min(timed(lambda: gemm_bf16(A, B, out=D)) for _ in range(3))
+        tc = min(timed(lambda: torch.matmul(A, B.T)) for _ in range(3))
+        ref = A[:256].float() @ B.float().T
+        err = float((D[:256] - ref).abs().max().item())
+        out["shapes"].append({"M": M, "N": N, "K": K, "us": t * 1e6, "tflops": 2.0 * M * N * K / t / 1e12,
+                              "cublas_us": tc * 1e6, "max_abs_err_vs_fp32_product": err})
+    return out
+
+
 def only_arm(args):
     """One extra workload on its own (profiling entry point)."""
     import torch
@@ -702,6 +737,8 @@ def only_arm(args):
         out = dense_workload(args, torch)
     elif args.only == "reforder":
         out = reforder_workload(args, torch)
+    elif args.only == "gemm":
+        out = gemm_workload(args, torch)
     else:
         from piqmc import fast, tools
         import scipy.sparse as sps
@@ -743,7 +780,7 @@ def main():
     ap.add_argument("--rpc", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched, dense and learned extras")
-    ap.add_argument("--only", choices=["batched", "dense", "learned", "reforder"], default=None,
+    ap.add_argument("--only", choices=["batched", "dense", "learned", "reforder", "gemm"], default=None,
                     help="run one extra workload alone (for profiling) and print its JSON")
     ap.add_argument("--batched-count", type=int, default=256)
     ap.add_argument("--batched-steps", type=int, default=500)

@@ -12,7 +12,9 @@
 //    TMEM accumulator and commits them to the stage's "empty" mbarrier, which hands
 //    the stage back to the producer; a final commit signals "done";
 //  * all four warps then read the accumulator with tcgen05.ld (warp w owns rows
-//    32w..32w+31) and write D = alpha * acc + bias.
+//    32w..32w+31), apply D = alpha * acc + bias and write it into the (now free)
+//    ring in 128-byte-swizzled 128 x 32 panels, which one thread stores with TMA
+//    (cp.async.bulk.tensor, coalesced whatever the row stride of D).
 // Stage layout: A then B, each [rows][64] BF16 as the TMA swizzle writes it (rows
 // of 128 B, 8-row atoms of 1024 B), every stage 1024-byte aligned.
 //
@@ -45,7 +47,7 @@ struct Cfg {
 template <int BN>
 __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA,
                                                          const __grid_constant__ CUtensorMap tmB,
-                                                         float* __restrict__ D, int ldd, int K, float alpha,
+                                                         const __grid_constant__ CUtensorMap tmD, int K, float alpha,
                                                          const float* __restrict__ bias, int32_t* status) {
     using C = Cfg<BN>;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -137,23 +139,34 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__
     tc::fence_after_sync();
     __syncthreads();
     if (!waited && threadIdx.x == 0) pq_set_status(status, PQ_ERR_TIMEOUT);
-    if (waited && !*abort_flag && nk > 0) {
-        const int row = m0 + 32 * warp + lane;
+    const bool good = waited && !*abort_flag && nk > 0;
+    if (good) {
+        const int rl = 32 * warp + lane;   // row within the tile = TMEM lane
 #pragma unroll 1
         for (int c0 = 0; c0 < BN; c0 += 32) {
             float v[32];
             tc::tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
-            float* dst = D + (size_t)row * ldd + n0 + c0;
+            // panel c0 / 32: [128 rows][32 floats], 16-byte unit u of row r at unit u ^ (r % 8)
+            unsigned char* panel = smem + (c0 / 32) * (BM * 128);
 #pragma unroll
-            for (int j = 0; j < 32; j += 4) {
+            for (int u = 0; u < 8; ++u) {
+                const int j = 4 * u;
                 float4 o;
                 o.x = alpha * v[j] + (bias ? bias[n0 + c0 + j] : 0.0f);
                 o.y = alpha * v[j + 1] + (bias ? bias[n0 + c0 + j + 1] : 0.0f);
                 o.z = alpha * v[j + 2] + (bias ? bias[n0 + c0 + j + 2] : 0.0f);
                 o.w = alpha * v[j + 3] + (bias ? bias[n0 + c0 + j + 3] : 0.0f);
-                *reinterpret_cast<float4*>(dst + j) = o;
+                *reinterpret_cast<float4*>(panel + rl * 128 + ((u ^ (rl & 7)) * 16)) = o;
             }
         }
+        tc::fence_async_shared();
+    }
+    __syncthreads();
+    if (good && threadIdx.x == 0) {
+#pragma unroll 1
+        for (int c0 = 0; c0 < BN; c0 += 32) tc::tma_store_2d(&tmD, n0 + c0, m0, base + (c0 / 32) * (BM * 128));
+        tc::tma_store_commit();
+        tc::tma_store_wait_read();
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -161,12 +174,13 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__
     if (warp == 0) tc::tmem_dealloc(tmem, BN);
 }
 
-// Row-major BF16 [rows][ld] matrix of which the first `cols` columns are used, as a
-// 2-D tensor map with a 64-column (128-byte) x box_rows box and the 128-byte swizzle.
-int encode_map(CUtensorMap* map, const void* ptr, int rows, int cols, int ld, int box_rows) {
+// Row-major [rows][ld] matrix of `esize`-byte elements (BF16 operands, FP32 result) of
+// which the first `cols` columns are used, as a 2-D tensor map with a 128-byte-wide
+// x box_rows box and the 128-byte swizzle.
+int encode_map(CUtensorMap* map, const void* ptr, int rows, int cols, int ld, int box_rows, int esize = 2) {
     const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-    const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
-    const cuuint32_t box[2] = {(cuuint32_t)KC, (cuuint32_t)box_rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * esize};
+    const cuuint32_t box[2] = {(cuuint32_t)(128 / esize), (cuuint32_t)box_rows};
     const cuuint32_t estr[2] = {1u, 1u};
     // the driver's encoder, looked up through the runtime so the library does not link libcuda
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
@@ -177,7 +191,8 @@ int encode_map(CUtensorMap* map, const void* ptr, int rows, int cols, int ld, in
         if (q != cudaDriverEntryPointSuccess || !fn) return PQ_ERR_NO_DEVICE;
         encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
     }
-    const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims, strides, box,
+    const CUresult r = encode(map, esize == 2 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                              const_cast<void*>(ptr), dims, strides, box,
                               estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? PQ_OK : PQ_ERR_INVALID_ARG;
@@ -187,10 +202,14 @@ template <int BN>
 int launch_gemm(const void* A, int lda, const void* B, int ldb, float* D, int ldd, int M, int N, int K, float alpha,
                 const float* bias, int32_t* status, cudaStream_t stream) {
     using C = Cfg<BN>;
+    static_assert(BN / 32 * BM * 128 <= C::kBarOff, "the result panels fit in the ring");
     CUtensorMap ta, tb;
     int rc = encode_map(&ta, A, M, K, lda, BM);
     if (rc != PQ_OK) return rc;
     rc = encode_map(&tb, B, N, K, ldb, BN);
+    if (rc != PQ_OK) return rc;
+    CUtensorMap td;
+    rc = encode_map(&td, D, M, N, ldd, BM, 4);
     if (rc != PQ_OK) return rc;
     static bool attr = false;
     if (!attr) {
@@ -198,7 +217,7 @@ int launch_gemm(const void* A, int lda, const void* B, int ldb, float* D, int ld
         attr = true;
     }
     dim3 grid(M / BM, N / BN);
-    tc_gemm_kernel<BN><<<grid, 128, C::kSmem, stream>>>(ta, tb, D, ldd, K, alpha, bias, status);
+    tc_gemm_kernel<BN><<<grid, 128, C::kSmem, stream>>>(ta, tb, td, K, alpha, bias, status);
     return pq_launch_status();
 }
 

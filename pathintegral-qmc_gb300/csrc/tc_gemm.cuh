@@ -148,6 +148,19 @@ __device__ __forceinline__ void tmem_ld32_async(uint32_t taddr, uint32_t (&r)[32
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// 2-D TMA tile store from shared memory (bulk group; completion by tma_store_wait).
+__device__ __forceinline__ void tma_store_2d(const void* tmap, int x, int y, uint32_t src) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                     reinterpret_cast<uint64_t>(tmap)),
+                 "r"(x), "r"(y), "r"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void tma_store_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// Wait until the committed stores have finished reading shared memory.
+__device__ __forceinline__ void tma_store_wait_read() {
+    asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+
 // Byte offset of element (r, k) in a K-major no-swizzle tile with KC columns.
 __host__ __device__ __forceinline__ uint32_t tile_off(int r, int k, int KC) {
     return (uint32_t)((r >> 3) * (KC >> 3) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
