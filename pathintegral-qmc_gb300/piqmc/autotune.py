@@ -15,7 +15,7 @@ import os
 import numpy as np
 import torch
 
-CANDIDATES = ((1, 1), (1, 2), (1, 4), (1, 8), (2, 1), (2, 2), (4, 1), (8, 1))
+CANDIDATES = ((1, 1), (1, 2), (1, 4), (1, 8), (2, 1), (2, 2), (2, 4), (4, 1), (4, 2), (8, 1), (8, 2))
 _cache = {}
 _loaded = False
 

@@ -26,7 +26,7 @@ import math
 import numpy as np
 import torch
 
-from . import _device, _native
+from . import _device, _native, tensor
 from .reforder import jperp_schedule
 from .tensor import gemm_bf16
 
@@ -87,7 +87,7 @@ class DenseProblem:
                                                      _device.ptr(out), _device.stream_handle()), "pq_unpack_spins")
         return out
 
-    def fields(self, words, P, out=None, scratch=None):
+    def fields(self, words, P, out=None, scratch=None, check=True):
         """f = h + K s for every configuration c = r*P + k: FP32 (Mpad, Npad), rows c < R*P valid."""
         R = words.shape[0]
         Mpad = _pad(R * P, 128)
@@ -96,7 +96,7 @@ class DenseProblem:
         _native.check(_native.lib().pq_dense_unpack_bf16(_device.ptr(words), self.N, P, R, self.Npad, Mpad,
                                                            _device.ptr(scratch), _device.stream_handle()),
                       "pq_dense_unpack_bf16")
-        return gemm_bf16(scratch, self.B, bias=self.h, out=out), scratch
+        return gemm_bf16(scratch, self.B, bias=self.h, out=out, check=check), scratch
 
     def energies(self, words, P):
         """FP64 energy of every (replica, slice), exactly sa.ClassicalIsingEnergy's definition."""
@@ -122,17 +122,21 @@ class DenseProblem:
             int(bool(per_slice_order)), _device.ptr(accepts), _device.stream_handle()), "pq_dense_sweep")
 
     def anneal(self, words, sched, P, temp, seed=0, mcsteps=1, recompute_every=50, accepts=None,
-               per_slice_order=False):
-        """Anneal packed replicas in place: GEMM field recompute, then up to ``recompute_every`` steps."""
+               per_slice_order=False, check=True):
+        """Anneal packed replicas in place: GEMM field recompute, then up to ``recompute_every`` steps.
+
+        ``check`` reads the GEMMs' device status once at the end (one host synchronisation)."""
         jp = torch.from_numpy(jperp_schedule(sched, P, temp) if P > 1 else np.zeros(len(sched), np.float32)).to(
             words.device)
         beta = np.float32(1.0) / np.float32(temp)
         F = scratch = None
         for g0 in range(0, len(sched), recompute_every):
             g1 = min(len(sched), g0 + recompute_every)
-            F, scratch = self.fields(words, P, out=F, scratch=scratch)
+            F, scratch = self.fields(words, P, out=F, scratch=scratch, check=False)
             self.sweep(words, F, P, jp[g0:g1], beta, seed, mcsteps=mcsteps, sweep_base=g0 * mcsteps,
                        accepts=accepts, per_slice_order=per_slice_order)
+        if check:
+            tensor.check_status(words.device)
         return words
 
 
