@@ -311,14 +311,15 @@ int pq_tc_gemm_bf16(const void* A, int lda, const void* B, int ldb, float* D, in
  * piqmc/qmc.pyx:141-242, with both quirks corrected).  words: uint32 [R][N]
  * world-lines (P <= 32).  F: FP32 local fields f = h + K s of every
  * configuration c = r*P + k, row c at F + c*ldf (the split-BF16 tensor-core GEMM
- * of pq_tc_gemm_bf16 produces them); they are copied to shared memory and
- * updated incrementally (rank-1) on every accepted flip.  K: FP32 symmetric
+ * of pq_tc_gemm_bf16 produces them); they are copied to shared memory,
+ * updated incrementally (rank-1) on every accepted flip and written back at the
+ * end, so F holds the fields of the final configurations.  K: FP32 symmetric
  * couplings [N][N] with zero diagonal.  units: the nunits integers coprime to N
  * (spin orders are random affine maps i = a t + b mod N, one per sweep shared by
  * every slice like the reference's permutation, or one per slice when
  * per_slice_order != 0).
  * ------------------------------------------------------------------------- */
-int pq_dense_sweep(uint32_t* words, const float* F, int ldf, const float* K, const int32_t* units, int nunits,
+int pq_dense_sweep(uint32_t* words, float* F, int ldf, const float* K, const int32_t* units, int nunits,
                    const float* jperp, int N, int P, int R, int nsched, int mcsteps, float beta, uint64_t seed,
                    int64_t sweep_base, int replica_base, int per_slice_order, unsigned long long* accepts,
                    void* stream);

@@ -6,7 +6,11 @@
 //
 // Every spin couples to every other, so within a Trotter slice the updates are
 // sequential; the parallelism is across the slices of one slice class (one
-// warp per slice) and across replicas (one CTA per replica).
+// warp per slice) and across replicas (one CTA per replica).  Within a slice the
+// warp still decides 32 positions at once: a decision reads only its own spin's
+// field, so all open positions decide from the current fields, the first accepted
+// one is final, its rank-1 update is applied, and the positions after it decide
+// again; rejected positions cost one lane each instead of a warp each.
 //
 // Specification of one sweep of replica r (sweep counter `sweep`):
 //  * slice classes as in the sparse sweep; warp w handles slice k = 2w + q of
@@ -40,7 +44,7 @@ struct DenseArgs {
     int replica_base;
 };
 
-__global__ void __launch_bounds__(512, 2) dense_sweep_kernel(uint32_t* __restrict__ words, const float* __restrict__ F,
+__global__ void __launch_bounds__(512, 2) dense_sweep_kernel(uint32_t* __restrict__ words, float* __restrict__ F,
                                                            const float* __restrict__ K, const int32_t* __restrict__ units,
                                                            const float* __restrict__ jperp, DenseArgs a,
                                                            unsigned long long* __restrict__ accepts) {
@@ -75,31 +79,50 @@ __global__ void __launch_bounds__(512, 2) dense_sweep_kernel(uint32_t* __restric
                     const uint32_t bm = ord.y % (uint32_t)N;
                     float* fk = sf + (size_t)k * N;
                     const int kl = k == 0 ? P - 1 : k - 1, kr = k == P - 1 ? 0 : k + 1;
+                    // positions are taken 32 at a time, lane l holding position t0 + l: all open
+                    // positions decide at once from the current fields; the first accepted one is
+                    // final, its rank-1 update is applied, and the positions after it decide
+                    // again -- the same decisions, in the same order of updates, as one spin at a time
+                    const uint32_t off_l = ((uint32_t)lane * am) % (uint32_t)N;     // (l a) mod N
+                    const uint32_t a32 = (32u * am) % (uint32_t)N;
+                    uint32_t i0 = bm;                                                // i_{t0}
                     pq_u32x4 mine{0, 0, 0, 0};
-                    // i_t = (a t + b) mod N, advanced incrementally (a < N, b < N)
-                    uint32_t i = bm;
-                    for (int t = 0; t < N; ++t) {
-                        if ((t & 127) == 0) {
-                            mine = pq_philox(pq_u32x4{(uint32_t)k, sweep, rep, (4u << 24) | (uint32_t)((t >> 2) + lane)},
+                    for (int t0 = 0; t0 < N; t0 += 32) {
+                        if ((t0 & 127) == 0)
+                            mine = pq_philox(pq_u32x4{(uint32_t)k, sweep, rep, (4u << 24) | (uint32_t)((t0 >> 2) + lane)},
                                              a.key0, a.key1);
+                        // position t = t0 + lane uses word t & 3 of Philox block t >> 2
+                        const int src = ((t0 & 127) >> 2) + (lane >> 2);
+                        const uint32_t wx = __shfl_sync(0xffffffffu, mine.x, src);
+                        const uint32_t wy = __shfl_sync(0xffffffffu, mine.y, src);
+                        const uint32_t wz = __shfl_sync(0xffffffffu, mine.z, src);
+                        const uint32_t ww = __shfl_sync(0xffffffffu, mine.w, src);
+                        const uint32_t comp = (lane & 3) == 0 ? wx : (lane & 3) == 1 ? wy : (lane & 3) == 2 ? wz : ww;
+                        const float u = pq_u01(comp);
+                        const int nb = min(32, N - t0);
+                        uint32_t i = i0 + off_l;
+                        if (i >= (uint32_t)N) i -= (uint32_t)N;
+                        float tt = 0.0f;
+                        uint32_t sbit = 0;
+                        if (lane < nb) {
+                            const uint32_t wi = sw[i];
+                            sbit = (wi >> k) & 1u;
+                            tt = __fadd_rn(flip_sign(jp, (((wi >> k) ^ (wi >> kl)) & 1u) << 31),
+                                           flip_sign(jp, (((wi >> k) ^ (wi >> kr)) & 1u) << 31));
                         }
-                        const uint32_t comp = (t & 3) == 0 ? mine.x : (t & 3) == 1 ? mine.y : (t & 3) == 2 ? mine.z : mine.w;
-                        const uint32_t rnd = __shfl_sync(0xffffffffu, comp, (t & 127) >> 2);
-                        uint32_t inext = i + am;
-                        if (inext >= (uint32_t)N) inext -= (uint32_t)N;
-                        // pull the next spin's coupling row into L1 (one 128-byte line per lane)
-                        if (t + 1 < N && lane * 32 < N)
-                            asm volatile("prefetch.global.L1 [%0];" ::"l"(K + (size_t)inext * N + lane * 32));
-                        const uint32_t wi = sw[i];
-                        const uint32_t sbit = (wi >> k) & 1u;
-                        const float e = flip_sign(fk[i], sbit << 31);
-                        const float tt = __fadd_rn(flip_sign(jp, (((wi >> k) ^ (wi >> kl)) & 1u) << 31),
-                                                   flip_sign(jp, (((wi >> k) ^ (wi >> kr)) & 1u) << 31));
-                        const bool acc = decide(__fadd_rn(e, tt), pq_u01(rnd), m2beta, m2blog2e);
-                        if (acc) {
+                        int start = 0;
+                        while (start < nb) {
+                            bool acc = false;
+                            if (lane >= start && lane < nb)
+                                acc = decide(__fadd_rn(flip_sign(fk[i], sbit << 31), tt), u, m2beta, m2blog2e);
+                            const uint32_t hit = __ballot_sync(0xffffffffu, acc);
+                            if (!hit) break;
+                            const int p = __ffs(hit) - 1;
+                            const uint32_t ip = __shfl_sync(0xffffffffu, i, p);
+                            const uint32_t sp = __shfl_sync(0xffffffffu, sbit, p);
                             // new spin = -old: s_new = +1 when the old bit was set (old spin -1)
-                            const float c = sbit ? 2.0f : -2.0f;
-                            const float* Ki = K + (size_t)i * N;
+                            const float c = sp ? 2.0f : -2.0f;
+                            const float* Ki = K + (size_t)ip * N;
                             if (N <= 512) {
                                 // all row loads in flight at once, then the updates
                                 float kv[16];
@@ -116,11 +139,13 @@ __global__ void __launch_bounds__(512, 2) dense_sweep_kernel(uint32_t* __restric
                             } else {
                                 for (int j = lane; j < N; j += 32) fk[j] = __fmaf_rn(c, __ldg(Ki + j), fk[j]);
                             }
-                            if (lane == 0) atomicXor(sw + i, 1u << k);
+                            if (lane == 0) atomicXor(sw + ip, 1u << k);
                             ++nacc;
+                            __syncwarp();
+                            start = p + 1;
                         }
-                        i = inext;
-                        __syncwarp();
+                        i0 += a32;
+                        if (i0 >= (uint32_t)N) i0 -= (uint32_t)N;
                     }
                 }
                 __syncthreads();
@@ -128,7 +153,11 @@ __global__ void __launch_bounds__(512, 2) dense_sweep_kernel(uint32_t* __restric
         }
     }
     for (int t = threadIdx.x; t < N; t += blockDim.x) words[(size_t)r * N + t] = sw[t];
-    if (accepts && lane == 0 && nacc) atomicAdd(accepts, nacc);
+    for (int t = threadIdx.x; t < P * N; t += blockDim.x) {
+        const int k = t / N, i = t - k * N;
+        F[(size_t)(r * P + k) * a.ldf + i] = sf[t];
+    }
+    if (accepts && lane == 0 && nacc) atomicAdd(accepts, nacc);   // nacc is warp-uniform
 }
 
 // words [R][N] (bits = slices) -> BF16 +-1 rows [R*P (padded to Mpad)][2 Npad]: row c = r*P + k holds
@@ -161,7 +190,7 @@ int pq_dense_unpack_bf16(const uint32_t* words, int N, int P, int R, int Npad, i
     return pq_launch_status();
 }
 
-int pq_dense_sweep(uint32_t* words, const float* F, int ldf, const float* K, const int32_t* units, int nunits,
+int pq_dense_sweep(uint32_t* words, float* F, int ldf, const float* K, const int32_t* units, int nunits,
                    const float* jperp, int N, int P, int R, int nsched, int mcsteps, float beta, uint64_t seed,
                    int64_t sweep_base, int replica_base, int per_slice_order, unsigned long long* accepts,
                    void* stream) {

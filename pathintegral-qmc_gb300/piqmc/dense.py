@@ -109,7 +109,7 @@ class DenseProblem:
 
     def sweep(self, words, F, P, jperp, beta, seed, mcsteps=1, sweep_base=0, replica_base=0, accepts=None,
               per_slice_order=False):
-        """Dense sweeps of every replica through len(jperp) field steps starting from fields F.
+        """Dense sweeps of every replica through len(jperp) field steps starting from fields F (updated in place).
 
         The spin order of a sweep is shared by every slice (as in the reference) unless
         ``per_slice_order`` -- which anneals faster but with different dynamics.

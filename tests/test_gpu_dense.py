@@ -28,7 +28,8 @@ def test_field_recompute_error_vs_fp64(N, P, R):
     assert err <= bound, (err, bound)
 
 
-@pytest.mark.parametrize("N,P,per_slice", [(64, 8, False), (50, 7, True), (96, 16, False), (64, 32, True)])
+@pytest.mark.parametrize("N,P,per_slice", [(64, 8, False), (50, 7, True), (96, 16, False), (64, 32, True),
+                                           (600, 4, False)])
 def test_dense_sweep_bit_exact_with_oracle(N, P, per_slice):
     from piqmc import dense
     J, g = _instance(N, 100 + N)
@@ -49,11 +50,12 @@ def test_dense_sweep_bit_exact_with_oracle(N, P, per_slice):
     for r in range(R):
         w = w0[r].cpu().numpy().view(np.uint32).copy()
         f = F0[r * P:(r + 1) * P, :N].cpu().numpy().copy()
-        n, _ = oracle.dense_sweep(f, prob.K.cpu().numpy(), prob.units.cpu().numpy(), w, P, jp, 2,
-                                  np.float32(1) / np.float32(0.05), 77, sweep_base=5, replica=r,
-                                  per_slice_order=per_slice)
+        n, f_after = oracle.dense_sweep(f, prob.K.cpu().numpy(), prob.units.cpu().numpy(), w, P, jp, 2,
+                                        np.float32(1) / np.float32(0.05), 77, sweep_base=5, replica=r,
+                                        per_slice_order=per_slice)
         tot += n
         np.testing.assert_array_equal(got[r], w, err_msg="replica %d" % r)
+        np.testing.assert_array_equal(F[r * P:(r + 1) * P, :N].cpu().numpy(), f_after, err_msg="fields %d" % r)
     assert int(acc.item()) == tot
 
 
