@@ -39,7 +39,7 @@ __device__ __forceinline__ void run_task_item(const pq_batch_item& bi, const pq_
     run_item_any(it, smem + bi.smem_off, g, bad, nacc);
 }
 
-__global__ void __launch_bounds__(256, 3) batch_kernel(const pq_batch_task* __restrict__ tasks, int ntasks,
+__global__ void __launch_bounds__(256, 2) batch_kernel(const pq_batch_task* __restrict__ tasks, int ntasks,
                                                     const pq_batch_item* __restrict__ items,
                                                     const pq_batch_inst* __restrict__ insts, const int32_t* nbr_pool,
                                                     const float* cpl_pool, const float* field_pool,
