@@ -206,14 +206,15 @@ __global__ void __launch_bounds__(32) qa_sparse_reforder_kernel(
 //    the current neighbour spins into signed couplings; a neighbour at an earlier
 //    position p of the same block is recorded (its term changes sign if p flips);
 //  * the accumulator is a sequential chain (FP32, one rounding per term, carried
-//    across spins as the reference carries it): all lanes walk the positions in
-//    order computing it -- the sum of position l and the number of uniforms
-//    consumed before it are kept by lane l -- until a position depends on an
-//    earlier position of the block whose decision is still open;
-//  * then the open positions decide in parallel, each lane with its own uniform
-//    (the window of the next 32 values of the stream) and exactly
-//    ref_accept's arithmetic; their flips resolve the pending sign changes and
-//    the walk continues.
+//    across spins as the reference carries it).  A round takes the open positions
+//    up to (not including) the first one with an in-block neighbour whose decision
+//    is still open; those positions first negate the terms of neighbours that
+//    flipped earlier in the block, then all lanes walk them in order computing the
+//    chain -- the sum of position l and the number of uniforms consumed before it
+//    are kept by lane l;
+//  * the walked positions then decide in parallel, each lane with its own uniform
+//    (the window of the next 32 values of the stream) and exactly ref_accept's
+//    arithmetic, and the next round starts.
 // Flips are written back at the end of the block.  Same results, same uniforms
 // consumed and the same close calls (recorded by the deciding lane) as
 // qa_sparse_reforder_kernel.
@@ -234,10 +235,8 @@ __global__ void __launch_bounds__(32) qa_sparse_reforder_warp_kernel(
     extern __shared__ __align__(16) int8_t sh[];
     int8_t* s = sh;                                                                             // [n][P]
     uint8_t* pos_of = reinterpret_cast<uint8_t*>(sh + (((size_t)n * P + 15) & ~(size_t)15));   // [n]
-    // records of the block's 32 positions (+ one spare so position l + 1 can be read ahead)
+    // terms of the block's 32 positions (+ one spare so position l + 1 can be read ahead)
     float4* rec = reinterpret_cast<float4*>(pos_of + (((size_t)n + 15) & ~(size_t)15));        // [33][2]
-    uint32_t* rec_dep = reinterpret_cast<uint32_t*>(rec + 66);                                  // [36]
-    uint8_t* rec_p = reinterpret_cast<uint8_t*>(rec_dep + 36);                                  // [32][MAXNB]
     const int r = blockIdx.x;
     if (r >= R) return;
     const int lane = threadIdx.x;
@@ -285,23 +284,29 @@ __global__ void __launch_bounds__(32) qa_sparse_reforder_warp_kernel(
                     const int i = cur.i;
                     if (lane < nb) pos_of[i] = (uint8_t)lane;
                     __syncwarp();
+                    // this lane's position: its terms (signed couplings, or with FP32 the
+                    // exact products s2 v), which earlier positions of the block they depend on
+                    // (dep, pp) -- kept in registers and published in rec for the walk
+                    float x[8];
+                    uint8_t pp[MAXNB];
+                    uint32_t dep = 0;
+#pragma unroll
+                    for (int m = 0; m < 8; ++m) x[m] = 0.0f;
+#pragma unroll
+                    for (int m = 0; m < MAXNB; ++m) pp[m] = 0xFF;
                     if (lane < nb) {
                         const int8_t* si_p = s + (int64_t)i * P;
-                        float x[8];
-                        uint32_t dep = 0;
 #pragma unroll
                         for (int m = 0; m < MAXNB; ++m) {
                             int j = cur.j[m];
                             if ((unsigned)j >= (unsigned)n) { bad = true; j = i; }
                             float v = cur.v[m];
-                            uint8_t pp = 0xFF;
                             if (j != i) {
                                 if (s[(int64_t)j * P + k] <= 0) v = -v;
                                 const uint8_t q = pos_of[j];
-                                if (q < lane) { pp = q; dep |= 1u << q; }
+                                if (q < lane) { pp[m] = q; dep |= 1u << q; }
                             }
                             x[m] = v;
-                            rec_p[lane * MAXNB + m] = pp;
                         }
                         x[MAXNB] = si_p[tl] > 0 ? jpf : -jpf;
                         x[MAXNB + 1] = si_p[tr] > 0 ? jpf : -jpf;
@@ -311,11 +316,8 @@ __global__ void __launch_bounds__(32) qa_sparse_reforder_warp_kernel(
 #pragma unroll
                             for (int m = 0; m < MAXNB + 2; ++m) x[m] = __fmul_rn(x[MAXNB + 2], x[m]);
                         }
-#pragma unroll
-                        for (int m = MAXNB + 3; m < 8; ++m) x[m] = 0.0f;
                         rec[2 * lane] = make_float4(x[0], x[1], x[2], x[3]);
                         rec[2 * lane + 1] = make_float4(x[4], x[5], x[6], x[7]);
-                        rec_dep[lane] = dep;
                     }
                     const int32_t rwin = used + lane < cap ? __ldg(rr + used + lane) : 0;
                     __syncwarp();
@@ -327,33 +329,33 @@ __global__ void __launch_bounds__(32) qa_sparse_reforder_warp_kernel(
                     while (l < nb) {
                         const int start = l;
                         const uint32_t open = ~((1u << start) - 1u);   // positions >= start are undecided
-                        // records of position l + 1 are loaded while position l's sum is chained
-                        uint32_t dep = rec_dep[l];
+                        // the walk stops before the first later position with an undecided in-block neighbour
+                        const uint32_t blocked = __ballot_sync(0xffffffffu, lane > start && lane < nb && (dep & open));
+                        const int end = blocked ? __ffs(blocked) - 1 : nb;
+                        // the walked positions apply the flips decided so far (all their neighbours' are)
+                        if (lane >= start && lane < end && (dep & flipmask)) {
+#pragma unroll
+                            for (int m = 0; m < MAXNB; ++m)
+                                if (pp[m] != 0xFF && ((flipmask >> pp[m]) & 1u)) x[m] = -x[m];
+                            rec[2 * lane] = make_float4(x[0], x[1], x[2], x[3]);
+                            rec[2 * lane + 1] = make_float4(x[4], x[5], x[6], x[7]);
+                        }
+                        __syncwarp();
+                        // records of position l + 1 are read while position l's sum is chained
                         float4 ra = rec[2 * l], rb = rec[2 * l + 1];
-                        for (; l < nb; ++l) {
-                            if (dep & open) break;
-                            const uint32_t dep_n = rec_dep[l + 1];
+                        for (; l < end; ++l) {
                             const float4 ra_n = rec[2 * l + 2], rb_n = rec[2 * l + 3];
-                            float x[8] = {ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w};
-                            const uint32_t dep_l = dep;
-                            dep = dep_n;
+                            const float y[8] = {ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w};
                             ra = ra_n;
                             rb = rb_n;
-                            if (dep_l & flipmask) {
-#pragma unroll
-                                for (int m = 0; m < MAXNB; ++m) {
-                                    const uint32_t pp = rec_p[l * MAXNB + m];
-                                    if (pp != 0xFFu && ((flipmask >> pp) & 1u)) x[m] = -x[m];
-                                }
-                            }
                             if (FIXQ2) ediff = 0.0f;
                             if constexpr (FP64) {
-                                const float s2 = x[MAXNB + 2];
+                                const float s2 = y[MAXNB + 2];
 #pragma unroll
-                                for (int m = 0; m < MAXNB + 2; ++m) ediff = acc2<true>(ediff, s2, x[m]);
+                                for (int m = 0; m < MAXNB + 2; ++m) ediff = acc2<true>(ediff, s2, y[m]);
                             } else {
 #pragma unroll
-                                for (int m = 0; m < MAXNB + 2; ++m) ediff = __fadd_rn(ediff, x[m]);
+                                for (int m = 0; m < MAXNB + 2; ++m) ediff = __fadd_rn(ediff, y[m]);
                             }
                             if (lane == l) { my_e = ediff; my_c = c; }
                             c += ediff > 0.0f ? 0 : 1;
@@ -765,7 +767,7 @@ int launch_qa_sparse_t(int8_t* spins, const int32_t* nb_idx, const float* nb_j, 
 
 template <bool FP64, int MAXNB>
 size_t warp_kernel_smem(int n, int P) {
-    return (((size_t)n * P + 15) & ~(size_t)15) + (((size_t)n + 15) & ~(size_t)15) + 33 * 32 + 36 * 4 + 32 * MAXNB;
+    return (((size_t)n * P + 15) & ~(size_t)15) + (((size_t)n + 15) & ~(size_t)15) + 33 * 32;
 }
 
 template <bool FP64, int MAXNB>
