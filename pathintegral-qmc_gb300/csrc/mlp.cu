@@ -601,18 +601,33 @@ __global__ void uniform_move_kernel(W* __restrict__ words, const int32_t* __rest
     }
 }
 
+// Persistent grid: SMs x resident CTAs per SM.  The runtime's occupancy query
+// reports one CTA per SM for this kernel (it cannot see the TMEM budget), so the
+// residency is computed from the kernel's own resources: shared memory, registers
+// and TMEM (4 x 128 columns per SM) -- four CTAs per SM.
 template <typename W, int MAXD>
 int move_grid(int64_t ntiles) {
     static int occ = 0, nsm = 0;
     if (!occ) {
         auto kernel = learned_move_kernel<W, MAXD>;
-        int dev = 0;
+        int dev = 0, smem_sm = 0, regs_sm = 0, reserved = 0;
         PQ_CUDA_TRY(cudaGetDevice(&dev));
         PQ_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        PQ_CUDA_TRY(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+        PQ_CUDA_TRY(cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev));
+        PQ_CUDA_TRY(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev));
         PQ_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemMove));
-        PQ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, 128, kSmemMove));
-        // four CTAs of 128 TMEM columns fill an SM's 512
-        occ = occ < 1 ? 1 : (occ > 4 ? 4 : occ);
+        PQ_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                         (int)cudaSharedmemCarveoutMaxShared));
+        cudaFuncAttributes fa;
+        PQ_CUDA_TRY(cudaFuncGetAttributes(&fa, kernel));
+        const int by_smem = smem_sm / (kSmemMove + (int)fa.sharedSizeBytes + reserved);
+        const int warp_regs = (fa.numRegs * 32 + 255) / 256 * 256;    // allocated per warp in units of 256
+        const int by_regs = regs_sm / (warp_regs * 4);
+        const int by_tmem = 512 / (2 * kLd);
+        occ = by_smem < by_regs ? by_smem : by_regs;
+        occ = occ < by_tmem ? occ : by_tmem;
+        occ = occ < 1 ? 1 : occ;
     }
     const int64_t g = (int64_t)nsm * occ;
     return (int)(ntiles < g ? ntiles : g);
