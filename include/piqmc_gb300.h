@@ -317,12 +317,14 @@ int pq_tc_gemm_bf16(const void* A, int lda, const void* B, int ldb, float* D, in
  * couplings [N][N] with zero diagonal.  units: the nunits integers coprime to N
  * (spin orders are random affine maps i = a t + b mod N, one per sweep shared by
  * every slice like the reference's permutation, or one per slice when
- * per_slice_order != 0).
+ * per_slice_order != 0).  For even P the slices of a replica advance as a
+ * wavefront (each waits, bounded, only for its Trotter neighbours); a wait that
+ * gives up records PQ_ERR_TIMEOUT in status (nullable).
  * ------------------------------------------------------------------------- */
 int pq_dense_sweep(uint32_t* words, float* F, int ldf, const float* K, const int32_t* units, int nunits,
                    const float* jperp, int N, int P, int R, int nsched, int mcsteps, float beta, uint64_t seed,
                    int64_t sweep_base, int replica_base, int per_slice_order, unsigned long long* accepts,
-                   void* stream);
+                   int32_t* status, void* stream);
 /* words [R][N] -> the GEMM operand: BF16 +-1 rows c = r*P + k (Mpad rows, zero
  * padding), each row = [s over j < Npad, the same again] (2*Npad columns, so one
  * GEMM against [K_hi | K_lo] sums both halves of the split couplings). */

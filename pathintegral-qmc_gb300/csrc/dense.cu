@@ -44,11 +44,115 @@ struct DenseArgs {
     int replica_base;
 };
 
+// One sweep of slice k of the replica whose fields sf and world-lines sw are in
+// shared memory (the specification above), run by one warp; returns the accepted
+// flips.
+__device__ __forceinline__ unsigned long long sweep_slice(int k, uint32_t sweep, float jp, float m2beta,
+                                                          float m2blog2e, float* __restrict__ sf,
+                                                          uint32_t* __restrict__ sw, const float* __restrict__ K,
+                                                          const int32_t* __restrict__ units, const DenseArgs& a,
+                                                          uint32_t rep, int lane) {
+    const int N = a.N, P = a.P;
+    unsigned long long nacc = 0;
+    const uint32_t kk = a.per_slice_order ? (uint32_t)k : 0u;
+    const pq_u32x4 ord = pq_philox(pq_u32x4{0xFFFFFFFEu, sweep, rep, (3u << 24) | kk}, a.key0, a.key1);
+    const uint32_t am = (uint32_t)__ldg(units + ord.x % (uint32_t)a.nunits);
+    const uint32_t bm = ord.y % (uint32_t)N;
+    float* fk = sf + (size_t)k * N;
+    const int kl = k == 0 ? P - 1 : k - 1, kr = k == P - 1 ? 0 : k + 1;
+    // positions are taken 32 at a time, lane l holding position t0 + l: all open
+    // positions decide at once from the current fields; the first accepted one is
+    // final, its rank-1 update is applied, and the positions after it decide
+    // again -- the same decisions, in the same order of updates, as one spin at a time
+    const uint32_t off_l = ((uint32_t)lane * am) % (uint32_t)N;     // (l a) mod N
+    const uint32_t a32 = (32u * am) % (uint32_t)N;
+    uint32_t i0 = bm;                                                // i_{t0}
+    pq_u32x4 mine{0, 0, 0, 0};
+    for (int t0 = 0; t0 < N; t0 += 32) {
+        if ((t0 & 127) == 0)
+            mine = pq_philox(pq_u32x4{(uint32_t)k, sweep, rep, (4u << 24) | (uint32_t)((t0 >> 2) + lane)},
+                             a.key0, a.key1);
+        // position t = t0 + lane uses word t & 3 of Philox block t >> 2
+        const int src = ((t0 & 127) >> 2) + (lane >> 2);
+        const uint32_t wx = __shfl_sync(0xffffffffu, mine.x, src);
+        const uint32_t wy = __shfl_sync(0xffffffffu, mine.y, src);
+        const uint32_t wz = __shfl_sync(0xffffffffu, mine.z, src);
+        const uint32_t ww = __shfl_sync(0xffffffffu, mine.w, src);
+        const uint32_t comp = (lane & 3) == 0 ? wx : (lane & 3) == 1 ? wy : (lane & 3) == 2 ? wz : ww;
+        const float u = pq_u01(comp);
+        const int nb = min(32, N - t0);
+        uint32_t i = i0 + off_l;
+        if (i >= (uint32_t)N) i -= (uint32_t)N;
+        float tt = 0.0f;
+        uint32_t sbit = 0;
+        if (lane < nb) {
+            const uint32_t wi = sw[i];
+            sbit = (wi >> k) & 1u;
+            tt = __fadd_rn(flip_sign(jp, (((wi >> k) ^ (wi >> kl)) & 1u) << 31),
+                           flip_sign(jp, (((wi >> k) ^ (wi >> kr)) & 1u) << 31));
+        }
+        int start = 0;
+        while (start < nb) {
+            bool acc = false;
+            if (lane >= start && lane < nb)
+                acc = decide(__fadd_rn(flip_sign(fk[i], sbit << 31), tt), u, m2beta, m2blog2e);
+            const uint32_t hit = __ballot_sync(0xffffffffu, acc);
+            if (!hit) break;
+            const int p = __ffs(hit) - 1;
+            const uint32_t ip = __shfl_sync(0xffffffffu, i, p);
+            const uint32_t sp = __shfl_sync(0xffffffffu, sbit, p);
+            // new spin = -old: s_new = +1 when the old bit was set (old spin -1)
+            const float c = sp ? 2.0f : -2.0f;
+            const float* Ki = K + (size_t)ip * N;
+            if (N <= 512) {
+                // all row loads in flight at once, then the updates
+                float kv[16];
+#pragma unroll
+                for (int m = 0; m < 16; ++m) {
+                    const int j = lane + 32 * m;
+                    kv[m] = j < N ? __ldg(Ki + j) : 0.0f;
+                }
+#pragma unroll
+                for (int m = 0; m < 16; ++m) {
+                    const int j = lane + 32 * m;
+                    if (j < N) fk[j] = __fmaf_rn(c, kv[m], fk[j]);
+                }
+            } else {
+                for (int j = lane; j < N; j += 32) fk[j] = __fmaf_rn(c, __ldg(Ki + j), fk[j]);
+            }
+            if (lane == 0) atomicXor(sw + ip, 1u << k);
+            ++nacc;
+            __syncwarp();
+            start = p + 1;
+        }
+        i0 += a32;
+        if (i0 >= (uint32_t)N) i0 -= (uint32_t)N;
+    }
+    return nacc;
+}
+
+constexpr long long kWaveWait = 1ll << 24;   // polls of a neighbour's progress before giving up
+
+// Wait until *flag >= need for every lane (each lane reads the flag itself, then
+// fences, so the producer's shared-memory writes before its release are visible).
+__device__ __forceinline__ bool wait_progress(const volatile int* flag, int need) {
+    for (long long it = 0; it < kWaveWait; ++it) {
+        if (__all_sync(0xffffffffu, *flag >= need)) {
+            __threadfence_block();
+            return true;
+        }
+        __nanosleep(64);
+    }
+    return false;
+}
+
 __global__ void __launch_bounds__(512, 2) dense_sweep_kernel(uint32_t* __restrict__ words, float* __restrict__ F,
                                                            const float* __restrict__ K, const int32_t* __restrict__ units,
                                                            const float* __restrict__ jperp, DenseArgs a,
-                                                           unsigned long long* __restrict__ accepts) {
+                                                           unsigned long long* __restrict__ accepts,
+                                                           int32_t* __restrict__ status) {
     extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int prog[2][32];   // slice phases completed: [class][warp]
     const int N = a.N, P = a.P;
     float* sf = reinterpret_cast<float*>(smem);                       // [P][N] fields
     uint32_t* sw = reinterpret_cast<uint32_t*>(sf + (size_t)P * N);    // [N] world-lines
@@ -60,98 +164,59 @@ __global__ void __launch_bounds__(512, 2) dense_sweep_kernel(uint32_t* __restric
         sf[t] = F[(size_t)(r * P + k) * a.ldf + i];
     }
     for (int t = threadIdx.x; t < N; t += blockDim.x) sw[t] = words[(size_t)r * N + t];
+    if (threadIdx.x < 64) prog[threadIdx.x >> 5][threadIdx.x & 31] = 0;
     __syncthreads();
-    const int nclass_q = P == 1 ? 1 : ((P & 1) ? 3 : 2);
     unsigned long long nacc = 0;
-    for (int g = 0; g < a.nsched; ++g) {
-        const float jp = P == 1 ? 0.0f : jperp[g];
-        const float m2beta = __fmul_rn(-2.0f, a.beta);
-        const float m2blog2e = __fmul_rn(m2beta, 1.44269502162933349609375f);
-        for (int step = 0; step < a.mcsteps; ++step) {
-            const uint32_t sweep = (uint32_t)(a.sweep_base + (int64_t)g * a.mcsteps + step);
-            for (int q = 0; q < nclass_q; ++q) {
-                const int nq = slice_count(P, q);
-                if (warp < nq) {
-                    const int k = slice_of(P, q, warp);
-                    const uint32_t kk = a.per_slice_order ? (uint32_t)k : 0u;
-                    const pq_u32x4 ord = pq_philox(pq_u32x4{0xFFFFFFFEu, sweep, rep, (3u << 24) | kk}, a.key0, a.key1);
-                    const uint32_t am = (uint32_t)__ldg(units + ord.x % (uint32_t)a.nunits);
-                    const uint32_t bm = ord.y % (uint32_t)N;
-                    float* fk = sf + (size_t)k * N;
-                    const int kl = k == 0 ? P - 1 : k - 1, kr = k == P - 1 ? 0 : k + 1;
-                    // positions are taken 32 at a time, lane l holding position t0 + l: all open
-                    // positions decide at once from the current fields; the first accepted one is
-                    // final, its rank-1 update is applied, and the positions after it decide
-                    // again -- the same decisions, in the same order of updates, as one spin at a time
-                    const uint32_t off_l = ((uint32_t)lane * am) % (uint32_t)N;     // (l a) mod N
-                    const uint32_t a32 = (32u * am) % (uint32_t)N;
-                    uint32_t i0 = bm;                                                // i_{t0}
-                    pq_u32x4 mine{0, 0, 0, 0};
-                    for (int t0 = 0; t0 < N; t0 += 32) {
-                        if ((t0 & 127) == 0)
-                            mine = pq_philox(pq_u32x4{(uint32_t)k, sweep, rep, (4u << 24) | (uint32_t)((t0 >> 2) + lane)},
-                                             a.key0, a.key1);
-                        // position t = t0 + lane uses word t & 3 of Philox block t >> 2
-                        const int src = ((t0 & 127) >> 2) + (lane >> 2);
-                        const uint32_t wx = __shfl_sync(0xffffffffu, mine.x, src);
-                        const uint32_t wy = __shfl_sync(0xffffffffu, mine.y, src);
-                        const uint32_t wz = __shfl_sync(0xffffffffu, mine.z, src);
-                        const uint32_t ww = __shfl_sync(0xffffffffu, mine.w, src);
-                        const uint32_t comp = (lane & 3) == 0 ? wx : (lane & 3) == 1 ? wy : (lane & 3) == 2 ? wz : ww;
-                        const float u = pq_u01(comp);
-                        const int nb = min(32, N - t0);
-                        uint32_t i = i0 + off_l;
-                        if (i >= (uint32_t)N) i -= (uint32_t)N;
-                        float tt = 0.0f;
-                        uint32_t sbit = 0;
-                        if (lane < nb) {
-                            const uint32_t wi = sw[i];
-                            sbit = (wi >> k) & 1u;
-                            tt = __fadd_rn(flip_sign(jp, (((wi >> k) ^ (wi >> kl)) & 1u) << 31),
-                                           flip_sign(jp, (((wi >> k) ^ (wi >> kr)) & 1u) << 31));
-                        }
-                        int start = 0;
-                        while (start < nb) {
-                            bool acc = false;
-                            if (lane >= start && lane < nb)
-                                acc = decide(__fadd_rn(flip_sign(fk[i], sbit << 31), tt), u, m2beta, m2blog2e);
-                            const uint32_t hit = __ballot_sync(0xffffffffu, acc);
-                            if (!hit) break;
-                            const int p = __ffs(hit) - 1;
-                            const uint32_t ip = __shfl_sync(0xffffffffu, i, p);
-                            const uint32_t sp = __shfl_sync(0xffffffffu, sbit, p);
-                            // new spin = -old: s_new = +1 when the old bit was set (old spin -1)
-                            const float c = sp ? 2.0f : -2.0f;
-                            const float* Ki = K + (size_t)ip * N;
-                            if (N <= 512) {
-                                // all row loads in flight at once, then the updates
-                                float kv[16];
-#pragma unroll
-                                for (int m = 0; m < 16; ++m) {
-                                    const int j = lane + 32 * m;
-                                    kv[m] = j < N ? __ldg(Ki + j) : 0.0f;
-                                }
-#pragma unroll
-                                for (int m = 0; m < 16; ++m) {
-                                    const int j = lane + 32 * m;
-                                    if (j < N) fk[j] = __fmaf_rn(c, kv[m], fk[j]);
-                                }
-                            } else {
-                                for (int j = lane; j < N; j += 32) fk[j] = __fmaf_rn(c, __ldg(Ki + j), fk[j]);
-                            }
-                            if (lane == 0) atomicXor(sw + ip, 1u << k);
-                            ++nacc;
-                            __syncwarp();
-                            start = p + 1;
-                        }
-                        i0 += a32;
-                        if (i0 >= (uint32_t)N) i0 -= (uint32_t)N;
-                    }
+    const float m2beta = __fmul_rn(-2.0f, a.beta);
+    const float m2blog2e = __fmul_rn(m2beta, 1.44269502162933349609375f);
+    if (P >= 2 && (P & 1) == 0) {
+        // Even P: warp w owns slices 2w (even class) and 2w + 1 (odd class) and runs them in
+        // turn; a slice only waits for its two Trotter neighbours' previous phases (slice 2w
+        // for warp w - 1's odd slice, slice 2w + 1 for warp w + 1's even slice), so the warps
+        // run as a wavefront instead of meeting at a CTA barrier after every slice class.
+        // The sweeps, and so the results, are the slice-class-by-slice-class ones.
+        const int W = P / 2, w = warp;
+        const int wl = (w + W - 1) % W, wr = (w + 1) % W;
+        volatile int* vprog = &prog[0][0];
+        bool ok = true;
+        int n = 0;
+        for (int g = 0; g < a.nsched && ok; ++g) {
+            const float jp = jperp[g];
+            for (int step = 0; step < a.mcsteps && ok; ++step, ++n) {
+                const uint32_t sweep = (uint32_t)(a.sweep_base + (int64_t)g * a.mcsteps + step);
+                if (!(ok = wait_progress(vprog + 32 + wl, n))) break;
+                nacc += sweep_slice(2 * w, sweep, jp, m2beta, m2blog2e, sf, sw, K, units, a, rep, lane);
+                __syncwarp();
+                __threadfence_block();
+                if (lane == 0) vprog[w] = n + 1;
+                if (!(ok = wait_progress(vprog + wr, n + 1))) break;
+                nacc += sweep_slice(2 * w + 1, sweep, jp, m2beta, m2blog2e, sf, sw, K, units, a, rep, lane);
+                __syncwarp();
+                __threadfence_block();
+                if (lane == 0) vprog[32 + w] = n + 1;
+            }
+        }
+        if (!ok) {
+            pq_set_status(status, PQ_ERR_TIMEOUT);
+            // release the neighbours that wait on this warp
+            if (lane == 0) { vprog[w] = 1 << 30; vprog[32 + w] = 1 << 30; }
+        }
+    } else {
+        const int nclass_q = P == 1 ? 1 : 3;
+        for (int g = 0; g < a.nsched; ++g) {
+            const float jp = P == 1 ? 0.0f : jperp[g];
+            for (int step = 0; step < a.mcsteps; ++step) {
+                const uint32_t sweep = (uint32_t)(a.sweep_base + (int64_t)g * a.mcsteps + step);
+                for (int q = 0; q < nclass_q; ++q) {
+                    if (warp < slice_count(P, q))
+                        nacc += sweep_slice(slice_of(P, q, warp), sweep, jp, m2beta, m2blog2e, sf, sw, K, units, a,
+                                            rep, lane);
+                    __syncthreads();
                 }
-                __syncthreads();
             }
         }
     }
+    __syncthreads();
     for (int t = threadIdx.x; t < N; t += blockDim.x) words[(size_t)r * N + t] = sw[t];
     for (int t = threadIdx.x; t < P * N; t += blockDim.x) {
         const int k = t / N, i = t - k * N;
@@ -193,7 +258,7 @@ int pq_dense_unpack_bf16(const uint32_t* words, int N, int P, int R, int Npad, i
 int pq_dense_sweep(uint32_t* words, float* F, int ldf, const float* K, const int32_t* units, int nunits,
                    const float* jperp, int N, int P, int R, int nsched, int mcsteps, float beta, uint64_t seed,
                    int64_t sweep_base, int replica_base, int per_slice_order, unsigned long long* accepts,
-                   void* stream) {
+                   int32_t* status, void* stream) {
     if (!words || !F || !K || !units || !jperp || N <= 0 || P < 1 || P > 32 || R < 0 || nsched < 0 || mcsteps < 0 ||
         nunits <= 0 || ldf < N)
         return PQ_ERR_INVALID_ARG;
@@ -210,7 +275,7 @@ int pq_dense_sweep(uint32_t* words, float* F, int ldf, const float* K, const int
     a.key0 = (uint32_t)seed; a.key1 = (uint32_t)(seed >> 32); a.sweep_base = sweep_base; a.replica_base = replica_base;
     const int maxq = P == 1 ? 1 : (P + 1) / 2;
     const int threads = 32 * maxq;
-    dense_sweep_kernel<<<R, threads, smem, (cudaStream_t)stream>>>(words, F, K, units, jperp, a, accepts);
+    dense_sweep_kernel<<<R, threads, smem, (cudaStream_t)stream>>>(words, F, K, units, jperp, a, accepts, status);
     return pq_launch_status();
 }
 

@@ -98,7 +98,7 @@ SIGNATURES = {
     "pq_batch_occupancy": (_I32, [_I32, _I32, _V, _V]),
     "pq_tc_gemm_bf16": (_I32, [_V, _I32, _V, _I32, _V, _I32, _I32, _I32, _I32, _F32, _V, _V, _V]),
     "pq_dense_sweep": (_I32, [_V, _V, _I32, _V, _V, _I32, _V, _I32, _I32, _I32, _I32, _I32, _F32, _U64, _I64, _I32,
-                              _I32, _V, _V]),
+                              _I32, _V, _V, _V]),
     "pq_dense_unpack_bf16": (_I32, [_V, _I32, _I32, _I32, _I32, _I32, _V, _V]),
     "pq_mlp_features": (_I32, [_V, _I32, _I32, _I32, _I32, _I32, _V, _V, _V, _I32, _I32, _I32, _F32, _F32, _V, _V,
                                _I64, _V]),

@@ -67,6 +67,7 @@ class DenseProblem:
         self.csr_ptr = torch.from_numpy(np.concatenate([[0], np.cumsum(np.bincount(rows, minlength=N))]).astype(np.int64)).to(dev)
         self.csr_col = torch.from_numpy(cols.astype(np.int32)).to(dev)
         self.csr_val = torch.from_numpy(J[rows, cols].astype(np.float64)).to(dev)
+        self._status = _device.Status()   # timed-out waits of the sweep
 
     # --------------------------------------------------------------------------------------
     def pack(self, spins):
@@ -108,7 +109,7 @@ class DenseProblem:
         return out
 
     def sweep(self, words, F, P, jperp, beta, seed, mcsteps=1, sweep_base=0, replica_base=0, accepts=None,
-              per_slice_order=False):
+              per_slice_order=False, status=None):
         """Dense sweeps of every replica through len(jperp) field steps starting from fields F (updated in place).
 
         The spin order of a sweep is shared by every slice (as in the reference) unless
@@ -119,7 +120,8 @@ class DenseProblem:
             _device.ptr(words), _device.ptr(F), F.stride(0), _device.ptr(self.K), _device.ptr(self.units),
             self.units.numel(), _device.ptr(jperp), self.N, int(P), R, int(jperp.numel()), int(mcsteps),
             float(np.float32(beta)), int(seed) & 0xFFFFFFFFFFFFFFFF, int(sweep_base), int(replica_base),
-            int(bool(per_slice_order)), _device.ptr(accepts), _device.stream_handle()), "pq_dense_sweep")
+            int(bool(per_slice_order)), _device.ptr(accepts), (status or self._status).ptr, _device.stream_handle()),
+            "pq_dense_sweep")
 
     def anneal(self, words, sched, P, temp, seed=0, mcsteps=1, recompute_every=50, accepts=None,
                per_slice_order=False, check=True):
@@ -137,7 +139,15 @@ class DenseProblem:
                        accepts=accepts, per_slice_order=per_slice_order)
         if check:
             tensor.check_status(words.device)
+            self.check_status()
         return words
+
+    def check_status(self):
+        """Raise if a sweep gave up waiting for a neighbouring slice (and clear the flag)."""
+        try:
+            self._status.raise_if_set("pq_dense_sweep")
+        finally:
+            self._status.reset()
 
 
 def field_error(problem, words, P):

@@ -29,7 +29,7 @@ def test_field_recompute_error_vs_fp64(N, P, R):
 
 
 @pytest.mark.parametrize("N,P,per_slice", [(64, 8, False), (50, 7, True), (96, 16, False), (64, 32, True),
-                                           (600, 4, False)])
+                                           (600, 4, False), (40, 2, False), (33, 1, False)])
 def test_dense_sweep_bit_exact_with_oracle(N, P, per_slice):
     from piqmc import dense
     J, g = _instance(N, 100 + N)
@@ -45,6 +45,7 @@ def test_dense_sweep_bit_exact_with_oracle(N, P, per_slice):
     acc = torch.zeros(1, dtype=torch.int64, device="cuda")
     prob.sweep(words, F, P, torch.from_numpy(jp).cuda(), np.float32(1) / np.float32(0.05), 77, mcsteps=2,
                sweep_base=5, accepts=acc, per_slice_order=per_slice)
+    prob.check_status()
     got = words.cpu().numpy().view(np.uint32)
     tot = 0
     for r in range(R):
