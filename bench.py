@@ -381,6 +381,14 @@ def gpu_arm(args):
             issue = pj.get("issue")
         except (OSError, ValueError):
             traffic = None
+    clocks = clk.summary()
+    if issue and issue.get("instructions_per_update"):
+        # the instruction-issue roof: 4 warp instructions per cycle per SM at the sampled SM clock
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
+        if mhz:
+            roof = sms * 4 * 32 * mhz * 1e6 / issue["instructions_per_update"]
+            issue = dict(issue, issue_roof_updates_per_s=roof, issue_frac=(value / world) / roof)
     line = {
         "metric": METRIC, "value": value, "unit": "updates/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -400,7 +408,7 @@ def gpu_arm(args):
                              "(qa_fast_kernel, one launch per step, CUDA events); peak = in-run FP32 FMA probe "
                              "(no FP32 figure in the measured-peaks file)" % FLOP_PER_UPDATE,
                      "binding_unit": issue},
-        "clocks": clk.summary(),
+        "clocks": clocks,
         "residual": {"best_slice_energy_per_spin_median": float(np.median(best)),
                      "best_slice_energy_per_spin_min": float(best.min())},
         "wall_s_timed": wall,
