@@ -463,6 +463,8 @@ def batched_workload(args, torch):
             "value": updates / float(np.median(times)), "unit": "updates/s", "ms_per_anneal": 1e3 * float(np.median(times)),
             "updates_per_anneal": updates, "tasks": int(len(B.tasks)), "grid": int(B.grid),
             "tiles": sorted(set(map(tuple, B.tiles))), "tune_s": tune_s,
+            "ms_per_field_step": 1e3 * float(np.median(times)) / len(sched),
+            "tuner_predicted_ms_per_field_step": 1e3 * getattr(B, "predicted_step_s", float("nan")),
             "best_energy_sum": float(sum(best))}
 
 

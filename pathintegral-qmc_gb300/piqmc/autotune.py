@@ -1,11 +1,21 @@
 """Autotuner of the batched kernel's tiles.
 
-For each instance shape (padded slot count rounded up to a power of two, P,
-couplings per spin, replicas) it times every candidate tile -- ``gwarps`` warps
-per work item and ``rpc`` replicas per item -- on a probe batch made of copies
-of the instance large enough to fill the GPU, for a few field steps, and keeps
-the fastest.  Results are cached per GPU name in memory and, when
-``PIQMC_TUNE_CACHE`` names a file, on disk (JSON).
+Two levels.  Per instance shape (padded slot count rounded up to a power of
+two, P, couplings per spin, replicas) ``measure`` times every candidate tile --
+``gwarps`` warps per work item and ``rpc`` replicas per item -- on a probe batch
+made of enough copies of the instance that the tile's tasks fill two CTAs per
+SM, for a few field steps: its rate is the GPU's throughput on that shape with
+every warp slot busy.  Per batch, ``plan`` then picks one tile per instance to
+minimise the predicted time of one field step,
+
+    max( sum_i warp-seconds_i / warp slots ,  longest item ),
+
+where an item of instance i with tile (gw, rpc) takes ``n_i P_i rpc / (gw w)``
+seconds per field step and ``w`` is the measured per-warp-slot rate of that
+tile.  The most efficient tile of a small instance is often one warp on eight
+replicas; the largest instances of a batch need more warps per item, or their
+items outlast the rest of the batch.  Rate tables are cached per GPU name in
+memory and, when ``PIQMC_TUNE_CACHE`` names a file, on disk (JSON).
 
 Use: ``Batch(nbs_list, replicas, slices, tuner=autotune.tune)``.
 """
@@ -16,6 +26,7 @@ import numpy as np
 import torch
 
 CANDIDATES = ((1, 1), (1, 2), (1, 4), (1, 8), (2, 1), (2, 2), (2, 4), (4, 1), (4, 2), (8, 1), (8, 2))
+CTAS_PER_SM = 2
 _cache = {}
 _loaded = False
 
@@ -34,7 +45,8 @@ def _load():
         try:
             with open(path) as f:
                 for k, v in json.load(f).items():
-                    _cache[k] = (tuple(v[0]), float(v[1]))
+                    if isinstance(v, dict):
+                        _cache[k] = {tuple(int(x) for x in t.split(",")): float(r) for t, r in v.items()}
         except (OSError, ValueError):
             pass
 
@@ -44,7 +56,8 @@ def _save():
     if path:
         try:
             with open(path, "w") as f:
-                json.dump({k: [list(v[0]), v[1]] for k, v in _cache.items()}, f, indent=1, sort_keys=True)
+                json.dump({k: {"%d,%d" % t: r for t, r in v.items()} for k, v in _cache.items()}, f, indent=1,
+                          sort_keys=True)
         except OSError:
             pass
 
@@ -56,22 +69,28 @@ def shape_key(problem, P, R):
     return "%s|%d|%d|%d|%d" % (torch.cuda.get_device_name(), b, P, problem.maxdeg, min(R, 8))
 
 
+def warp_slots(sms):
+    from .batch import WARPS
+    return CTAS_PER_SM * WARPS * sms
+
+
 def measure(problem, P, R, steps=8, candidates=CANDIDATES, repeats=2):
-    """Time each candidate tile on a probe batch; returns ((gwarps, rpc), updates/s) of the best.
+    """Time each candidate tile on a probe batch that fills the GPU; returns {(gwarps, rpc): updates/s}.
 
     Each candidate is timed ``repeats`` times over ``steps`` field steps and keeps its best time."""
     from . import _native
-    from .batch import SMEM_TASK_BUDGET, Batch
+    from .batch import SMEM_TASK_BUDGET, WARPS, Batch
     lib = _native.lib()
     sms = torch.cuda.get_device_properties(0).multi_processor_count
-    copies = max(1, (sms * 8) // R)
     g = np.random.default_rng(0)
     spins = np.where(g.random((R, problem.n, P)) < 0.5, -1, 1).astype(np.int8)
     sched = np.linspace(3.0, 1e-8, steps + 1)
-    best = None
+    rates = {}
     for gw, rpc in candidates:
         if rpc > R or lib.pq_batch_smem_bytes(rpc, problem.nslots, P) > SMEM_TASK_BUDGET:
             continue
+        items = -(-R // rpc)
+        copies = max(1, -(-CTAS_PER_SM * sms * (WARPS // gw) // items))
         B = Batch([problem] * copies, [R] * copies, [P] * copies, tiles=[(gw, rpc)] * copies)
         B.set_spins([spins] * copies)
         B.anneal(sched[:1], 0.05, seed=1)
@@ -85,29 +104,65 @@ def measure(problem, P, R, steps=8, candidates=CANDIDATES, repeats=2):
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1)
             best_ms = ms if best_ms is None else min(best_ms, ms)
-        rate = copies * R * problem.n * P * steps / (best_ms * 1e-3)
-        if best is None or rate > best[1]:
-            best = ((gw, rpc), rate)
-    return best
+        rates[(gw, rpc)] = copies * R * problem.n * P * steps / (best_ms * 1e-3)
+    return rates
+
+
+def plan(shapes, tables, slots, candidates=CANDIDATES):
+    """Tiles minimising the predicted field-step time of a batch.
+
+    ``shapes``: (slots n_i, P_i, R_i) per instance; ``tables``: {(gwarps, rpc): updates/s at fill}
+    per instance; ``slots``: warp slots of the GPU.  Returns (tiles, predicted seconds per field
+    step)."""
+    n_inst, C = len(shapes), len(candidates)
+    if n_inst == 0:
+        return [], 0.0
+    dur = np.full((n_inst, C), np.inf)
+    cost = np.full((n_inst, C), np.inf)
+    for i, ((n, P, R), tab) in enumerate(zip(shapes, tables)):
+        for c, (gw, rpc) in enumerate(candidates):
+            rate = tab.get((gw, rpc))
+            if not rate or rpc > R:
+                continue
+            w = rate / slots                        # updates/s of one busy warp slot
+            dur[i, c] = n * P * rpc / (gw * w)
+            cost[i, c] = n * P * R / w              # warp-seconds per field step
+    if np.isinf(dur).all(axis=1).any():
+        raise ValueError("an instance has no measured tile")
+    rows = np.arange(n_inst)
+    best = None
+    for T in np.unique(dur[np.isfinite(dur)]):
+        m = np.where(dur <= T, cost, np.inf)
+        ch = m.argmin(axis=1)
+        if np.isinf(m[rows, ch]).any():
+            continue
+        pred = max(m[rows, ch].sum() / slots, dur[rows, ch].max())
+        if best is None or pred < best[1]:
+            best = (ch, pred)
+    ch, pred = best
+    return [candidates[c] for c in ch], float(pred)
 
 
 def tune(batch):
     """Tiles for every instance of ``batch`` (a Batch under construction)."""
     _load()
-    tiles = []
+    tables = []
     changed = False
     for pb, P, R in zip(batch.problems, batch.P, batch.R):
         key = shape_key(pb, P, R)
         if key not in _cache:
             _cache[key] = measure(pb, P, R)
             changed = True
-        tiles.append(_cache[key][0])
+        tables.append(_cache[key])
     if changed:
         _save()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    shapes = [(pb.nslots, P, R) for pb, P, R in zip(batch.problems, batch.P, batch.R)]
+    tiles, batch.predicted_step_s = plan(shapes, tables, warp_slots(sms))
     return tiles
 
 
 def table():
-    """The cached measurements: {shape key: ((gwarps, rpc), updates/s)}."""
+    """The cached measurements: {shape key: {(gwarps, rpc): updates/s at fill}}."""
     _load()
     return dict(_cache)

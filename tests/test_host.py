@@ -189,3 +189,28 @@ def test_instance_file_and_neighbor_cache_round_trip(tmp_path):
         bad = tmp_path / "bad.txt"
         bad.write_text("0 1 0.5\n")
         tools.LoadIsingInstance(str(bad))
+
+
+def test_autotune_plan_balances_the_batch():
+    """The batch planner keeps the efficient tile where it can and splits the items that would outlast the rest."""
+    from piqmc import autotune
+    slots = 2432
+    small = {(1, 8): 3.0e11, (1, 1): 1.0e11, (8, 1): 0.5e11}
+    big = {(1, 8): 3.0e11, (2, 1): 2.5e11, (8, 1): 2.0e11}
+    # many small instances and one large one: the large one's (1, 8) item alone would take
+    # 2048*64*8 / 1.23e8 = 8.5 ms per step against ~1 ms for the whole batch's load
+    shapes = [(64, 16, 8)] * 200 + [(2048, 64, 8)]
+    tiles, pred = autotune.plan(shapes, [small] * 200 + [big], slots)
+    assert tiles[:200] == [(1, 8)] * 200
+    assert tiles[200] == (8, 1)
+    w8 = big[(8, 1)] / slots
+    total = (200 * 64 * 16 * 8 / (small[(1, 8)] / slots) + 2048 * 64 * 8 / w8) / slots
+    assert pred == pytest.approx(max(total, 2048 * 64 / (8 * w8)))
+    # a GPU full of equal small instances keeps the most efficient tile
+    tiles, _ = autotune.plan([(64, 16, 8)] * 5000, [small] * 5000, slots)
+    assert set(tiles) == {(1, 8)}
+    # tiles with more replicas than the instance has are never chosen
+    tiles, _ = autotune.plan([(64, 16, 1)], [small], slots)
+    assert tiles == [(8, 1)] or tiles == [(1, 1)]
+    with pytest.raises(ValueError):
+        autotune.plan([(64, 16, 8)], [{}], slots)
