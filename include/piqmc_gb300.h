@@ -259,7 +259,9 @@ typedef struct pq_batch_item {
 } pq_batch_item;
 
 typedef struct pq_batch_task {
-    int item0, nitems, gwarps, pad_;
+    int item0, nitems, gwarps;
+    int lanes_per_site; /* 2: items with P = 64 and 4 couplings per spin give each site a lane
+                           pair (one 32-bit half of the world-line each); otherwise 1 */
 } pq_batch_task;
 
 typedef struct pq_batch_run {

@@ -3,7 +3,8 @@
 //
 // Work is cut into items (a few replicas of one instance) and items into tasks
 // (up to 8 items that each take `gwarps` warps of a CTA, with a named barrier
-// per item).  Persistent CTAs take tasks from a queue head in global memory
+// per item; `lanes_per_site` = 2 gives the task's 64-slice items a lane pair per
+// site).  Persistent CTAs take tasks from a queue head in global memory
 // (one atomicAdd per task) until the queue is empty; the host orders tasks
 // longest first.  Each item runs exactly the sweep of sweep_core.cuh, so a
 // batched anneal equals the single-instance anneals of its instances bit for
@@ -19,7 +20,7 @@ __device__ __forceinline__ void run_task_item(const pq_batch_item& bi, const pq_
                                               const float* cpl_pool, const float* field_pool,
                                               const int32_t* csize_pool, const float* jperp_pool,
                                               unsigned char* words_pool, unsigned char* smem, const Group& g,
-                                              bool& bad, unsigned long long& nacc) {
+                                              int lanes_per_site, bool& bad, unsigned long long& nacc) {
     Item it;
     it.nbr = nbr_pool + in.tab_off;
     it.cpl = cpl_pool + in.tab_off;
@@ -36,7 +37,7 @@ __device__ __forceinline__ void run_task_item(const pq_batch_item& bi, const pq_
     it.sweep_base = run.sweep_base;
     it.nsched = run.nsched; it.mcsteps = run.mcsteps; it.global_moves = run.global_moves;
     it.beta = run.beta;
-    run_item_any(it, smem + bi.smem_off, g, bad, nacc);
+    run_item_any(it, smem + bi.smem_off, g, bad, nacc, lanes_per_site);
 }
 
 __global__ void __launch_bounds__(256, 2) batch_kernel(const pq_batch_task* __restrict__ tasks, int ntasks,
@@ -64,7 +65,7 @@ __global__ void __launch_bounds__(256, 2) batch_kernel(const pq_batch_task* __re
             const Group g{(int)threadIdx.x - gi * gthr, gthr,
                           (task.nitems == 1 && gthr == (int)blockDim.x) ? 0 : 1 + gi};
             run_task_item(bi, in, run, nbr_pool, cpl_pool, field_pool, csize_pool, jperp_pool, words_pool, smem, g,
-                          bad, nacc);
+                          task.lanes_per_site, bad, nacc);
         }
         __syncthreads();
     }

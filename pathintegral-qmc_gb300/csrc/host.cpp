@@ -5,6 +5,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <tuple>
 #include <vector>
 
 #include "piqmc_gb300.h"
@@ -141,18 +142,14 @@ int pq_generate_neighbors(int nspins, int64_t nkeys, const int64_t* rows, const 
 }
 
 // Greedy colouring in spin order over the undirected coupling graph (an entry
-// (i, j, J) with j != i and J != 0 couples i and j in both directions).
-int pq_color_graph(int n, int maxnb, const int32_t* nb_idx, const float* nb_j, int32_t* color) {
-    if (n <= 0 || maxnb < 0 || !color || (maxnb > 0 && (!nb_idx || !nb_j))) return -PQ_ERR_INVALID_ARG;
-    std::vector<std::vector<int>> adj((size_t)n);
-    for (int i = 0; i < n; ++i)
-        for (int m = 0; m < maxnb; ++m) {
-            const int j = nb_idx[(size_t)i * maxnb + m];
-            if (nb_j[(size_t)i * maxnb + m] == 0.0f || j == i) continue;
-            if (j < 0 || j >= n) return -PQ_ERR_BAD_INDEX;
-            adj[i].push_back(j);
-            adj[j].push_back(i);
-        }
+// (i, j, J) with j != i and J != 0 couples i and j in both directions).  When
+// that needs more than two colours, DSatur (Brelaz, "New methods to color the
+// vertices of a graph", CACM 1979: colour next the uncoloured vertex with the
+// most distinct colours among its neighbours, ties by degree, then by index)
+// is run as well and the colouring with fewer colours is kept, greedy on a tie.
+// A periodic lattice of odd side gets 3 colours this way instead of greedy's 4;
+// two-colourable graphs keep greedy's colouring.
+static int greedy_colors(int n, const std::vector<std::vector<int>>& adj, int32_t* color) {
     int ncol = 0;
     std::vector<int> mark;
     for (int i = 0; i < n; ++i) color[i] = -1;
@@ -166,6 +163,70 @@ int pq_color_graph(int n, int maxnb, const int32_t* nb_idx, const float* nb_j, i
         ncol = std::max(ncol, c + 1);
     }
     return ncol;
+}
+
+static int dsatur_colors(int n, const std::vector<std::vector<int>>& adj, int32_t* color) {
+    // seen[i]: colours among i's coloured neighbours (sorted, distinct); the heap holds
+    // (saturation, degree, -index) entries, stale ones skipped when popped
+    std::vector<std::vector<int>> seen((size_t)n);
+    std::vector<std::tuple<int, int, int>> heap;
+    heap.reserve((size_t)n * 2);
+    for (int i = 0; i < n; ++i) {
+        color[i] = -1;
+        heap.emplace_back(0, (int)adj[i].size(), -i);
+    }
+    std::make_heap(heap.begin(), heap.end());
+    int ncol = 0;
+    while (!heap.empty()) {
+        std::pop_heap(heap.begin(), heap.end());
+        const auto [sat, deg, negi] = heap.back();
+        heap.pop_back();
+        const int i = -negi;
+        if (color[i] >= 0 || sat != (int)seen[i].size()) continue;
+        int c = 0;
+        for (int u : seen[i]) {
+            if (u != c) break;
+            ++c;
+        }
+        color[i] = c;
+        ncol = std::max(ncol, c + 1);
+        for (int j : adj[i]) {
+            if (color[j] >= 0) continue;
+            auto& sj = seen[j];
+            auto it = std::lower_bound(sj.begin(), sj.end(), c);
+            if (it != sj.end() && *it == c) continue;
+            sj.insert(it, c);
+            heap.emplace_back((int)sj.size(), (int)adj[j].size(), -j);
+            std::push_heap(heap.begin(), heap.end());
+        }
+    }
+    return ncol;
+}
+
+int pq_color_graph(int n, int maxnb, const int32_t* nb_idx, const float* nb_j, int32_t* color) {
+    if (n <= 0 || maxnb < 0 || !color || (maxnb > 0 && (!nb_idx || !nb_j))) return -PQ_ERR_INVALID_ARG;
+    std::vector<std::vector<int>> adj((size_t)n);
+    for (int i = 0; i < n; ++i)
+        for (int m = 0; m < maxnb; ++m) {
+            const int j = nb_idx[(size_t)i * maxnb + m];
+            if (nb_j[(size_t)i * maxnb + m] == 0.0f || j == i) continue;
+            if (j < 0 || j >= n) return -PQ_ERR_BAD_INDEX;
+            adj[i].push_back(j);
+            adj[j].push_back(i);
+        }
+    for (auto& a : adj) {
+        std::sort(a.begin(), a.end());
+        a.erase(std::unique(a.begin(), a.end()), a.end());
+    }
+    const int ng = greedy_colors(n, adj, color);
+    if (ng <= 2) return ng;
+    std::vector<int32_t> alt((size_t)n);
+    const int nd = dsatur_colors(n, adj, alt.data());
+    if (nd < ng) {
+        std::copy(alt.begin(), alt.end(), color);
+        return nd;
+    }
+    return ng;
 }
 
 }  // extern "C"

@@ -64,8 +64,11 @@ struct Group {
     int bar;    // named barrier id; 0 = __syncthreads (the group is the whole CTA)
 };
 
+// A one-warp group needs no CTA barrier: __syncwarp orders its shared-memory
+// accesses as bar.sync would.
 __device__ __forceinline__ void group_sync(const Group& g) {
     if (g.bar == 0) __syncthreads();
+    else if (g.nthr == 32) __syncwarp();
     else asm volatile("bar.sync %0, %1;" ::"r"(g.bar), "r"(g.nthr) : "memory");
 }
 
@@ -213,11 +216,36 @@ __device__ __forceinline__ W update_fixed(W wi, const W (&d)[DEG], const float (
     return flips << q;
 }
 
+// One 32-bit half (bits 32*half .. 32*half+31) of update_fixed<32, DEG, uint64_t>:
+// the same updates, uniforms and arithmetic for the slices of that half, so two
+// lanes that take one half each and combine their flips reproduce it exactly.
+template <int DEG, typename KS>
+__device__ __forceinline__ uint64_t update_fixed_half64(uint64_t wi, const uint64_t (&d)[DEG], const float (&J)[DEG],
+                                                        float h, float jp, int q, int half, uint32_t i,
+                                                        uint32_t sweep, uint32_t rep, const KS& ks, float m2beta,
+                                                        float m2blog2e) {
+    const uint64_t up = (wi << 1) | (wi >> 63);
+    const uint64_t dn = (wi >> 1) | (wi << 63);
+    const uint64_t dlw = wi ^ up, drw = wi ^ dn;
+    const int sh = 32 * half;
+    uint32_t dq[DEG];
+#pragma unroll
+    for (int m = 0; m < DEG; ++m) dq[m] = (uint32_t)(d[m] >> sh) >> q;
+    const uint32_t f = update_half<16, DEG, KS>((uint32_t)(wi >> sh) >> q, dq, (uint32_t)(dlw >> sh) >> q,
+                                                (uint32_t)(drw >> sh) >> q, J, h, jp, q, 4 * half, i, sweep, rep, ks,
+                                                m2beta, m2blog2e);
+    return ((uint64_t)f << sh) << q;
+}
+
 // Anneal one item through its schedule.  sw: shared memory holding the item's
 // nrep x n words (staged by the caller); order: nrep x kMaxClasses bytes;
 // parity: nrep words.  Counts accepted local flips into nacc and out-of-range
 // indices into bad.
-template <typename W, int MAXDEG, int NQC, bool INLINE, typename KS>
+//
+// SPLIT (64-bit words with P = 64 only): two adjacent lanes share each site, one
+// 32-bit half of the world-line each, and exchange their flips after every slice
+// class; the sweep's serial work per lane halves, its result is unchanged.
+template <typename W, int MAXDEG, int NQC, bool INLINE, typename KS, bool SPLIT = false>
 __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* sw, uint8_t* order, uint32_t* parity,
                                               const Group& g, bool& bad, unsigned long long& nacc);
 
@@ -229,19 +257,25 @@ __device__ __forceinline__ void run_item(const Item& it, const PhiloxKeyTable& k
     run_item_body<W, MAXDEG, NQC, true, PhiloxKeysTab>(it, PhiloxKeysTab{keys}, sw, order, parity, g, bad, nacc);
 }
 
-template <typename W, int MAXDEG, int NQC>
+template <typename W, int MAXDEG, int NQC, bool SPLIT = false>
 __device__ __noinline__ void run_item_call(const Item& it, W* sw, uint8_t* order, uint32_t* parity, const Group& g,
                                            bool& bad, unsigned long long& nacc) {
-    run_item_body<W, MAXDEG, NQC, false, PhiloxKeysReg>(it, PhiloxKeysReg{it.key0, it.key1}, sw, order, parity, g,
-                                                        bad, nacc);
+    run_item_body<W, MAXDEG, NQC, false, PhiloxKeysReg, SPLIT>(it, PhiloxKeysReg{it.key0, it.key1}, sw, order,
+                                                               parity, g, bad, nacc);
 }
 
-template <typename W, int MAXDEG, int NQC, bool INLINE, typename KS>
+template <typename W, int MAXDEG, int NQC, bool INLINE, typename KS, bool SPLIT>
 __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* sw, uint8_t* order, uint32_t* parity,
                                               const Group& g, bool& bad, unsigned long long& nacc) {
     const int n = it.n, P = it.P, S = it.stride, nrep = it.nrep;
     const W mask = full_mask<W>(P);
     const int nclass_q = P == 1 ? 1 : ((P & 1) ? 3 : 2);
+    static_assert(!SPLIT || (sizeof(W) == 8 && NQC == 32), "lane pairs split 64-slice world-lines only");
+    // site walk of the local updates: one lane per site, or a lane pair per site
+    const int site_tid = SPLIT ? g.tid >> 1 : g.tid;
+    const int site_nthr = SPLIT ? g.nthr >> 1 : g.nthr;
+    const int half = SPLIT ? (g.tid & 1) : 0;
+    const unsigned pair_mask = 3u << ((g.tid & 31) & ~1);
     for (int gs = 0; gs < it.nsched; ++gs) {
         const float jp = P == 1 ? 0.0f : __ldg(it.jperp + gs);
         const float beta = it.betas ? __ldg(it.betas + gs) : it.beta;
@@ -257,12 +291,19 @@ __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* s
             // its spins one at a time through every slice class (in the replica's parity
             // order): the same result as slice class by slice class over all spins, with
             // one barrier and one load of the neighbourhood per spin and class.
+            // The group's threads walk the phase's sites replica after replica, each
+            // replica over the real size of the class it visits in this phase.
             for (int p = 0; p < it.nclass; ++p) {
-                int rl = 0, s = g.tid;
-                while (s >= S) { s -= S; ++rl; }
+                int rl = 0, s = site_tid;
+                int cls = order[p], cs = it.csize[cls];
+                while (s >= cs) {
+                    s -= cs;
+                    if (++rl == nrep) break;
+                    cls = order[rl * kMaxClasses + p];
+                    cs = it.csize[cls];
+                }
                 for (; rl < nrep;) {
-                    const int cls = order[rl * kMaxClasses + p];
-                    if (s < it.csize[cls]) {
+                    {
                         const int i = cls * S + s;
                         W* rw = sw + rl * n;
                         W wi = rw[i];
@@ -275,7 +316,12 @@ __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* s
                         for (int qq = 0; qq < nclass_q; ++qq) {
                             const int q = nclass_q == 2 ? (qq ^ (int)first) : qq;
                             W fl;
-                            if constexpr (NQC > 0) {
+                            if constexpr (SPLIT) {
+                                const W own = update_fixed_half64<MAXDEG, KS>(wi, d, J, h, jp, q, half, (uint32_t)i,
+                                                                             sweep, rep, ks, m2beta, m2blog2e);
+                                nacc += __popcll((unsigned long long)own);
+                                fl = own | (W)__shfl_xor_sync(pair_mask, (unsigned long long)own, 1);
+                            } else if constexpr (NQC > 0) {
                                 fl = update_fixed<NQC, MAXDEG, W, KS>(wi, d, J, h, jp, q, (uint32_t)i, sweep, rep, ks,
                                                                       m2beta, m2blog2e);
                             } else {
@@ -308,12 +354,18 @@ __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* s
                             wi ^= fl;
 #pragma unroll
                             for (int m = 0; m < MAXDEG; ++m) d[m] ^= fl;
-                            nacc += sizeof(W) == 8 ? __popcll((unsigned long long)fl) : __popc((uint32_t)fl);
+                            if constexpr (!SPLIT)
+                                nacc += sizeof(W) == 8 ? __popcll((unsigned long long)fl) : __popc((uint32_t)fl);
                         }
-                        rw[i] = wi;
+                        if (half == 0) rw[i] = wi;
                     }
-                    s += g.nthr;
-                    while (s >= S) { s -= S; ++rl; }
+                    s += site_nthr;
+                    while (s >= cs) {
+                        s -= cs;
+                        if (++rl == nrep) break;
+                        cls = order[rl * kMaxClasses + p];
+                        cs = it.csize[cls];
+                    }
                 }
                 group_sync(g);
             }
@@ -323,10 +375,11 @@ __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* s
             const uint32_t sweep = (uint32_t)(it.sweep_base + (int64_t)gs * it.mcsteps + it.mcsteps - 1);
             for (int cls = 0; cls < it.nclass; ++cls) {
                 const int csz = it.csize[cls];
+                if (csz <= 0) continue;
                 int rl = 0, s = g.tid;
-                while (s >= S) { s -= S; ++rl; }
+                while (s >= csz) { s -= csz; ++rl; }
                 for (; rl < nrep;) {
-                    if (s < csz) {
+                    {
                         const int i = cls * S + s;
                         W* rw = sw + rl * n;
                         const W wi = rw[i];
@@ -349,7 +402,7 @@ __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* s
                         if (decide(E, pq_u01(rnd.x), m2beta, m2blog2e)) rw[i] = wi ^ mask;
                     }
                     s += g.nthr;
-                    while (s >= S) { s -= S; ++rl; }
+                    while (s >= csz) { s -= csz; ++rl; }
                 }
                 group_sync(g);
             }
@@ -374,7 +427,7 @@ __device__ __forceinline__ void stage_out(const Item& it, const W* sw, const Gro
 
 // Word type / degree / compile-time P dispatch of one item.
 __device__ inline void run_item_any(const Item& it, unsigned char* smem, const Group& g, bool& bad,
-                                    unsigned long long& nacc) {
+                                    unsigned long long& nacc, int lanes_per_site = 1) {
     // layout of the item's shared memory: words, then order bytes, then parity words
     const size_t wbytes = it.P <= 32 ? 4 : 8;
     const size_t words_bytes = ((size_t)it.nrep * it.n * wbytes + 15) & ~(size_t)15;
@@ -392,7 +445,9 @@ __device__ inline void run_item_any(const Item& it, unsigned char* smem, const G
     } else {
         uint64_t* sw = reinterpret_cast<uint64_t*>(smem);
         stage_in<uint64_t>(it, sw, g);
-        if (it.maxdeg == 4 && it.P == 64) run_item_call<uint64_t, 4, 32>(it, sw, order, parity, g, bad, nacc);
+        if (it.maxdeg == 4 && it.P == 64 && lanes_per_site == 2)
+            run_item_call<uint64_t, 4, 32, true>(it, sw, order, parity, g, bad, nacc);
+        else if (it.maxdeg == 4 && it.P == 64) run_item_call<uint64_t, 4, 32>(it, sw, order, parity, g, bad, nacc);
         else if (it.maxdeg <= 4) run_item_call<uint64_t, 4, 0>(it, sw, order, parity, g, bad, nacc);
         else run_item_call<uint64_t, 8, 0>(it, sw, order, parity, g, bad, nacc);
         stage_out<uint64_t>(it, sw, g);

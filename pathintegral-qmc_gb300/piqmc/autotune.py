@@ -2,7 +2,8 @@
 
 Two levels.  Per instance shape (padded slot count rounded up to a power of
 two, P, couplings per spin, replicas) ``measure`` times every candidate tile --
-``gwarps`` warps per work item and ``rpc`` replicas per item -- on a probe batch
+``gwarps`` warps per work item, ``rpc`` replicas per item, and for 64-slice
+instances one lane or a lane pair per site -- on a probe batch
 made of enough copies of the instance that the tile's tasks fill two CTAs per
 SM, for a few field steps: its rate is the GPU's throughput on that shape with
 every warp slot busy.  Per batch, ``plan`` then picks one tile per instance to
@@ -25,7 +26,9 @@ import os
 import numpy as np
 import torch
 
-CANDIDATES = ((1, 1), (1, 2), (1, 4), (1, 8), (2, 1), (2, 2), (2, 4), (4, 1), (4, 2), (8, 1), (8, 2))
+_BASE = ((1, 1), (1, 2), (1, 4), (1, 8), (2, 1), (2, 2), (2, 4), (4, 1), (4, 2), (8, 1), (8, 2))
+# (gwarps, rpc, lanes_per_site); lane pairs only for instances that support them
+CANDIDATES = tuple((gw, rpc, 1) for gw, rpc in _BASE) + tuple((gw, rpc, 2) for gw, rpc in _BASE)
 CTAS_PER_SM = 2
 _cache = {}
 _loaded = False
@@ -46,7 +49,8 @@ def _load():
             with open(path) as f:
                 for k, v in json.load(f).items():
                     if isinstance(v, dict):
-                        _cache[k] = {tuple(int(x) for x in t.split(",")): float(r) for t, r in v.items()}
+                        _cache[k] = {(tuple(int(x) for x in t.split(",")) + (1,))[:3]: float(r)
+                                     for t, r in v.items()}
         except (OSError, ValueError):
             pass
 
@@ -56,7 +60,7 @@ def _save():
     if path:
         try:
             with open(path, "w") as f:
-                json.dump({k: {"%d,%d" % t: r for t, r in v.items()} for k, v in _cache.items()}, f, indent=1,
+                json.dump({k: {"%d,%d,%d" % t: r for t, r in v.items()} for k, v in _cache.items()}, f, indent=1,
                           sort_keys=True)
         except OSError:
             pass
@@ -75,23 +79,25 @@ def warp_slots(sms):
 
 
 def measure(problem, P, R, steps=8, candidates=CANDIDATES, repeats=2):
-    """Time each candidate tile on a probe batch that fills the GPU; returns {(gwarps, rpc): updates/s}.
+    """Time each candidate tile on a probe batch that fills the GPU; returns {(gwarps, rpc, lanes): updates/s}.
 
     Each candidate is timed ``repeats`` times over ``steps`` field steps and keeps its best time."""
     from . import _native
-    from .batch import SMEM_TASK_BUDGET, WARPS, Batch
+    from .batch import SMEM_TASK_BUDGET, WARPS, Batch, lane_pairs_supported
     lib = _native.lib()
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     g = np.random.default_rng(0)
     spins = np.where(g.random((R, problem.n, P)) < 0.5, -1, 1).astype(np.int8)
     sched = np.linspace(3.0, 1e-8, steps + 1)
     rates = {}
-    for gw, rpc in candidates:
+    for gw, rpc, lps in candidates:
         if rpc > R or lib.pq_batch_smem_bytes(rpc, problem.nslots, P) > SMEM_TASK_BUDGET:
+            continue
+        if lps == 2 and not lane_pairs_supported(problem, P):
             continue
         items = -(-R // rpc)
         copies = max(1, -(-CTAS_PER_SM * sms * (WARPS // gw) // items))
-        B = Batch([problem] * copies, [R] * copies, [P] * copies, tiles=[(gw, rpc)] * copies)
+        B = Batch([problem] * copies, [R] * copies, [P] * copies, tiles=[(gw, rpc, lps)] * copies)
         B.set_spins([spins] * copies)
         B.anneal(sched[:1], 0.05, seed=1)
         torch.cuda.synchronize()
@@ -104,14 +110,14 @@ def measure(problem, P, R, steps=8, candidates=CANDIDATES, repeats=2):
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1)
             best_ms = ms if best_ms is None else min(best_ms, ms)
-        rates[(gw, rpc)] = copies * R * problem.n * P * steps / (best_ms * 1e-3)
+        rates[(gw, rpc, lps)] = copies * R * problem.n * P * steps / (best_ms * 1e-3)
     return rates
 
 
 def plan(shapes, tables, slots, candidates=CANDIDATES):
     """Tiles minimising the predicted field-step time of a batch.
 
-    ``shapes``: (slots n_i, P_i, R_i) per instance; ``tables``: {(gwarps, rpc): updates/s at fill}
+    ``shapes``: (slots n_i, P_i, R_i) per instance; ``tables``: {(gwarps, rpc, lanes): updates/s at fill}
     per instance; ``slots``: warp slots of the GPU.  Returns (tiles, predicted seconds per field
     step)."""
     n_inst, C = len(shapes), len(candidates)
@@ -120,8 +126,8 @@ def plan(shapes, tables, slots, candidates=CANDIDATES):
     dur = np.full((n_inst, C), np.inf)
     cost = np.full((n_inst, C), np.inf)
     for i, ((n, P, R), tab) in enumerate(zip(shapes, tables)):
-        for c, (gw, rpc) in enumerate(candidates):
-            rate = tab.get((gw, rpc))
+        for c, (gw, rpc, _) in enumerate(candidates):
+            rate = tab.get(candidates[c])
             if not rate or rpc > R:
                 continue
             w = rate / slots                        # updates/s of one busy warp slot
@@ -163,6 +169,6 @@ def tune(batch):
 
 
 def table():
-    """The cached measurements: {shape key: {(gwarps, rpc): updates/s at fill}}."""
+    """The cached measurements: {shape key: {(gwarps, rpc, lanes): updates/s at fill}}."""
     _load()
     return dict(_cache)

@@ -4,10 +4,12 @@ A ``Batch`` holds instances of different size, slice count and replica count.
 Their tables are concatenated into pools, their world-lines into one byte pool,
 and the work is cut into *items* (``rpc`` replicas of one instance, run by a
 group of ``gwarps`` warps) packed into *tasks* (items sharing a CTA, each with
-its own named barrier).  One persistent launch (``pq_batch_anneal``) drains the
+its own named barrier).  A tile may add ``lanes_per_site`` = 2: a 64-slice
+instance then gives each site a lane pair, one 32-bit half of the world-line
+each, which halves the serial work of a sweep (same result).  One persistent launch (``pq_batch_anneal``) drains the
 task queue; tasks are ordered longest first.  The tile of each instance --
-``(gwarps, rpc)`` -- comes from ``piqmc.autotune`` (measured) or a size
-heuristic.
+``(gwarps, rpc[, lanes_per_site])`` -- comes from ``piqmc.autotune`` (measured)
+or a size heuristic.
 
 ``anneal`` splits the schedule into chunks of ``chunk`` field steps, one launch
 each, and can capture the chunk sequence as a CUDA graph that is replayed for
@@ -31,7 +33,7 @@ INST_DTYPE = np.dtype([("tab_off", "<i8"), ("field_off", "<i8"), ("csize_off", "
                        ("key0", "<u4"), ("key1", "<u4"), ("pad", "<i4")])
 ITEM_DTYPE = np.dtype([("inst", "<i4"), ("nrep", "<i4"), ("replica0", "<i4"), ("smem_off", "<i4"),
                        ("word_off", "<i8")])
-TASK_DTYPE = np.dtype([("item0", "<i4"), ("nitems", "<i4"), ("gwarps", "<i4"), ("pad", "<i4")])
+TASK_DTYPE = np.dtype([("item0", "<i4"), ("nitems", "<i4"), ("gwarps", "<i4"), ("lanes_per_site", "<i4")])
 assert INST_DTYPE.itemsize == 56 and ITEM_DTYPE.itemsize == 24 and TASK_DTYPE.itemsize == 16
 
 THREADS = 256
@@ -53,6 +55,22 @@ def heuristic_tile(nslots, P, R):
     while rpc < R and rpc * S < 32 and _native.lib().pq_batch_smem_bytes(rpc * 2, nslots, P) < SMEM_TASK_BUDGET // 2:
         rpc *= 2
     return 1, min(rpc, R)
+
+
+def lane_pairs_supported(problem, P):
+    """Items of this instance can give each site a lane pair (64-slice world-lines, 4 couplings)."""
+    return P == 64 and problem.maxdeg == 4
+
+
+def normalise_tile(tile, problem, P):
+    """(gwarps, rpc[, lanes_per_site]) -> (gwarps, rpc, lanes_per_site); lane pairs only where supported."""
+    gw, rpc = int(tile[0]), int(tile[1])
+    lps = int(tile[2]) if len(tile) > 2 else 1
+    if gw not in (1, 2, 4, 8) or rpc < 1 or lps not in (1, 2):
+        raise ValueError("tile %r: gwarps in {1, 2, 4, 8}, rpc >= 1, lanes_per_site in {1, 2}" % (tuple(tile),))
+    if lps == 2 and not lane_pairs_supported(problem, P):
+        lps = 1
+    return gw, rpc, lps
 
 
 class Batch:
@@ -105,7 +123,8 @@ class Batch:
         # tiles, items, tasks
         if tiles is None and tuner is not None:
             tiles = tuner(self)
-        self.tiles = tiles or [heuristic_tile(pb.nslots, P, R) for pb, P, R in zip(self.problems, self.P, self.R)]
+        tiles = tiles or [heuristic_tile(pb.nslots, P, R) for pb, P, R in zip(self.problems, self.P, self.R)]
+        self.tiles = [normalise_tile(t, pb, P) for t, pb, P in zip(tiles, self.problems, self.P)]
         self._build_tasks(lib)
         self._jperp_key = None
         self._graphs = {}
@@ -115,13 +134,13 @@ class Batch:
     def _build_tasks(self, lib):
         items = []
         for i, (pb, P, R) in enumerate(zip(self.problems, self.P, self.R)):
-            gw, rpc = self.tiles[i]
+            gw, rpc, lps = self.tiles[i]
             wbytes = 4 if P <= 32 else 8
             for r0 in range(0, R, rpc):
                 nrep = min(rpc, R - r0)
                 smem = lib.pq_batch_smem_bytes(nrep, pb.nslots, P)
                 cost = pb.nslots * P * nrep / (32.0 * gw)
-                items.append((cost, gw, smem, i, nrep, r0, self.word_offsets[i] + r0 * pb.nslots * wbytes))
+                items.append((cost, (gw, lps), smem, i, nrep, r0, self.word_offsets[i] + r0 * pb.nslots * wbytes))
         if any(it[2] > SMEM_TASK_BUDGET for it in items):
             raise _native.PiqmcError(_native.PQ_ERR_TOO_LARGE, "an item needs more than %d B of shared memory"
                                      % SMEM_TASK_BUDGET)
@@ -131,25 +150,25 @@ class Batch:
         for it in items:
             by_gw.setdefault(it[1], []).append(it)
         tasks = []
-        for gw, lst in by_gw.items():
+        for (gw, lps), lst in by_gw.items():
             per = WARPS // gw
             cur = []
             used = 0
             for it in lst:
                 if cur and (len(cur) == per or used + _align(it[2]) > SMEM_TASK_BUDGET):
-                    tasks.append((gw, cur))
+                    tasks.append(((gw, lps), cur))
                     cur, used = [], 0
                 cur.append(it)
                 used += _align(it[2])
             if cur:
-                tasks.append((gw, cur))
+                tasks.append(((gw, lps), cur))
         tasks.sort(key=lambda t: -max(it[0] for it in t[1]))
         item_arr = np.zeros(len(items), dtype=ITEM_DTYPE)
         task_arr = np.zeros(len(tasks), dtype=TASK_DTYPE)
         k = 0
         max_smem = 16
-        for t, (gw, lst) in enumerate(tasks):
-            task_arr[t] = (k, len(lst), gw, 0)
+        for t, ((gw, lps), lst) in enumerate(tasks):
+            task_arr[t] = (k, len(lst), gw, lps)
             off = 0
             for it in lst:
                 item_arr[k] = (it[3], it[4], it[5], off, it[6])

@@ -5,11 +5,16 @@ device form the packed kernel reads:
 
 * self entries become the field h_i; zero couplings (the table's padding) are
   dropped -- adding +-0 never changes a decision;
-* spins are coloured greedily; each colour is cut into ``subclasses`` update
-  classes of near-equal size by a fixed hash of the spin index, giving M
-  independent sets (M <= 32).  Visiting many small classes in a random order
-  per sweep makes the sweep behave like the reference's random sequential
-  order; plain colour order anneals measurably worse;
+* spins are coloured (greedy in spin order, or DSatur when that needs fewer
+  colours); each colour is cut, in the order of a fixed hash of the spin index,
+  into update classes of T = ceil(n / (2 * subclasses)) spins (T rounded up to a
+  multiple of ``quantum`` once the classes are that large) plus one class with
+  the remainder, giving M independent sets (M <= 32; T grows if needed).  A
+  two-colourable graph with colours of n/2 spins gets ``subclasses`` classes per
+  colour; a small third colour gets one class instead of ``subclasses``
+  near-empty ones.  Visiting many small classes in a random order per sweep
+  makes the sweep behave like the reference's random sequential order; plain
+  colour order anneals measurably worse;
 * spins are relabelled into "device order": class c occupies slots
   [c*S, c*S + size_c) of a padded space of M*S slots; ``perm[i]`` is the slot of
   original spin i;
@@ -84,13 +89,20 @@ class Problem:
         if nc > MAX_CLASSES:
             raise _native.PiqmcError(_native.PQ_ERR_UNSUPPORTED, "graph needs %d colours (> %d)" % (nc, MAX_CLASSES))
         self.ncolors = int(nc)
-        K = max(1, min(int(subclasses), MAX_CLASSES // self.ncolors))
+        K = max(1, int(subclasses))
         self.subclasses = K
-        # sub-class sizes are multiples of `quantum` spins (the thread count a
-        # replica's CTA uses), so every thread has the same work in every phase
+        # class size T: n / (2K) spins, a multiple of `quantum` (the thread count a
+        # replica's CTA uses) once classes are that large, so that every thread has
+        # the same work in the phases of full classes
         if quantum is None:
             quantum = 128 if n >= 4096 else 32
         self.quantum = int(quantum)
+        counts = np.bincount(color, minlength=self.ncolors)
+        T = max(1, -(-n // (2 * K)))
+        if n >= 2 * K * self.quantum:
+            T = -(-T // self.quantum) * self.quantum
+        while int(np.sum(-(-np.maximum(counts, 1) // T))) > MAX_CLASSES:
+            T += 1
         h = _mix32(np.arange(n, dtype=np.uint64))
         cls = np.empty(n, dtype=np.int64)
         base = 0
@@ -98,10 +110,8 @@ class Problem:
             members = np.nonzero(color == c)[0]
             ranked = members[np.argsort(h[members], kind="stable")]
             m = len(members)
-            chunk = -(-max(m, 1) // K)
-            chunk = -(-chunk // self.quantum) * self.quantum if m >= K * self.quantum else chunk
-            cls[ranked] = base + np.arange(m) // chunk
-            base += -(-m // chunk) if m else 0
+            cls[ranked] = base + np.arange(m) // T
+            base += -(-m // T) if m else 0
         M = int(base)
         sizes = np.bincount(cls, minlength=M)
         S = int(sizes.max()) if n else 1

@@ -12,7 +12,7 @@ def _instances(seed=0):
     from piqmc import tools
     g = np.random.default_rng(seed)
     shapes = [(4, True, 1, 3), (5, True, 7, 2), (8, True, 20, 8), (6, False, 16, 1), (9, True, 33, 3),
-              (12, True, 64, 2), (7, True, 20, 5), (10, True, 32, 4), (3, True, 2, 8)]
+              (12, True, 64, 2), (7, True, 20, 5), (10, True, 32, 4), (3, True, 2, 8), (9, True, 64, 5)]
     nbs, R, P = [], [], []
     for L, per, p, r in shapes:
         J = lattice(L, per, g, dist=lambda x: x.normal(), fields=(lambda x: x.normal(0, 0.2)) if L % 2 else None)
@@ -34,15 +34,21 @@ def _single(nbs, R, P, g_spins, sched, T, seed, mcsteps=1, global_moves=0):
     return out
 
 
-@pytest.mark.parametrize("tiles", ["heuristic", "mixed"])
+@pytest.mark.parametrize("tiles", ["heuristic", "mixed", "lane_pairs"])
 def test_batch_equals_single(tiles):
     from piqmc import batch
     nbs, R, P, g = _instances()
     spins = [np.where(g.random((r, nb.shape[0], p)) < 0.5, -1, 1).astype(np.int8) for nb, r, p in zip(nbs, R, P)]
     t = None
     if tiles == "mixed":
-        t = [(1, 1), (2, 2), (1, 8), (4, 1), (1, 3), (2, 1), (8, 1), (1, 2), (1, 4)]
+        t = [(1, 1), (2, 2), (1, 8), (4, 1), (1, 3), (2, 1), (8, 1), (1, 2), (1, 4), (2, 2)]
+    elif tiles == "lane_pairs":
+        # the two 64-slice instances take lane pairs (the others fall back to one lane per site)
+        t = [(1, 1, 2), (2, 2, 2), (1, 8, 2), (4, 1, 2), (1, 3, 2), (1, 1, 2), (8, 1, 2), (1, 2, 2), (1, 4, 2),
+             (2, 2, 2)]
     B = batch.Batch(nbs, R, P, tiles=t)
+    if tiles == "lane_pairs":
+        assert [tl[2] for tl in B.tiles] == [2 if p == 64 else 1 for p in P]
     B.set_spins(spins)
     sched = np.linspace(3.0, 1e-8, 9)
     B.anneal(sched, 0.05, seed=11, mcsteps=2, global_moves=1)

@@ -149,6 +149,50 @@ def test_greedy_colouring(native):
         assert col[a] != col[b]
 
 
+def _colour(native, L, periodic, seed):
+    from piqmc import tools
+    J = lattice(L, periodic, np.random.default_rng(seed))
+    n = L * L
+    nbs = tools.GenerateNeighbors(n, J, 4)
+    idx = np.ascontiguousarray(np.trunc(nbs[:, :, 0]).astype(np.int32))
+    jv = np.ascontiguousarray(nbs[:, :, 1].astype(np.float32))
+    col = np.empty(n, np.int32)
+    nc = native.pq_color_graph(n, 4, idx.ctypes.data, jv.ctypes.data, col.ctypes.data)
+    for (a, b) in J.keys():
+        assert a == b or col[a] != col[b]
+    assert set(col.tolist()) == set(range(nc))
+    return nc, col, J
+
+
+@pytest.mark.parametrize("L", [5, 9, 15, 33])
+def test_colouring_odd_torus_uses_three_colours(native, L):
+    """Greedy in spin order needs 4 colours on an odd periodic lattice; DSatur finds 3."""
+    nc, _, _ = _colour(native, L, True, L)
+    assert nc == 3
+
+
+@pytest.mark.parametrize("L,periodic", [(8, True), (16, True), (7, False), (10, False)])
+def test_colouring_bipartite_keeps_greedy(native, L, periodic):
+    nc, col, J = _colour(native, L, periodic, L)
+    assert nc == 2
+    # greedy in spin order on a connected bipartite lattice: colour = checkerboard from spin 0
+    x, y = np.arange(L * L) % L, np.arange(L * L) // L
+    assert np.array_equal(col, (x + y) % 2)
+
+
+def test_class_layout_even_and_odd_lattices(native):
+    """Balanced two-colourings keep subclasses classes per colour; a small third colour gets one class."""
+    from piqmc import fast, tools
+    for L, want_classes in ((80, 14), (32, 16), (8, 16)):
+        J = lattice(L, True, np.random.default_rng(L))
+        p = fast.Problem(tools.GenerateNeighbors(L * L, J, 4), on_device=False)
+        assert p.nclass == want_classes
+    J = lattice(33, True, np.random.default_rng(3))
+    p = fast.Problem(tools.GenerateNeighbors(33 * 33, J, 4), on_device=False)
+    assert p.ncolors == 3 and p.nclass <= 18
+    assert p.nslots <= 1.15 * 33 * 33
+
+
 GENERATORS = {
     "ising2d_5": lambda t, rs: t.Generate2DIsingInstance(5, rs),
     "ising2d_2": lambda t, rs: t.Generate2DIsingInstance(2, rs),
@@ -195,22 +239,27 @@ def test_autotune_plan_balances_the_batch():
     """The batch planner keeps the efficient tile where it can and splits the items that would outlast the rest."""
     from piqmc import autotune
     slots = 2432
-    small = {(1, 8): 3.0e11, (1, 1): 1.0e11, (8, 1): 0.5e11}
-    big = {(1, 8): 3.0e11, (2, 1): 2.5e11, (8, 1): 2.0e11}
+    small = {(1, 8, 1): 3.0e11, (1, 1, 1): 1.0e11, (8, 1, 1): 0.5e11}
+    big = {(1, 8, 1): 3.0e11, (2, 1, 1): 2.5e11, (8, 1, 1): 2.0e11}
     # many small instances and one large one: the large one's (1, 8) item alone would take
     # 2048*64*8 / 1.23e8 = 8.5 ms per step against ~1 ms for the whole batch's load
     shapes = [(64, 16, 8)] * 200 + [(2048, 64, 8)]
     tiles, pred = autotune.plan(shapes, [small] * 200 + [big], slots)
-    assert tiles[:200] == [(1, 8)] * 200
-    assert tiles[200] == (8, 1)
-    w8 = big[(8, 1)] / slots
-    total = (200 * 64 * 16 * 8 / (small[(1, 8)] / slots) + 2048 * 64 * 8 / w8) / slots
+    assert tiles[:200] == [(1, 8, 1)] * 200
+    assert tiles[200] == (8, 1, 1)
+    w8 = big[(8, 1, 1)] / slots
+    total = (200 * 64 * 16 * 8 / (small[(1, 8, 1)] / slots) + 2048 * 64 * 8 / w8) / slots
     assert pred == pytest.approx(max(total, 2048 * 64 / (8 * w8)))
     # a GPU full of equal small instances keeps the most efficient tile
     tiles, _ = autotune.plan([(64, 16, 8)] * 5000, [small] * 5000, slots)
-    assert set(tiles) == {(1, 8)}
+    assert set(tiles) == {(1, 8, 1)}
     # tiles with more replicas than the instance has are never chosen
     tiles, _ = autotune.plan([(64, 16, 1)], [small], slots)
-    assert tiles == [(8, 1)] or tiles == [(1, 1)]
+    assert tiles == [(8, 1, 1)] or tiles == [(1, 1, 1)]
+    # a lane-pair tile that shortens the critical item wins for it
+    pairs = dict(big)
+    pairs[(8, 1, 2)] = 3.5e11
+    tiles, _ = autotune.plan(shapes, [small] * 200 + [pairs], slots)
+    assert tiles[200] == (8, 1, 2)
     with pytest.raises(ValueError):
         autotune.plan([(64, 16, 8)], [{}], slots)
