@@ -13,9 +13,9 @@ minimise the predicted time of one field step,
 
 where an item of instance i with tile (gw, rpc) takes ``n_i P_i rpc / (gw w)``
 seconds per field step and ``w`` is the measured per-warp-slot rate of that
-tile.  The most efficient tile of a small instance is often one warp on eight
-replicas; the largest instances of a batch need more warps per item, or their
-items outlast the rest of the batch.  Rate tables are cached per GPU name in
+tile.  The most efficient tile of a small instance is often one warp on eight replicas; the
+largest instances of a batch need more warps per item, or their items outlast
+the rest of the batch.  Rate tables are cached per GPU name in
 memory and, when ``PIQMC_TUNE_CACHE`` names a file, on disk (JSON).
 
 Use: ``Batch(nbs_list, replicas, slices, tuner=autotune.tune)``.
@@ -118,8 +118,10 @@ def plan(shapes, tables, slots, candidates=CANDIDATES):
     """Tiles minimising the predicted field-step time of a batch.
 
     ``shapes``: (slots n_i, P_i, R_i) per instance; ``tables``: {(gwarps, rpc, lanes): updates/s at fill}
-    per instance; ``slots``: warp slots of the GPU.  Returns (tiles, predicted seconds per field
-    step)."""
+    per instance; ``slots``: warp slots of the GPU.  For a cap T on the item duration every
+    instance takes its cheapest tile (fewest warp-seconds) whose items last at most T; the
+    prediction of a choice is max(warp-seconds / slots, longest item), minimised over the caps.
+    Returns (tiles, predicted seconds per field step)."""
     n_inst, C = len(shapes), len(candidates)
     if n_inst == 0:
         return [], 0.0

@@ -73,6 +73,41 @@ def normalise_tile(tile, problem, P):
     return gw, rpc, lps
 
 
+def sweep_variant(P):
+    """Which compiled sweep an item of P slices runs (the kernel has one per fixed P it
+    specialises, and one generic per word size)."""
+    return P if P in (16, 20, 32, 64) else (0 if P <= 32 else 1)
+
+
+def pack_tasks(items):
+    """Items ``(cost, (gwarps, lanes, variant), smem bytes, ...)`` -> tasks ``[(kind, [items])]``.
+
+    Items of one kind, in decreasing cost, fill a task up to ``WARPS // gwarps`` items
+    within the shared-memory budget, so the warps of a CTA run one compiled sweep; tasks
+    are ordered by their longest item, longest first (the persistent CTAs take them in
+    that order)."""
+    items = sorted(items, key=lambda t: -t[0])
+    by_kind = {}
+    for it in items:
+        by_kind.setdefault(it[1], []).append(it)
+    tasks = []
+    for kind, lst in by_kind.items():
+        gw = kind[0]
+        per = WARPS // gw
+        cur = []
+        used = 0
+        for it in lst:
+            if cur and (len(cur) == per or used + _align(it[2]) > SMEM_TASK_BUDGET):
+                tasks.append((kind, cur))
+                cur, used = [], 0
+            cur.append(it)
+            used += _align(it[2])
+        if cur:
+            tasks.append((kind, cur))
+    tasks.sort(key=lambda t: -max(it[0] for it in t[1]))
+    return tasks
+
+
 class Batch:
     """Many sparse instances with their replicas, resident on the device."""
 
@@ -140,35 +175,18 @@ class Batch:
                 nrep = min(rpc, R - r0)
                 smem = lib.pq_batch_smem_bytes(nrep, pb.nslots, P)
                 cost = pb.nslots * P * nrep / (32.0 * gw)
-                items.append((cost, (gw, lps), smem, i, nrep, r0, self.word_offsets[i] + r0 * pb.nslots * wbytes))
+                items.append((cost, (gw, lps, sweep_variant(P)), smem, i, nrep, r0,
+                              self.word_offsets[i] + r0 * pb.nslots * wbytes))
         if any(it[2] > SMEM_TASK_BUDGET for it in items):
             raise _native.PiqmcError(_native.PQ_ERR_TOO_LARGE, "an item needs more than %d B of shared memory"
                                      % SMEM_TASK_BUDGET)
-        items.sort(key=lambda t: -t[0])
-        # pack items with the same gwarps into tasks, longest first, within the smem budget
-        by_gw = {}
-        for it in items:
-            by_gw.setdefault(it[1], []).append(it)
-        tasks = []
-        for (gw, lps), lst in by_gw.items():
-            per = WARPS // gw
-            cur = []
-            used = 0
-            for it in lst:
-                if cur and (len(cur) == per or used + _align(it[2]) > SMEM_TASK_BUDGET):
-                    tasks.append(((gw, lps), cur))
-                    cur, used = [], 0
-                cur.append(it)
-                used += _align(it[2])
-            if cur:
-                tasks.append(((gw, lps), cur))
-        tasks.sort(key=lambda t: -max(it[0] for it in t[1]))
+        tasks = pack_tasks(items)
         item_arr = np.zeros(len(items), dtype=ITEM_DTYPE)
         task_arr = np.zeros(len(tasks), dtype=TASK_DTYPE)
         k = 0
         max_smem = 16
-        for t, ((gw, lps), lst) in enumerate(tasks):
-            task_arr[t] = (k, len(lst), gw, lps)
+        for t, (kind, lst) in enumerate(tasks):
+            task_arr[t] = (k, len(lst), kind[0], kind[1])
             off = 0
             for it in lst:
                 item_arr[k] = (it[3], it[4], it[5], off, it[6])
