@@ -80,6 +80,69 @@ __device__ __forceinline__ int fp32_decide(float xf, int32_t rv) {
     return -1;
 }
 
+// The same decision from a cheaper estimate, for the warp kernels: x' = e * rl with
+// rl = fl(fl(1 / T) * fl(log2 e)) (set once per temperature) and 2^x' by ex2.approx.
+// Against exp((double)fl(e / T)) the estimate errs by under 5e-5 (relative) wherever
+// exp > 1e-30: ex2.approx of a once-rounded argument is within 2e-5 of expf_neg there
+// (pq_guard_band_probe checks every such FP32 input), the three extra roundings of
+// the argument add under 2.1e-5 and the quotient's own rounding 5.2e-6.  Below that
+// both sides are under about 1e-30, far below any nonzero uniform (>= 2^-31).  A 1e-4
+// band around the FP32 uniform therefore leaves only decisions that the exact path
+// would also find close -- including every close call it records -- to that path.
+// 1 accept, 0 reject, -1 undecided (rv == 0, e > 0 or NaN, or inside the band).
+__device__ __forceinline__ int quick_decide(float e, float rl, int32_t rv) {
+    if (rv <= 0 || !(e <= 0.0f)) return -1;
+    const float pf = pq_ex2_approx(__fmul_rn(e, rl));
+    const float qf = __fmul_rn((float)rv, 4.656612873077392578125e-10f);  // 2^-31
+    if (pf > __fmul_rn(qf, 1.0001f)) return 1;
+    if (pf < __fmul_rn(qf, 0.9999f)) return 0;
+    return -1;
+}
+
+// rl of quick_decide for temperature T, or 0 (quick path off) when T is not a
+// normal positive FP32 value.
+__device__ __forceinline__ float quick_scale(float temp) {
+    if (!(temp >= 1.17549435e-38f && temp <= 3.4e38f)) return 0.0f;
+    return __fmul_rn(__frcp_rn(temp), 1.44269502162933349609375f);
+}
+
+// The caller's uniform stream read by a warp in chunks of 32 values, the two chunks
+// after the current one loaded ahead of use: a block of 32 positions consumes at
+// most 32 values, so the values at used .. used + 63 are always in registers.
+// Loads go to clamped, always valid addresses; values past the end of the stream
+// are never used (the caller stops at cap).
+__device__ const int32_t g_no_rands[1] = {0};
+
+struct UniformRing {
+    const int32_t* rr;
+    int64_t last;       // index of the last value (0 for an empty stream, read from g_no_rands)
+    int64_t k;          // chunk index of a
+    int32_t a, b, c;    // this lane's values of chunks k, k + 1, k + 2
+    __device__ __forceinline__ int32_t load(int64_t kk, int lane) const {
+        const int64_t t = kk * 32 + lane;
+        return __ldg(rr + (t < last ? t : last));
+    }
+    __device__ __forceinline__ void init(const int32_t* rr_, int64_t cap_, int lane) {
+        rr = cap_ > 0 ? rr_ : g_no_rands;
+        last = cap_ > 0 ? cap_ - 1 : 0;
+        k = 0;
+        a = load(0, lane); b = load(1, lane); c = load(2, lane);
+    }
+    // Value at stream index u, 32k <= u < 32k + 64 (every lane of the warp calls it).
+    __device__ __forceinline__ int32_t get(int64_t u) const {
+        const int32_t va = __shfl_sync(0xffffffffu, a, (int)(u & 31));
+        const int32_t vb = __shfl_sync(0xffffffffu, b, (int)(u & 31));
+        return (u >> 5) == k ? va : vb;
+    }
+    // The stream has advanced to index used.
+    __device__ __forceinline__ void advance(int64_t used, int lane) {
+        while ((used >> 5) > k) {
+            a = b; b = c; ++k;
+            c = load(k + 2, lane);
+        }
+    }
+};
+
 // Metropolis test of reference piqmc/qmc.pyx:130-133 (ge = false) and
 // piqmc/sa.pyx:114-117 (ge = true): deterministic accept on ediff > 0 (>= 0),
 // otherwise exp((double)(ediff / temp)) > rand() / (double)RAND_MAX.
@@ -201,8 +264,8 @@ __global__ void __launch_bounds__(32) qa_sparse_reforder_kernel(
 // The same sweep with the warp sharing the work (replicas whose spins fit in
 // shared memory, maxnb 4 or 5).  The permutation is taken in blocks of 32
 // positions, lane l owning position l:
-//  * each lane loads its spin's neighbour row and couplings (the global loads of
-//    the next block are issued before the current block is resolved) and folds
+//  * each lane loads its spin's neighbour row and couplings (the permutation entry
+//    two blocks ahead, the row one block ahead of its use) and folds
 //    the current neighbour spins into signed couplings; a neighbour at an earlier
 //    position p of the same block is recorded (its term changes sign if p flips);
 //  * the accumulator is a sequential chain (FP32, one rounding per term, carried
@@ -248,18 +311,35 @@ __global__ void __launch_bounds__(32) qa_sparse_reforder_warp_kernel(
     const int32_t* rr = rands + (int64_t)r * rand_stride;
     const int64_t cap = rand_stride;
     int64_t used = 0;
+    UniformRing ring;
+    ring.init(rr, cap, lane);
+    const float rl = quick_scale(temp);
     bool bad = false, dead = false;
     const int nblk = (nperm + 31) / 32;
     const int64_t total = (int64_t)nsched * mcsteps * P * nblk;   // blocks in the whole run
 
-    // this lane's inputs of block number b (global loads only)
-    auto load_in = [&](int64_t b, RefBlockIn<FP64, MAXNB>& in) {
+    // This lane's inputs arrive in two steps, so that no load waits on another inside
+    // a block: its permutation entry two blocks ahead, its neighbour row one block ahead
+    // (from the entry loaded a block earlier).
+    // The block whose entry is loaded next is tracked by counters (permutation, slice,
+    // block within the permutation) stepped once per block: no 64-bit division.  The
+    // load is unconditional from a valid address (entry 0 stands in past the end).
+    int64_t q_sweep = 0;
+    int q_k = 0, q_blk = 0;
+    const int64_t nsweeps = (int64_t)nsched * mcsteps;
+    auto perm_next = [&](bool& has) -> int {
+        const int t = q_blk * 32 + lane;
+        has = q_sweep < nsweeps && t < nperm;
+        const int v = __ldg(pr + (has ? q_sweep * nperm + t : 0));
+        if (++q_blk == nblk) {
+            q_blk = 0;
+            if (++q_k == P) { q_k = 0; ++q_sweep; }
+        }
+        return v;
+    };
+    auto rows_of = [&](bool has, int i, RefBlockIn<FP64, MAXNB>& in) {
         in.i = -1;
-        if (b >= total) return;
-        const int64_t sweep = b / ((int64_t)P * nblk);
-        const int t = (int)(b % nblk) * 32 + lane;
-        if (t >= nperm) return;
-        int i = __ldg(pr + sweep * nperm + t);
+        if (!has) return;
         if ((unsigned)i >= (unsigned)n) { bad = true; i = 0; }
         in.i = i;
 #pragma unroll
@@ -269,9 +349,15 @@ __global__ void __launch_bounds__(32) qa_sparse_reforder_warp_kernel(
         }
     };
     RefBlockIn<FP64, MAXNB> cur, nxt;
-    load_in(0, cur);
+    bool p_has = false;
+    int p_next = 0;
+    if (total > 0) {
+        p_next = perm_next(p_has);   // block 0
+        rows_of(p_has, p_next, cur);
+        p_next = perm_next(p_has);   // block 1
+    }
     int64_t b = 0;
-    for (int g = 0; g < nsched && !dead; ++g) {
+    for (int g = 0; g < nsched && total > 0 && !dead; ++g) {
         const float jpf = jperp[g];
         for (int step = 0; step < mcsteps && !dead; ++step) {
             for (int k = 0; k < P && !dead; ++k) {
@@ -279,7 +365,8 @@ __global__ void __launch_bounds__(32) qa_sparse_reforder_warp_kernel(
                 if (flags & PQ_FIX_Q1) { tl = k == 0 ? P - 1 : k - 1; tr = k == P - 1 ? 0 : k + 1; }
                 float ediff = 0.0f;       // Q2 as shipped: reset once per slice (piqmc/qmc.pyx:134-135)
                 for (int blk = 0; blk < nblk && !dead; ++blk, ++b) {
-                    load_in(b + 1, nxt);
+                    rows_of(p_has, p_next, nxt);     // block b + 1
+                    p_next = perm_next(p_has);       // block b + 2
                     const int nb = min(32, nperm - blk * 32);
                     const int i = cur.i;
                     if (lane < nb) pos_of[i] = (uint8_t)lane;
@@ -319,7 +406,6 @@ __global__ void __launch_bounds__(32) qa_sparse_reforder_warp_kernel(
                         rec[2 * lane] = make_float4(x[0], x[1], x[2], x[3]);
                         rec[2 * lane + 1] = make_float4(x[4], x[5], x[6], x[7]);
                     }
-                    const int32_t rwin = used + lane < cap ? __ldg(rr + used + lane) : 0;
                     __syncwarp();
                     uint32_t flipmask = 0;
                     int c = 0;               // uniforms consumed in this block so far
@@ -361,7 +447,7 @@ __global__ void __launch_bounds__(32) qa_sparse_reforder_warp_kernel(
                             c += ediff > 0.0f ? 0 : 1;
                         }
                         // decisions of positions [start, l), one per lane
-                        const int32_t rv = __shfl_sync(0xffffffffu, rwin, my_c & 31);
+                        const int32_t rv = ring.get(used + my_c);
                         bool flip = false, out = false;
                         if (lane >= start && lane < l) {
                             if (my_e > 0.0f) {
@@ -369,13 +455,18 @@ __global__ void __launch_bounds__(32) qa_sparse_reforder_warp_kernel(
                             } else if (used + my_c >= cap) {
                                 out = true;
                             } else {
-                                const float xf = __fdiv_rn(my_e, temp);
-                                const int quick = fp32_decide(xf, rv);
-                                if (quick >= 0) {
-                                    flip = quick != 0;
+                                const int fast = rl != 0.0f ? quick_decide(my_e, rl, rv) : -1;
+                                if (fast >= 0) {
+                                    flip = fast != 0;
                                 } else {
-                                    const double q = (double)rv / 2147483647.0;   // glibc RAND_MAX
-                                    flip = patched_exp(xf, q, ep) > q;
+                                    const float xf = __fdiv_rn(my_e, temp);
+                                    const int quick = fp32_decide(xf, rv);
+                                    if (quick >= 0) {
+                                        flip = quick != 0;
+                                    } else {
+                                        const double q = (double)rv / 2147483647.0;   // glibc RAND_MAX
+                                        flip = patched_exp(xf, q, ep) > q;
+                                    }
                                 }
                             }
                         }
@@ -387,6 +478,7 @@ __global__ void __launch_bounds__(32) qa_sparse_reforder_warp_kernel(
                         flipmask |= __ballot_sync(0xffffffffu, flip);
                     }
                     used += c;
+                    ring.advance(used, lane);
                     if (lane < nb) {
                         if ((flipmask >> lane) & 1u) s[(int64_t)i * P + k] = (int8_t)-s[(int64_t)i * P + k];
                         pos_of[i] = 0xFF;
@@ -607,33 +699,57 @@ __global__ void __launch_bounds__(32) sa_sparse_reforder_warp_kernel(
     const int32_t* rr = rands + (int64_t)r * rand_stride;
     const int64_t cap = rand_stride;
     int64_t used = 0;
+    UniformRing ring;
+    ring.init(rr, cap, lane);
     bool bad = false, dead = false;
     const int nblk = (n + 31) / 32;
     const int64_t total = (int64_t)nsched * mcsteps * nblk;
     struct In { int i; int j[MAXNB]; float v[MAXNB]; };
-    auto load_in = [&](int64_t b, In& in) {
+    // permutation entry two blocks ahead, neighbour row one block ahead (see the QA kernel)
+    int64_t q_sweep = 0;
+    int q_blk = 0;
+    const int64_t nsweeps = (int64_t)nsched * mcsteps;
+    auto perm_next = [&](bool& has) -> int {
+        const int t = q_blk * 32 + lane;
+        has = q_sweep < nsweeps && t < n;
+        const int v = __ldg(pr + (has ? q_sweep * n + t : 0));
+        if (++q_blk == nblk) { q_blk = 0; ++q_sweep; }
+        return v;
+    };
+    auto rows_of = [&](bool has, int i, In& in) {
         in.i = -1;
-        if (b >= total) return;
-        const int64_t sweep = b / nblk;
-        const int t = (int)(b % nblk) * 32 + lane;
-        if (t >= n) return;
-        int i = __ldg(pr + sweep * n + t);
+        if (!has) return;
         if ((unsigned)i >= (unsigned)n) { bad = true; i = 0; }
         in.i = i;
+        if (maxnb <= 0) {
+#pragma unroll
+            for (int m = 0; m < MAXNB; ++m) { in.j[m] = i; in.v[m] = 0.0f; }
+            return;
+        }
+        // entries m >= maxnb repeat the last one: the fold never reads them
 #pragma unroll
         for (int m = 0; m < MAXNB; ++m) {
-            in.j[m] = m < maxnb ? __ldg(nb_idx + (int64_t)i * maxnb + m) : i;
-            in.v[m] = m < maxnb ? __ldg(nb_j + (int64_t)i * maxnb + m) : 0.0f;
+            const int mm = m < maxnb ? m : maxnb - 1;
+            in.j[m] = __ldg(nb_idx + (int64_t)i * maxnb + mm);
+            in.v[m] = __ldg(nb_j + (int64_t)i * maxnb + mm);
         }
     };
     In cur, nxt;
-    load_in(0, cur);
+    bool p_has = false;
+    int p_next = 0;
+    if (total > 0) {
+        p_next = perm_next(p_has);   // block 0
+        rows_of(p_has, p_next, cur);
+        p_next = perm_next(p_has);   // block 1
+    }
     int64_t b = 0;
-    for (int g = 0; g < nsched && !dead; ++g) {
+    for (int g = 0; g < nsched && total > 0 && !dead; ++g) {
         const float temp = temps[g];
+        const float rl = quick_scale(temp);
         for (int step = 0; step < mcsteps && !dead; ++step) {
             for (int blk = 0; blk < nblk && !dead; ++blk, ++b) {
-                load_in(b + 1, nxt);
+                rows_of(p_has, p_next, nxt);     // block b + 1
+                p_next = perm_next(p_has);       // block b + 2
                 const int nb = min(32, n - blk * 32);
                 const int i = cur.i;
                 if (lane < nb) pos_of[i] = (uint8_t)lane;
@@ -660,7 +776,6 @@ __global__ void __launch_bounds__(32) sa_sparse_reforder_warp_kernel(
                         x[m] = v;
                     }
                 }
-                const int32_t rwin = used + lane < cap ? __ldg(rr + used + lane) : 0;
                 uint32_t flipmask = 0;
                 int c = 0;
                 int start = 0;
@@ -682,7 +797,7 @@ __global__ void __launch_bounds__(32) sa_sparse_reforder_warp_kernel(
                     const bool consume = mine && !(ediff >= 0.0f);
                     const uint32_t cons = __ballot_sync(0xffffffffu, consume);
                     const int my_c = c + __popc(cons & ((1u << lane) - 1u));
-                    const int32_t rv = __shfl_sync(0xffffffffu, rwin, my_c & 31);
+                    const int32_t rv = ring.get(used + my_c);
                     bool flip = false, out = false;
                     if (mine) {
                         if (!consume) {
@@ -690,13 +805,18 @@ __global__ void __launch_bounds__(32) sa_sparse_reforder_warp_kernel(
                         } else if (used + my_c >= cap) {
                             out = true;
                         } else {
-                            const float xf = __fdiv_rn(ediff, temp);
-                            const int quick = fp32_decide(xf, rv);
-                            if (quick >= 0) {
-                                flip = quick != 0;
+                            const int fast = rl != 0.0f ? quick_decide(ediff, rl, rv) : -1;
+                            if (fast >= 0) {
+                                flip = fast != 0;
                             } else {
-                                const double q = (double)rv / 2147483647.0;   // glibc RAND_MAX
-                                flip = patched_exp(xf, q, ep) > q;
+                                const float xf = __fdiv_rn(ediff, temp);
+                                const int quick = fp32_decide(xf, rv);
+                                if (quick >= 0) {
+                                    flip = quick != 0;
+                                } else {
+                                    const double q = (double)rv / 2147483647.0;   // glibc RAND_MAX
+                                    flip = patched_exp(xf, q, ep) > q;
+                                }
                             }
                         }
                     }
@@ -710,6 +830,7 @@ __global__ void __launch_bounds__(32) sa_sparse_reforder_warp_kernel(
                     start = end;
                 }
                 used += c;
+                ring.advance(used, lane);
                 if (lane < nb) {
                     if ((flipmask >> lane) & 1u) s[i] = (int8_t)-s[i];
                     pos_of[i] = 0xFF;
