@@ -50,7 +50,17 @@ struct ExpPatch {
     int* close_cnt;
 };
 
-__device__ __forceinline__ double patched_exp(float xf, double q, const ExpPatch& ep, bool record = true) {
+// Records a close call that had no override: x and the device exp value used.
+__device__ __forceinline__ void record_close(const ExpPatch& ep, float xf, double e) {
+    if (!ep.close_cnt) return;
+    const int slot = atomicAdd(ep.close_cnt, 1);
+    if (slot < ep.close_cap) { ep.close_x[slot] = __float_as_uint(xf); ep.close_y[slot] = e; }
+}
+
+// exp((double)xf) for the test against q, with the host-libm override for x when the
+// two are close.  A close call without an override is recorded -- or, with deferred,
+// only flagged there, for a caller that records it once the decision is known to stand.
+__device__ __forceinline__ double patched_exp(float xf, double q, const ExpPatch& ep, bool* deferred = nullptr) {
     double e = exp((double)xf);
     const double d = fabs(e - q);
     const bool close = d <= 1e-15 * fmax(e, q) || (q == 0.0 && e < 1e-300);
@@ -62,10 +72,8 @@ __device__ __forceinline__ double patched_exp(float xf, double q, const ExpPatch
         if (ep.ov_x[mid] < xb) lo = mid + 1; else hi = mid;
     }
     if (lo < ep.ov_n && ep.ov_x[lo] == xb) return ep.ov_y[lo];
-    if (ep.close_cnt && record) {
-        const int slot = atomicAdd(ep.close_cnt, 1);
-        if (slot < ep.close_cap) { ep.close_x[slot] = xb; ep.close_y[slot] = e; }
-    }
+    if (deferred) *deferred = true;
+    else record_close(ep, xf, e);
     return e;
 }
 
@@ -269,15 +277,18 @@ __global__ void __launch_bounds__(32) qa_sparse_reforder_kernel(
 //    the current neighbour spins into signed couplings; a neighbour at an earlier
 //    position p of the same block is recorded (its term changes sign if p flips);
 //  * the accumulator is a sequential chain (FP32, one rounding per term, carried
-//    across spins as the reference carries it).  A round takes the open positions
-//    up to (not including) the first one with an in-block neighbour whose decision
-//    is still open; those positions first negate the terms of neighbours that
-//    flipped earlier in the block, then all lanes walk them in order computing the
-//    chain -- the sum of position l and the number of uniforms consumed before it
-//    are kept by lane l;
+//    across spins as the reference carries it).  A round takes every open position:
+//    they first negate the terms of neighbours whose flips stand, then all lanes walk
+//    them in order computing the chain, taking in-block neighbours that are still
+//    undecided as not flipping -- the sum of position l and the number of uniforms
+//    consumed before it are kept by lane l;
 //  * the walked positions then decide in parallel, each lane with its own uniform
-//    (the window of the next 32 values of the stream) and exactly ref_accept's
-//    arithmetic, and the next round starts.
+//    (from the next values of the stream) and exactly ref_accept's arithmetic.  The
+//    decisions stand up to the first position with an in-block neighbour that
+//    flipped in this round; from that position the next round walks again, from
+//    the chain value and the uniform count before it (flips are rare at annealing
+//    temperatures, so most blocks take one round).  Close calls are recorded only
+//    for decisions that stand.
 // Flips are written back at the end of the block.  Same results, same uniforms
 // consumed and the same close calls (recorded by the deciding lane) as
 // qa_sparse_reforder_kernel.
@@ -407,29 +418,32 @@ __global__ void __launch_bounds__(32) qa_sparse_reforder_warp_kernel(
                         rec[2 * lane + 1] = make_float4(x[4], x[5], x[6], x[7]);
                     }
                     __syncwarp();
-                    uint32_t flipmask = 0;
+                    uint32_t flipmask = 0;   // flips of this block that stand
+                    uint32_t applied = 0;    // of those, the ones already folded into this lane's terms
                     int c = 0;               // uniforms consumed in this block so far
                     float my_e = 0.0f;       // this lane's position: its sum ...
                     int my_c = 0;            // ... and the uniforms consumed before it
                     int l = 0;
                     while (l < nb) {
                         const int start = l;
-                        const uint32_t open = ~((1u << start) - 1u);   // positions >= start are undecided
-                        // the walk stops before the first later position with an undecided in-block neighbour
-                        const uint32_t blocked = __ballot_sync(0xffffffffu, lane > start && lane < nb && (dep & open));
-                        const int end = blocked ? __ffs(blocked) - 1 : nb;
-                        // the walked positions apply the flips decided so far (all their neighbours' are)
-                        if (lane >= start && lane < end && (dep & flipmask)) {
+                        // open positions fold in the flips that stand (a flipped neighbour's term
+                        // is the exact negation)
+                        if (lane >= start && lane < nb) {
+                            const uint32_t nf = dep & flipmask & ~applied;
+                            if (nf) {
 #pragma unroll
-                            for (int m = 0; m < MAXNB; ++m)
-                                if (pp[m] != 0xFF && ((flipmask >> pp[m]) & 1u)) x[m] = -x[m];
-                            rec[2 * lane] = make_float4(x[0], x[1], x[2], x[3]);
-                            rec[2 * lane + 1] = make_float4(x[4], x[5], x[6], x[7]);
+                                for (int m = 0; m < MAXNB; ++m)
+                                    if (pp[m] != 0xFF && ((nf >> pp[m]) & 1u)) x[m] = -x[m];
+                                rec[2 * lane] = make_float4(x[0], x[1], x[2], x[3]);
+                                rec[2 * lane + 1] = make_float4(x[4], x[5], x[6], x[7]);
+                                applied |= nf;
+                            }
                         }
                         __syncwarp();
-                        // records of position l + 1 are read while position l's sum is chained
+                        // walk every open position, taking its undecided in-block neighbours as
+                        // not flipping; records of position l + 1 are read while l's sum is chained
                         float4 ra = rec[2 * l], rb = rec[2 * l + 1];
-                        for (; l < end; ++l) {
+                        for (; l < nb; ++l) {
                             const float4 ra_n = rec[2 * l + 2], rb_n = rec[2 * l + 3];
                             const float y[8] = {ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w};
                             ra = ra_n;
@@ -446,10 +460,11 @@ __global__ void __launch_bounds__(32) qa_sparse_reforder_warp_kernel(
                             if (lane == l) { my_e = ediff; my_c = c; }
                             c += ediff > 0.0f ? 0 : 1;
                         }
-                        // decisions of positions [start, l), one per lane
+                        // decisions of positions [start, nb), one per lane
                         const int32_t rv = ring.get(used + my_c);
-                        bool flip = false, out = false;
-                        if (lane >= start && lane < l) {
+                        bool flip = false, out = false, miss = false;
+                        float xf = 0.0f;
+                        if (lane >= start && lane < nb) {
                             if (my_e > 0.0f) {
                                 flip = true;
                             } else if (used + my_c >= cap) {
@@ -459,23 +474,34 @@ __global__ void __launch_bounds__(32) qa_sparse_reforder_warp_kernel(
                                 if (fast >= 0) {
                                     flip = fast != 0;
                                 } else {
-                                    const float xf = __fdiv_rn(my_e, temp);
+                                    xf = __fdiv_rn(my_e, temp);
                                     const int quick = fp32_decide(xf, rv);
                                     if (quick >= 0) {
                                         flip = quick != 0;
                                     } else {
                                         const double q = (double)rv / 2147483647.0;   // glibc RAND_MAX
-                                        flip = patched_exp(xf, q, ep) > q;
+                                        flip = patched_exp(xf, q, ep, &miss) > q;
                                     }
                                 }
                             }
                         }
-                        if (__any_sync(0xffffffffu, out)) {
+                        // the walk stands up to the first position whose in-block neighbour
+                        // flipped in this round; from there it is taken again
+                        const uint32_t fl = __ballot_sync(0xffffffffu, flip);
+                        const uint32_t wrong = __ballot_sync(0xffffffffu, lane > start && lane < nb && (dep & fl));
+                        const int p = wrong ? __ffs(wrong) - 1 : nb;
+                        if (__any_sync(0xffffffffu, out && lane < p)) {
                             if (lane == 0) pq_set_status(status, PQ_ERR_RAND_EXHAUSTED);
                             dead = true;
                             break;
                         }
-                        flipmask |= __ballot_sync(0xffffffffu, flip);
+                        if (miss && lane < p) record_close(ep, xf, exp((double)xf));
+                        flipmask |= fl & (p >= 32 ? 0xffffffffu : ((1u << p) - 1u));
+                        if (p < nb) {
+                            ediff = __shfl_sync(0xffffffffu, my_e, p - 1);   // the chain before position p
+                            c = __shfl_sync(0xffffffffu, my_c, p);           // the uniforms consumed before p
+                            l = p;
+                        }
                     }
                     used += c;
                     ring.advance(used, lane);
@@ -673,12 +699,14 @@ __global__ void sa_bipartite_reforder_kernel(int8_t* __restrict__ spins, const d
 // sa.Anneal with the warp sharing the work (spins in shared memory, maxnb <= 8).
 // The energy difference is reset for every spin (piqmc/sa.pyx:119), so the sums
 // of a block's 32 positions are independent except through neighbours flipped
-// earlier in the same block.  Each pass takes the longest run of open positions
-// whose in-block neighbours are all decided: their sums are computed in parallel
-// (each lane its own FP32 chain in the reference's term order), the uniforms they
-// consume are numbered by a ballot prefix count (a position consumes one when
-// ediff < 0, :114-117), and they decide in parallel with ref_accept's arithmetic.
-// Same results, uniforms and close calls as sa_sparse_reforder_kernel.
+// earlier in the same block.  Each pass takes every open position, with in-block
+// neighbours still undecided taken as not flipping: their sums are computed in
+// parallel (each lane its own FP32 chain in the reference's term order), the
+// uniforms they consume are numbered by a ballot prefix count (a position consumes
+// one when ediff < 0, :114-117), and they decide in parallel with ref_accept's
+// arithmetic.  The decisions stand up to the first position with an in-block
+// neighbour that flipped in the pass, where the next pass starts.  Same results,
+// uniforms and close calls as sa_sparse_reforder_kernel.
 template <bool FP64>
 __global__ void __launch_bounds__(32) sa_sparse_reforder_warp_kernel(
     int8_t* __restrict__ spins, const int32_t* __restrict__ nb_idx, const float* __restrict__ nb_j, int n, int maxnb,
@@ -776,14 +804,13 @@ __global__ void __launch_bounds__(32) sa_sparse_reforder_warp_kernel(
                         x[m] = v;
                     }
                 }
-                uint32_t flipmask = 0;
+                uint32_t flipmask = 0;   // flips of this block that stand
                 int c = 0;
                 int start = 0;
                 while (start < nb) {
-                    const bool ready = (dep & ~((1u << start) - 1u)) == 0;
-                    const uint32_t wait = __ballot_sync(0xffffffffu, lane >= start && lane < nb && !ready);
-                    const int end = wait ? __ffs(wait) - 1 : nb;
-                    const bool mine = lane >= start && lane < end;
+                    // every open position sums its terms; in-block neighbours still undecided
+                    // are taken as not flipping (checked below)
+                    const bool mine = lane >= start && lane < nb;
                     float ediff = 0.0f;
                     if (mine) {
 #pragma unroll
@@ -798,7 +825,8 @@ __global__ void __launch_bounds__(32) sa_sparse_reforder_warp_kernel(
                     const uint32_t cons = __ballot_sync(0xffffffffu, consume);
                     const int my_c = c + __popc(cons & ((1u << lane) - 1u));
                     const int32_t rv = ring.get(used + my_c);
-                    bool flip = false, out = false;
+                    bool flip = false, out = false, miss = false;
+                    float xf = 0.0f;
                     if (mine) {
                         if (!consume) {
                             flip = true;
@@ -809,25 +837,32 @@ __global__ void __launch_bounds__(32) sa_sparse_reforder_warp_kernel(
                             if (fast >= 0) {
                                 flip = fast != 0;
                             } else {
-                                const float xf = __fdiv_rn(ediff, temp);
+                                xf = __fdiv_rn(ediff, temp);
                                 const int quick = fp32_decide(xf, rv);
                                 if (quick >= 0) {
                                     flip = quick != 0;
                                 } else {
                                     const double q = (double)rv / 2147483647.0;   // glibc RAND_MAX
-                                    flip = patched_exp(xf, q, ep) > q;
+                                    flip = patched_exp(xf, q, ep, &miss) > q;
                                 }
                             }
                         }
                     }
-                    if (__any_sync(0xffffffffu, out)) {
+                    // decisions stand up to the first position with an in-block neighbour that
+                    // flipped in this pass; the next pass starts there
+                    const uint32_t fl = __ballot_sync(0xffffffffu, flip);
+                    const uint32_t wrong = __ballot_sync(0xffffffffu, lane > start && lane < nb && (dep & fl));
+                    const int p = wrong ? __ffs(wrong) - 1 : nb;
+                    const uint32_t keep = p >= 32 ? 0xffffffffu : ((1u << p) - 1u);
+                    if (__any_sync(0xffffffffu, out && lane < p)) {
                         if (lane == 0) pq_set_status(status, PQ_ERR_RAND_EXHAUSTED);
                         dead = true;
                         break;
                     }
-                    flipmask |= __ballot_sync(0xffffffffu, flip);
-                    c += __popc(cons);
-                    start = end;
+                    if (miss && lane < p) record_close(ep, xf, exp((double)xf));
+                    flipmask |= fl & keep;
+                    c += __popc(cons & keep);
+                    start = p;
                 }
                 used += c;
                 ring.advance(used, lane);
