@@ -698,6 +698,39 @@ def reforder_workload(args, torch):
             raise RuntimeError("reference-order SA bench: status %d" % int(status.item()))
         times.append(e0.elapsed_time(e1) * 1e-3)
     out["sa_replicas_1"] = {"value": float(n) * steps / min(times), "unit": "updates/s", "ms": 1e3 * min(times)}
+    # QuantumAnneal_dense's reference-order sweep on the dense workload's instance (N = 512, P = 32)
+    Jd = dense_instance()
+    nd, Pd = Jd.shape[0], 32
+    d_Jd = torch.from_numpy(Jd).cuda()
+    for R, dsteps in ((1, 4), (256, 2)):
+        dsched = schedule(1000)[:dsteps]
+        jpd = torch.from_numpy(reforder.jperp_schedule(dsched, Pd, TEMP)).cuda()
+        perms = torch.from_numpy(np.stack([np.stack([g.permutation(nd) for _ in range(dsteps)]) for _ in range(R)])
+                                 .astype(np.int32)).cuda()
+        cap = nd * Pd * dsteps
+        rands = torch.from_numpy(g.integers(0, 2 ** 31 - 1, size=(R, cap), dtype=np.int64).astype(np.int32)).cuda()
+        s0 = torch.from_numpy(np.repeat(np.where(g.random((R, nd)) < 0.5, -1, 1).astype(np.int8)[:, :, None], Pd,
+                                        axis=2)).cuda()
+        used = torch.zeros(R, dtype=torch.int64, device="cuda")
+        status = torch.zeros(1, dtype=torch.int32, device="cuda")
+        times = []
+        for it in range(2):
+            sp = s0.clone()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            rc = lib.pq_qa_dense_reforder(_device.ptr(sp), _device.ptr(d_Jd), nd, Pd, R, _device.ptr(jpd), dsteps, 1,
+                                          float(np.float32(TEMP)), _device.ptr(perms), _device.ptr(rands), cap,
+                                          _device.ptr(used), 0, _device.ptr(status), _device.stream_handle())
+            e1.record()
+            torch.cuda.synchronize()
+            _native.check(rc, "pq_qa_dense_reforder")
+            if int(status.item()) or int(used.min().item()) < 0:
+                raise RuntimeError("reference-order dense bench: status %d" % int(status.item()))
+            times.append(e0.elapsed_time(e1) * 1e-3)
+        out["dense_replicas_%d" % R] = {"value": float(nd) * Pd * dsteps * R / min(times), "unit": "updates/s",
+                                        "ms": 1e3 * min(times),
+                                        "workload": "dense N=512, P=32, %d field steps, reference order" % dsteps}
     return out
 
 

@@ -884,6 +884,232 @@ __global__ void __launch_bounds__(32) sa_sparse_reforder_warp_kernel(
     for (int t = lane; t < n; t += 32) gs[t] = s[t];
 }
 
+// Dense reference-order sweeps (QuantumAnneal_dense, piqmc/qmc.pyx:181-242, and
+// sa.Anneal_dense, piqmc/sa.pyx:126-187) with one warp per replica.  For each
+// position of the permutation the lanes compute the n terms of the reference's sum
+// (and QA's two Trotter terms) in parallel -- every term -2 s_i (J_ij s_j) is exactly
+// +-2 J_ij in FP64 -- into shared memory, and the warp then walks the accumulator
+// chain through them in the reference's order.  When every term of the update is an
+// FP32 value, (float)((double)e + t) equals the FP32 sum e + t (double rounding
+// through 53 >= 2*24 + 2 bits is innocuous), so the chain is FP32 adds; otherwise it
+// is the reference's FP64 add and rounding, term by term.  The row of J the next
+// position needs -- J[i][j] for j >= i and J[j][i] below the diagonal, the upper
+// triangle the reference reads (piqmc/qmc.pyx:206-219) -- is copied into shared
+// memory by cp.async while the current position is resolved, and the uniforms come
+// from the register ring.  Same spins, uniforms and close calls (recorded by lane 0)
+// as qa_dense_reforder_kernel and sa_dense_reforder_kernel.
+__device__ __forceinline__ void cp_async8(void* smem_dst, const void* gsrc) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+__host__ __device__ inline size_t dense_warp_align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+// Shared memory of the dense warp kernels: spins [n][P], two J rows, FP64 and FP32 terms
+// (FP32 padded for the read-ahead), one flag per row.
+__host__ __device__ inline size_t dense_warp_smem(int n, int P) {
+    return dense_warp_align16((size_t)n * P) + (size_t)16 * n + dense_warp_align16((size_t)8 * (n + 2)) +
+           dense_warp_align16((size_t)4 * (n + 8)) + dense_warp_align16((size_t)n);
+}
+
+// The FP32 value of an FP64 value that is zero or a normal FP32 number, by its bits.
+__device__ __forceinline__ float f32_of_exact(double d) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const uint32_t hi = (uint32_t)(b >> 32);
+    const uint32_t e = (hi >> 20) & 0x7FFu;
+    const uint32_t sign = hi & 0x80000000u;
+    const uint32_t man = (uint32_t)(b >> 29) & 0x7FFFFFu;
+    return __uint_as_float(e == 0 ? sign : (sign | ((e - 896u) << 23) | man));
+}
+
+// v is zero or a normal FP32 number whose double 2v is finite in FP32: then every
+// term +-2v is an FP32 value and f32_of_exact(v) gives v.
+__device__ __forceinline__ bool fp32_term_exact(double v) {
+    const double a = fabs(v);
+    return v == 0.0 || (a >= 1.1754943508222875e-38 && a <= 1.7014117331926443e38 && (double)__double2float_rn(v) == v);
+}
+
+template <bool QA>
+__global__ void __launch_bounds__(32) dense_reforder_warp_kernel(
+    int8_t* __restrict__ spins, const double* __restrict__ J, int n, int P, int R,
+    const float* __restrict__ per_step,   // QA: J-perp of each field step; SA: its temperature
+    int nsched, int mcsteps, float temp_qa, const int32_t* __restrict__ perms, const int32_t* __restrict__ rands,
+    int64_t rand_stride, int64_t* __restrict__ rand_used, int flags, ExpPatch ep, int32_t* status) {
+    extern __shared__ __align__(16) int8_t sh[];
+    const int r = blockIdx.x;
+    if (r >= R) return;
+    const int lane = threadIdx.x;
+    const int Pq = QA ? P : 1;
+    int8_t* s = sh;                                                                                   // [n][P]
+    double* row = reinterpret_cast<double*>(sh + dense_warp_align16((size_t)n * Pq));                 // [2][n]
+    double* t64 = row + (size_t)2 * n;                                                               // [n + 2]
+    float* t32 = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(t64) +
+                                          dense_warp_align16((size_t)8 * (n + 2)));                  // [n + 8]
+    uint8_t* row_f32 = reinterpret_cast<uint8_t*>(t32) + dense_warp_align16((size_t)4 * (n + 8));   // [n]
+    int8_t* gs = spins + (int64_t)r * n * Pq;
+    for (int64_t t = lane; t < (int64_t)n * Pq; t += 32) s[t] = gs[t];
+    // which rows give FP32 terms only (the upper triangle and diagonal the reference reads)
+    for (int i = 0; i < n; ++i) {
+        bool ok = true;
+        for (int j = lane; j < n; j += 32) ok = ok && fp32_term_exact(j >= i ? J[(int64_t)i * n + j] : J[(int64_t)j * n + i]);
+        ok = __all_sync(0xffffffffu, ok);
+        if (lane == 0) row_f32[i] = ok ? 1 : 0;
+    }
+    __syncwarp();
+    const int32_t* pr = perms + (int64_t)r * nsched * mcsteps * n;
+    const int64_t cap = rand_stride;
+    UniformRing ring;
+    ring.init(rands + (int64_t)r * rand_stride, cap, lane);
+    int64_t used = 0;
+    bool bad = false, dead = false;
+    const int64_t nsweeps = (int64_t)nsched * mcsteps;
+    // permutation entry of the position loaded next (counters stepped, no division)
+    int64_t q_sweep = 0;
+    int q_k = 0, q_t = 0;
+    auto next_entry = [&](bool& has) -> int {
+        has = q_sweep < nsweeps;
+        const int v = __ldg(pr + (has ? q_sweep * n + q_t : 0));
+        if (++q_t == n) {
+            q_t = 0;
+            if (++q_k == Pq) { q_k = 0; ++q_sweep; }
+        }
+        return v;
+    };
+    auto prefetch_row = [&](int i, int b) {
+        if ((unsigned)i >= (unsigned)n) i = 0;   // a bad entry stops the run when it is reached
+        double* dst = row + (size_t)b * n;
+        for (int j = lane; j < n; j += 32)
+            cp_async8(dst + j, j >= i ? J + (int64_t)i * n + j : J + (int64_t)j * n + i);
+        cp_async_commit();
+    };
+    if (nsweeps > 0 && n > 0) {
+        bool h0, h1, h2;
+        int i0 = next_entry(h0);
+        int i1 = next_entry(h1);
+        prefetch_row(i0, 0);
+        int buf = 0;
+        for (int g = 0; g < nsched && !dead; ++g) {
+            const float temp = QA ? temp_qa : per_step[g];
+            const double jp = QA ? (double)per_step[g] : 0.0;
+            const bool jp_ok = !QA || fabs(jp) <= 1.7014117331926443e38;   // +-2 J-perp is an FP32 value
+            const float rl = quick_scale(temp);
+            for (int step = 0; step < mcsteps && !dead; ++step) {
+                for (int k = 0; k < Pq && !dead; ++k) {
+                    int tl = P - 1, tr = 1;   // Q1 as shipped (piqmc/qmc.pyx:233-236)
+                    if (QA && (flags & PQ_FIX_Q1)) { tl = k == 0 ? P - 1 : k - 1; tr = k == P - 1 ? 0 : k + 1; }
+                    float ediff = 0.0f;       // QA, Q2 as shipped: reset once per slice
+                    for (int t = 0; t < n && !dead; ++t) {
+                        const int i = i0;
+                        if (h1) prefetch_row(i1, buf ^ 1);
+                        else cp_async_commit();
+                        const int i2 = next_entry(h2);
+                        cp_async_wait<1>();   // this position's row has landed
+                        __syncwarp();
+                        if ((unsigned)i >= (unsigned)n) {
+                            bad = dead = true;
+                            break;
+                        }
+                        // the terms, one per lane and column: FP32 when every term of the row is an
+                        // FP32 value (s_i s_j J_ij -> +-2 J_ij by sign bits and one exact multiply),
+                        // else FP64 as the reference forms them
+                        const int8_t si8 = s[(int64_t)i * Pq + k];
+                        const double* rw = row + (size_t)buf * n;
+                        const bool f32 = jp_ok && row_f32[i];
+                        if (f32) {
+                            const float m2si = si8 > 0 ? -2.0f : 2.0f;
+                            for (int j = lane; j < n; j += 32) {
+                                const float jf = f32_of_exact(rw[j]);
+                                const uint32_t sgn = j == i ? 0u : ((uint32_t)(int32_t)s[(int64_t)j * Pq + k] & 0x80000000u);
+                                t32[j] = __fmul_rn(__uint_as_float(__float_as_uint(m2si) ^ sgn), jf);
+                            }
+                            if (QA && lane == 0) {
+                                const float jpf = (float)jp;
+                                t32[n] = __fmul_rn(m2si, s[(int64_t)i * Pq + tl] > 0 ? jpf : -jpf);
+                                t32[n + 1] = __fmul_rn(m2si, s[(int64_t)i * Pq + tr] > 0 ? jpf : -jpf);
+                            }
+                        } else {
+                            const double m2si = -2.0 * (double)si8;
+                            for (int j = lane; j < n; j += 32) {
+                                const double jv = rw[j];
+                                t64[j] = j == i ? m2si * jv : m2si * (jv * (double)s[(int64_t)j * Pq + k]);
+                            }
+                            if (QA && lane == 0) {
+                                t64[n] = m2si * (jp * (double)s[(int64_t)i * Pq + tl]);
+                                t64[n + 1] = m2si * (jp * (double)s[(int64_t)i * Pq + tr]);
+                            }
+                        }
+                        __syncwarp();
+                        // the chain, in the reference's order (every lane, same values; the next
+                        // values are read while the current ones are added)
+                        if (!QA || (flags & PQ_FIX_Q2)) ediff = 0.0f;
+                        const int nt = QA ? n + 2 : n;
+                        if (f32) {
+                            const float4* tv = reinterpret_cast<const float4*>(t32);
+                            const int nq = nt >> 2;
+                            float4 v = tv[0];
+                            for (int q = 0; q < nq; ++q) {
+                                const float4 vn = tv[q + 1];
+                                ediff = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(ediff, v.x), v.y), v.z), v.w);
+                                v = vn;
+                            }
+                            for (int j = nq * 4; j < nt; ++j) ediff = __fadd_rn(ediff, t32[j]);
+                        } else {
+                            double v = t64[0];
+                            for (int j = 0; j < nt; ++j) {
+                                const double vn = t64[j + 1 < nt ? j + 1 : j];
+                                ediff = acc(ediff, v);
+                                v = vn;
+                            }
+                        }
+                        // Metropolis test (ref_accept's arithmetic; one uniform when ediff <= 0)
+                        bool flip = false;
+                        if (ediff > 0.0f) {
+                            flip = true;
+                        } else if (used >= cap) {
+                            if (lane == 0) pq_set_status(status, PQ_ERR_RAND_EXHAUSTED);
+                            dead = true;
+                            break;
+                        } else {
+                            const int32_t rv = ring.get(used);
+                            ++used;
+                            ring.advance(used, lane);
+                            const int fast = rl != 0.0f ? quick_decide(ediff, rl, rv) : -1;
+                            if (fast >= 0) {
+                                flip = fast != 0;
+                            } else {
+                                const float xf = __fdiv_rn(ediff, temp);
+                                const int quick = fp32_decide(xf, rv);
+                                if (quick >= 0) {
+                                    flip = quick != 0;
+                                } else {
+                                    const double q = (double)rv / 2147483647.0;   // glibc RAND_MAX
+                                    bool miss = false;
+                                    flip = patched_exp(xf, q, ep, &miss) > q;
+                                    if (miss && lane == 0) record_close(ep, xf, exp((double)xf));
+                                }
+                            }
+                        }
+                        if (flip && lane == 0) s[(int64_t)i * Pq + k] = (int8_t)-s[(int64_t)i * Pq + k];
+                        __syncwarp();
+                        i0 = i1; h0 = h1;
+                        i1 = i2; h1 = h2;
+                        buf ^= 1;
+                    }
+                }
+            }
+        }
+        (void)h0;
+    }
+    cp_async_wait<0>();
+    __syncwarp();
+    if (bad && lane == 0) pq_set_status(status, PQ_ERR_BAD_INDEX);
+    if (lane == 0) rand_used[r] = dead ? -1 : used;
+    for (int64_t t = lane; t < (int64_t)n * Pq; t += 32) gs[t] = s[t];
+}
+
 __global__ void exp_probe_kernel(const float* __restrict__ x, double* __restrict__ y, int64_t n) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) y[i] = exp((double)x[i]);
@@ -1034,6 +1260,14 @@ int pq_qa_dense_reforder_ex(int8_t* spins, const double* J, int n, int P, int R,
     if (P < 2 || !spins || !J || !rand_used) return PQ_ERR_INVALID_ARG;
     if (R == 0) return PQ_OK;
     ExpPatch ep = make_patch(ov_x, ov_y, ov_n, close_x, close_y, close_cap, close_cnt);
+    const size_t wsmem = dense_warp_smem(n, P);
+    if (wsmem <= kRefSmemMax) {
+        PQ_CUDA_TRY(cudaFuncSetAttribute(dense_reforder_warp_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)wsmem));
+        dense_reforder_warp_kernel<true><<<R, 32, wsmem, (cudaStream_t)stream>>>(
+            spins, J, n, P, R, jperp, nsched, mcsteps, temp, perms, rands, rand_stride, rand_used, flags, ep, status);
+        return pq_launch_status();
+    }
     qa_dense_reforder_kernel<<<(R + kRefThreads - 1) / kRefThreads, kRefThreads, 0, (cudaStream_t)stream>>>(
         spins, J, n, P, R, jperp, nsched, mcsteps, temp, perms, rands, rand_stride, rand_used, flags,
         ep, status);
@@ -1107,6 +1341,14 @@ int pq_sa_dense_reforder_ex(int8_t* spins, const double* J, int n, int R, const 
     if (!spins || !J || !temps || !rand_used || (nsched * mcsteps > 0 && !perms)) return PQ_ERR_INVALID_ARG;
     if (R == 0) return PQ_OK;
     ExpPatch ep = make_patch(ov_x, ov_y, ov_n, close_x, close_y, close_cap, close_cnt);
+    const size_t wsmem = dense_warp_smem(n, 1);
+    if (wsmem <= kRefSmemMax) {
+        PQ_CUDA_TRY(cudaFuncSetAttribute(dense_reforder_warp_kernel<false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsmem));
+        dense_reforder_warp_kernel<false><<<R, 32, wsmem, (cudaStream_t)stream>>>(
+            spins, J, n, 1, R, temps, nsched, mcsteps, 1.0f, perms, rands, rand_stride, rand_used, 0, ep, status);
+        return pq_launch_status();
+    }
     sa_dense_reforder_kernel<<<(R + kRefThreads - 1) / kRefThreads, kRefThreads, 0, (cudaStream_t)stream>>>(
         spins, J, n, R, temps, nsched, mcsteps, perms, rands, rand_stride, rand_used, ep, status);
     return pq_launch_status();

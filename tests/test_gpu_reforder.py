@@ -205,6 +205,62 @@ def test_random_sa_cases_vs_oracle(piqmc, seed):
             assert used[r] == u
 
 
+def _dense_j(g, n, kind):
+    """Upper triangle + diagonal as the reference reads them, junk below (never read)."""
+    J = np.triu(g.normal(0, 1, (n, n)), 1) + np.diag(g.normal(0, 0.3, n))
+    if kind == "fp32":
+        J = J.astype(np.float32).astype(np.float64)
+    elif kind == "mixed":   # some rows FP32-valued: updates switch between the FP32 and FP64 chains
+        rows = g.random(n) < 0.5
+        J[rows] = J[rows].astype(np.float32).astype(np.float64)
+    return J + np.tril(g.normal(0, 5, (n, n)), -1)
+
+
+@pytest.mark.parametrize("kind", ["fp32", "fp64", "mixed"])
+@pytest.mark.parametrize("flags", [0, 1, 2, 3])
+def test_random_dense_cases_vs_oracle(piqmc, flags, kind):
+    """QuantumAnneal_dense in reference order (one warp per replica) against the oracle: every
+    Q1/Q2 flag, FP32-valued, general FP64 and mixed J, n across 32-lane chunks, hot and cold."""
+    from piqmc import reforder
+    g = np.random.default_rng(100 + flags)
+    for n, P in [(37, 5), (70, 4), (8, 2)]:
+        J = _dense_j(g, n, kind)
+        sched = np.linspace(2.0, 1e-6, 6)
+        R = 3
+        spins = np.where(g.random((R, n, P)) < 0.5, -1, 1).astype(np.int8)
+        perms = np.array([oracle.reference_perms(np.random.RandomState(r + 5), n, 12) for r in range(R)])
+        rands = g.integers(0, 2 ** 31 - 1, size=(R, n * P * 12), dtype=np.int64).astype(np.int32)
+        for T in (0.3, 5.0):
+            out, used = reforder.quantum_anneal_dense(spins, J, sched, 2, T, perms, rands, flags=flags)
+            out = out.cpu().numpy()
+            for r in range(R):
+                sp = spins[r].copy()
+                u = oracle.qa_dense(sp, J, sched, 2, T, perms[r], rands[r], flags=flags)
+                np.testing.assert_array_equal(out[r], sp)
+                assert used[r] == u
+
+
+@pytest.mark.parametrize("kind", ["fp32", "fp64"])
+def test_random_sa_dense_cases_vs_oracle(piqmc, kind):
+    """sa.Anneal_dense in reference order (one warp per replica) against the oracle."""
+    from piqmc import reforder
+    g = np.random.default_rng(7)
+    for n in (45, 96, 3):
+        J = _dense_j(g, n, kind)
+        sched = np.linspace(3.0, 0.1, 8)
+        R = 3
+        spins = np.where(g.random((R, n)) < 0.5, -1, 1).astype(np.int8)
+        perms = np.array([oracle.reference_perms(np.random.RandomState(r + 9), n, 16) for r in range(R)])
+        rands = g.integers(0, 2 ** 31 - 1, size=(R, n * 16), dtype=np.int64).astype(np.int32)
+        out, used = reforder.anneal_dense(spins, J, sched, 2, perms, rands)
+        out = out.cpu().numpy()
+        for r in range(R):
+            sp = spins[r].copy()
+            u = oracle.sa_dense(sp, J, sched, 2, perms[r], rands[r])
+            np.testing.assert_array_equal(out[r], sp)
+            assert used[r] == u
+
+
 def test_fp64_accumulator_with_huge_couplings(piqmc):
     """Couplings near FP32's range switch the sweeps to the FP64 accumulator (2J would overflow)."""
     from piqmc import reforder
