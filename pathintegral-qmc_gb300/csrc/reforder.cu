@@ -1110,6 +1110,154 @@ __global__ void __launch_bounds__(32) dense_reforder_warp_kernel(
     for (int64_t t = lane; t < (int64_t)n * Pq; t += 32) gs[t] = s[t];
 }
 
+// sa.Anneal_bipartite in reference order (piqmc/sa.pyx:411-500) with one warp per
+// replica: the left spins in order, then the right spins, each update's terms
+// ((2 s_i J s_j) + b_i s_i) + b_j s_j formed in FP64 by the lanes in parallel and the
+// chain ediff = (float)((double)ediff - t) walked in order -- as FP32 subtractions
+// when every term of the update is an FP32 value (the same value, see the dense
+// kernel), else in FP64 term by term.  The J vector of the next spin (a row for a
+// left spin, a column for a right one) is copied into shared memory by cp.async while
+// the current spin is resolved.
+__host__ __device__ inline size_t bipartite_warp_smem(int nl, int nr) {
+    const size_t m = (size_t)(nl > nr ? nl : nr);
+    return dense_warp_align16((size_t)nl + nr) + 16 * m + dense_warp_align16(8 * (m + 1)) +
+           dense_warp_align16(4 * (m + 8));
+}
+
+__global__ void __launch_bounds__(32) sa_bipartite_reforder_warp_kernel(
+    int8_t* __restrict__ spins, const double* __restrict__ J, int nl, int nr, const double* __restrict__ lbias,
+    const double* __restrict__ rbias, int R, const float* __restrict__ temps, int nsched, int mcsteps,
+    const int32_t* __restrict__ rands, int64_t rand_stride, int64_t* __restrict__ rand_used, ExpPatch ep,
+    int32_t* status) {
+    extern __shared__ __align__(16) int8_t sh[];
+    const int r = blockIdx.x;
+    if (r >= R) return;
+    const int lane = threadIdx.x;
+    const int m = nl > nr ? nl : nr;
+    int8_t* lv = sh;                                                                                 // [nl]
+    int8_t* rv = sh + nl;                                                                            // [nr]
+    double* vec = reinterpret_cast<double*>(sh + dense_warp_align16((size_t)nl + nr));              // [2][m]
+    double* t64 = vec + (size_t)2 * m;                                                               // [m + 1]
+    float* t32 = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(t64) +
+                                          dense_warp_align16((size_t)8 * (m + 1)));                 // [m + 8]
+    int8_t* gs = spins + (int64_t)r * (nl + nr);
+    for (int t = lane; t < nl + nr; t += 32) sh[t] = gs[t];
+    __syncwarp();
+    const int64_t cap = rand_stride;
+    UniformRing ring;
+    ring.init(rands + (int64_t)r * rand_stride, cap, lane);
+    int64_t used = 0;
+    bool dead = false;
+    // J vector of spin (side, i): side 0 = left (row i of J, nr entries), 1 = right (column i, nl entries)
+    auto prefetch = [&](int side, int i, int b) {
+        double* dst = vec + (size_t)b * m;
+        if (side == 0) {
+            for (int j = lane; j < nr; j += 32) cp_async8(dst + j, J + (int64_t)i * nr + j);
+        } else {
+            for (int j = lane; j < nl; j += 32) cp_async8(dst + j, J + (int64_t)j * nr + i);
+        }
+        cp_async_commit();
+    };
+    const int64_t total = (int64_t)nsched * mcsteps * (nl + nr);
+    if (total > 0) {
+        // the spin after (side, i) in the sweep order
+        auto after = [&](int& side, int& i) {
+            if (side == 0) {
+                if (++i == nl) { i = 0; side = nr > 0 ? 1 : 0; }
+            } else {
+                if (++i == nr) { i = 0; side = nl > 0 ? 0 : 1; }
+            }
+        };
+        int side = nl > 0 ? 0 : 1, i = 0;
+        prefetch(side, i, 0);
+        int buf = 0;
+        int64_t pos = 0;
+        for (int g = 0; g < nsched && !dead; ++g) {
+            const float temp = temps[g];
+            const float rl = quick_scale(temp);
+            for (int64_t q = 0; q < (int64_t)mcsteps * (nl + nr) && !dead; ++q, ++pos) {
+                int nside = side, ni = i;
+                after(nside, ni);
+                if (pos + 1 < total) prefetch(nside, ni, buf ^ 1);
+                else cp_async_commit();
+                cp_async_wait<1>();
+                __syncwarp();
+                // terms of spin (side, i) against the other side, FP64 in the reference's order
+                const double* jv = vec + (size_t)buf * m;
+                const int8_t* self = side == 0 ? lv : rv;
+                const int8_t* other = side == 0 ? rv : lv;
+                const int no = side == 0 ? nr : nl;
+                const double si = (double)self[i];
+                bool exact = true;
+                for (int j = lane; j < no; j += 32) {
+                    const double sj = (double)other[j];
+                    const double t = side == 0 ? 2.0 * si * jv[j] * sj + lbias[i] * si + rbias[j] * sj
+                                               : 2.0 * si * jv[j] * sj + lbias[j] * sj + rbias[i] * si;
+                    const float tf = __double2float_rn(t);
+                    exact = exact && (double)tf == t;
+                    t64[j] = t;
+                    t32[j] = tf;
+                }
+                const bool f32 = __all_sync(0xffffffffu, exact);
+                __syncwarp();
+                float ediff = 0.0f;
+                if (f32) {
+                    const float4* tv = reinterpret_cast<const float4*>(t32);
+                    const int nq = no >> 2;
+                    float4 v = tv[0];
+                    for (int qq = 0; qq < nq; ++qq) {
+                        const float4 vn = tv[qq + 1];
+                        ediff = __fsub_rn(__fsub_rn(__fsub_rn(__fsub_rn(ediff, v.x), v.y), v.z), v.w);
+                        v = vn;
+                    }
+                    for (int j = nq * 4; j < no; ++j) ediff = __fsub_rn(ediff, t32[j]);
+                } else {
+                    for (int j = 0; j < no; ++j) ediff = __double2float_rn(__dsub_rn((double)ediff, t64[j]));
+                }
+                bool flip = false;
+                if (ediff > 0.0f) {
+                    flip = true;
+                } else if (used >= cap) {
+                    if (lane == 0) pq_set_status(status, PQ_ERR_RAND_EXHAUSTED);
+                    dead = true;
+                    break;
+                } else {
+                    const int32_t rvv = ring.get(used);
+                    ++used;
+                    ring.advance(used, lane);
+                    const int fast = rl != 0.0f ? quick_decide(ediff, rl, rvv) : -1;
+                    if (fast >= 0) {
+                        flip = fast != 0;
+                    } else {
+                        const float xf = __fdiv_rn(ediff, temp);
+                        const int quick = fp32_decide(xf, rvv);
+                        if (quick >= 0) {
+                            flip = quick != 0;
+                        } else {
+                            const double qv = (double)rvv / 2147483647.0;   // glibc RAND_MAX
+                            bool miss = false;
+                            flip = patched_exp(xf, qv, ep, &miss) > qv;
+                            if (miss && lane == 0) record_close(ep, xf, exp((double)xf));
+                        }
+                    }
+                }
+                if (flip && lane == 0) {
+                    int8_t* sp = side == 0 ? lv : rv;
+                    sp[i] = (int8_t)-sp[i];
+                }
+                __syncwarp();
+                side = nside;
+                i = ni;
+                buf ^= 1;
+            }
+        }
+    }
+    cp_async_wait<0>();
+    __syncwarp();
+    if (lane == 0) rand_used[r] = dead ? -1 : used;
+    for (int t = lane; t < nl + nr; t += 32) gs[t] = sh[t];
+}
+
 __global__ void exp_probe_kernel(const float* __restrict__ x, double* __restrict__ y, int64_t n) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) y[i] = exp((double)x[i]);
@@ -1371,6 +1519,14 @@ int pq_sa_bipartite_reforder_ex(int8_t* spins, const double* J, int nl, int nr, 
         return PQ_ERR_INVALID_ARG;
     if (R == 0) return PQ_OK;
     ExpPatch ep = make_patch(ov_x, ov_y, ov_n, close_x, close_y, close_cap, close_cnt);
+    const size_t wsmem = bipartite_warp_smem(nl, nr);
+    if (nl > 0 && nr > 0 && wsmem <= kRefSmemMax) {
+        PQ_CUDA_TRY(cudaFuncSetAttribute(sa_bipartite_reforder_warp_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsmem));
+        sa_bipartite_reforder_warp_kernel<<<R, 32, wsmem, (cudaStream_t)stream>>>(
+            spins, J, nl, nr, lbias, rbias, R, temps, nsched, mcsteps, rands, rand_stride, rand_used, ep, status);
+        return pq_launch_status();
+    }
     sa_bipartite_reforder_kernel<<<(R + kRefThreads - 1) / kRefThreads, kRefThreads, 0, (cudaStream_t)stream>>>(
         spins, J, nl, nr, lbias, rbias, R, temps, nsched, mcsteps, rands, rand_stride, rand_used, ep, status);
     return pq_launch_status();

@@ -261,6 +261,34 @@ def test_random_sa_dense_cases_vs_oracle(piqmc, kind):
             assert used[r] == u
 
 
+@pytest.mark.parametrize("kind", ["fp32", "fp64"])
+def test_random_bipartite_cases_vs_oracle(piqmc, kind):
+    """sa.Anneal_bipartite in reference order (one warp per replica) against the oracle:
+    FP32-valued weights and biases (FP32 chain) and general FP64 ones, uneven sides."""
+    from piqmc import reforder
+    g = np.random.default_rng(21)
+    for nl, nr in [(37, 70), (70, 5), (1, 33), (40, 40)]:
+        J = g.normal(0, 1, (nl, nr))
+        lb, rb = g.normal(0, 0.5, nl), g.normal(0, 0.5, nr)
+        if kind == "fp32":
+            J, lb, rb = (a.astype(np.float32).astype(np.float64) for a in (J, lb, rb))
+            lb[:] = np.round(lb * 4) / 4   # terms stay FP32 values: 2J +- b with b on a coarse grid
+            rb[:] = np.round(rb * 4) / 4
+            J = np.round(J * 64) / 64
+        sched = np.linspace(3.0, 0.1, 6)
+        R = 3
+        spins = np.where(g.random((R, nl + nr)) < 0.5, -1, 1).astype(np.int8)
+        rands = g.integers(0, 2 ** 31 - 1, size=(R, (nl + nr) * 12), dtype=np.int64).astype(np.int32)
+        out, used = reforder.anneal_bipartite(spins, nl, J, lb, rb, sched, 2, rands)
+        out = out.cpu().numpy()
+        for r in range(R):
+            lv, rv = spins[r, :nl].copy(), spins[r, nl:].copy()
+            u = oracle.sa_bipartite(lv, rv, J, lb, rb, sched, 2, rands[r])
+            np.testing.assert_array_equal(out[r, :nl], lv)
+            np.testing.assert_array_equal(out[r, nl:], rv)
+            assert used[r] == u
+
+
 def test_fp64_accumulator_with_huge_couplings(piqmc):
     """Couplings near FP32's range switch the sweeps to the FP64 accumulator (2J would overflow)."""
     from piqmc import reforder
