@@ -912,7 +912,7 @@ __host__ __device__ inline size_t dense_warp_align16(size_t x) { return (x + 15)
 // (FP32 padded for the read-ahead), one flag per row.
 __host__ __device__ inline size_t dense_warp_smem(int n, int P) {
     return dense_warp_align16((size_t)n * P) + (size_t)16 * n + dense_warp_align16((size_t)8 * (n + 2)) +
-           dense_warp_align16((size_t)4 * (n + 8)) + dense_warp_align16((size_t)n);
+           dense_warp_align16((size_t)4 * (n + 12)) + dense_warp_align16((size_t)n);
 }
 
 // The FP32 value of an FP64 value that is zero or a normal FP32 number, by its bits.
@@ -947,8 +947,8 @@ __global__ void __launch_bounds__(32) dense_reforder_warp_kernel(
     double* row = reinterpret_cast<double*>(sh + dense_warp_align16((size_t)n * Pq));                 // [2][n]
     double* t64 = row + (size_t)2 * n;                                                               // [n + 2]
     float* t32 = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(t64) +
-                                          dense_warp_align16((size_t)8 * (n + 2)));                  // [n + 8]
-    uint8_t* row_f32 = reinterpret_cast<uint8_t*>(t32) + dense_warp_align16((size_t)4 * (n + 8));   // [n]
+                                          dense_warp_align16((size_t)8 * (n + 2)));                  // [n + 12]
+    uint8_t* row_f32 = reinterpret_cast<uint8_t*>(t32) + dense_warp_align16((size_t)4 * (n + 12));  // [n]
     int8_t* gs = spins + (int64_t)r * n * Pq;
     for (int64_t t = lane; t < (int64_t)n * Pq; t += 32) s[t] = gs[t];
     // which rows give FP32 terms only (the upper triangle and diagonal the reference reads)
@@ -1047,13 +1047,15 @@ __global__ void __launch_bounds__(32) dense_reforder_warp_kernel(
                         if (!QA || (flags & PQ_FIX_Q2)) ediff = 0.0f;
                         const int nt = QA ? n + 2 : n;
                         if (f32) {
+                            // two vectors ahead: a shared-memory read outlasts one vector's four adds
                             const float4* tv = reinterpret_cast<const float4*>(t32);
                             const int nq = nt >> 2;
-                            float4 v = tv[0];
+                            float4 v = tv[0], v1 = tv[1];
                             for (int q = 0; q < nq; ++q) {
-                                const float4 vn = tv[q + 1];
+                                const float4 v2 = tv[q + 2];
                                 ediff = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(ediff, v.x), v.y), v.z), v.w);
-                                v = vn;
+                                v = v1;
+                                v1 = v2;
                             }
                             for (int j = nq * 4; j < nt; ++j) ediff = __fadd_rn(ediff, t32[j]);
                         } else {
@@ -1121,7 +1123,7 @@ __global__ void __launch_bounds__(32) dense_reforder_warp_kernel(
 __host__ __device__ inline size_t bipartite_warp_smem(int nl, int nr) {
     const size_t m = (size_t)(nl > nr ? nl : nr);
     return dense_warp_align16((size_t)nl + nr) + 16 * m + dense_warp_align16(8 * (m + 1)) +
-           dense_warp_align16(4 * (m + 8));
+           dense_warp_align16(4 * (m + 12));
 }
 
 __global__ void __launch_bounds__(32) sa_bipartite_reforder_warp_kernel(
@@ -1139,7 +1141,7 @@ __global__ void __launch_bounds__(32) sa_bipartite_reforder_warp_kernel(
     double* vec = reinterpret_cast<double*>(sh + dense_warp_align16((size_t)nl + nr));              // [2][m]
     double* t64 = vec + (size_t)2 * m;                                                               // [m + 1]
     float* t32 = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(t64) +
-                                          dense_warp_align16((size_t)8 * (m + 1)));                 // [m + 8]
+                                          dense_warp_align16((size_t)8 * (m + 1)));                 // [m + 12]
     int8_t* gs = spins + (int64_t)r * (nl + nr);
     for (int t = lane; t < nl + nr; t += 32) sh[t] = gs[t];
     __syncwarp();
@@ -1204,11 +1206,12 @@ __global__ void __launch_bounds__(32) sa_bipartite_reforder_warp_kernel(
                 if (f32) {
                     const float4* tv = reinterpret_cast<const float4*>(t32);
                     const int nq = no >> 2;
-                    float4 v = tv[0];
+                    float4 v = tv[0], v1 = tv[1];
                     for (int qq = 0; qq < nq; ++qq) {
-                        const float4 vn = tv[qq + 1];
+                        const float4 v2 = tv[qq + 2];
                         ediff = __fsub_rn(__fsub_rn(__fsub_rn(__fsub_rn(ediff, v.x), v.y), v.z), v.w);
-                        v = vn;
+                        v = v1;
+                        v1 = v2;
                     }
                     for (int j = nq * 4; j < no; ++j) ediff = __fsub_rn(ediff, t32[j]);
                 } else {
