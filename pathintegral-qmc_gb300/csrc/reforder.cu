@@ -885,19 +885,18 @@ __global__ void __launch_bounds__(32) sa_sparse_reforder_warp_kernel(
 }
 
 // Dense reference-order sweeps (QuantumAnneal_dense, piqmc/qmc.pyx:181-242, and
-// sa.Anneal_dense, piqmc/sa.pyx:126-187) with one warp per replica.  For each
-// position of the permutation the lanes compute the n terms of the reference's sum
-// (and QA's two Trotter terms) in parallel -- every term -2 s_i (J_ij s_j) is exactly
-// +-2 J_ij in FP64 -- into shared memory, and the warp then walks the accumulator
-// chain through them in the reference's order.  When every term of the update is an
-// FP32 value, (float)((double)e + t) equals the FP32 sum e + t (double rounding
-// through 53 >= 2*24 + 2 bits is innocuous), so the chain is FP32 adds; otherwise it
-// is the reference's FP64 add and rounding, term by term.  The row of J the next
-// position needs -- J[i][j] for j >= i and J[j][i] below the diagonal, the upper
-// triangle the reference reads (piqmc/qmc.pyx:206-219) -- is copied into shared
-// memory by cp.async while the current position is resolved, and the uniforms come
-// from the register ring.  Same spins, uniforms and close calls (recorded by lane 0)
-// as qa_dense_reforder_kernel and sa_dense_reforder_kernel.
+// sa.Anneal_dense, piqmc/sa.pyx:126-187) by warps: for each position of the
+// permutation the lanes form the n terms of the reference's sum (and QA's two Trotter
+// terms) in parallel -- every term -2 s_i (J_ij s_j) is exactly +-2 J_ij in FP64 --
+// into shared memory, and a warp then walks the accumulator chain through them in the
+// reference's order.  For rows whose entries are all zero or normal FP32 values with
+// 2J finite the terms are formed in FP32 and the chain is FP32 adds:
+// (float)((double)e + t) equals the FP32 sum e + t for FP32 e and t (double rounding
+// through 53 >= 2*24 + 2 bits is innocuous); otherwise the chain is the reference's
+// FP64 add and rounding, term by term.  The J row a position needs -- J[i][j] for
+// j >= i and J[j][i] below the diagonal, the upper triangle the reference reads
+// (piqmc/qmc.pyx:206-219) -- is copied into shared memory by cp.async ahead of use,
+// and the uniforms come from the register ring.
 __device__ __forceinline__ void cp_async8(void* smem_dst, const void* gsrc) {
     const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(gsrc) : "memory");
@@ -907,13 +906,6 @@ template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 __host__ __device__ inline size_t dense_warp_align16(size_t x) { return (x + 15) & ~(size_t)15; }
-
-// Shared memory of the dense warp kernels: spins [n][P], two J rows, FP64 and FP32 terms
-// (FP32 padded for the read-ahead), one flag per row.
-__host__ __device__ inline size_t dense_warp_smem(int n, int P) {
-    return dense_warp_align16((size_t)n * P) + (size_t)16 * n + dense_warp_align16((size_t)8 * (n + 2)) +
-           dense_warp_align16((size_t)4 * (n + 12)) + dense_warp_align16((size_t)n);
-}
 
 // The FP32 value of an FP64 value that is zero or a normal FP32 number, by its bits.
 __device__ __forceinline__ float f32_of_exact(double d) {
@@ -932,8 +924,42 @@ __device__ __forceinline__ bool fp32_term_exact(double v) {
     return v == 0.0 || (a >= 1.1754943508222875e-38 && a <= 1.7014117331926443e38 && (double)__double2float_rn(v) == v);
 }
 
+// The same sweeps with two warps per replica on two SM sub-partitions: the term warp
+// forms the terms of position p + 1 (and copies in J rows) while the chain warp walks
+// and decides position p; one 64-thread named barrier per position.  The term warp
+// forms position p + 1 before p's flip is known, so after the barrier the chain warp
+// corrects them exactly: a flip of spin (i_p, k_p) negates position p + 1's column
+// i_p when the slice is the same, all its terms when it is the same spin in the same
+// slice (a new sweep of sa.Anneal_dense can start with the spin the last one ended
+// on), and a Trotter term of the same spin that reads slice k_p.  The term warp owns
+// the spins and applies each flip after the barrier.  Same spins, uniforms and close
+// calls as the single-warp kernel.
+// One position of the sweep order: field step g, MC step, slice k, index t in the
+// permutation; next() steps through g -> step -> k -> t without divisions.
+struct DensePos {
+    int g, step, k, t;
+    __device__ __forceinline__ void next(int n, int Pq, int mcsteps) {
+        if (++t == n) {
+            t = 0;
+            if (++k == Pq) {
+                k = 0;
+                if (++step == mcsteps) { step = 0; ++g; }
+            }
+        }
+    }
+};
+
+// Shared memory of the dense pair kernel: spins [n][P], two J rows, two sets of FP64 and
+// FP32 terms (FP32 padded for the chain's read-ahead), one flag per row, control words.
+__host__ __device__ inline size_t dense_pair_smem(int n, int P) {
+    return dense_warp_align16((size_t)n * P) + (size_t)16 * n + dense_warp_align16((size_t)16 * (n + 2)) +
+           2 * dense_warp_align16((size_t)4 * (n + 12)) + dense_warp_align16((size_t)n) + 16;
+}
+
+__device__ __forceinline__ void pair_barrier() { asm volatile("bar.sync 1, 64;" ::: "memory"); }
+
 template <bool QA>
-__global__ void __launch_bounds__(32) dense_reforder_warp_kernel(
+__global__ void __launch_bounds__(64) dense_reforder_pair_kernel(
     int8_t* __restrict__ spins, const double* __restrict__ J, int n, int P, int R,
     const float* __restrict__ per_step,   // QA: J-perp of each field step; SA: its temperature
     int nsched, int mcsteps, float temp_qa, const int32_t* __restrict__ perms, const int32_t* __restrict__ rands,
@@ -941,36 +967,35 @@ __global__ void __launch_bounds__(32) dense_reforder_warp_kernel(
     extern __shared__ __align__(16) int8_t sh[];
     const int r = blockIdx.x;
     if (r >= R) return;
-    const int lane = threadIdx.x;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int Pq = QA ? P : 1;
+    const int nt = QA ? n + 2 : n;
     int8_t* s = sh;                                                                                   // [n][P]
     double* row = reinterpret_cast<double*>(sh + dense_warp_align16((size_t)n * Pq));                 // [2][n]
-    double* t64 = row + (size_t)2 * n;                                                               // [n + 2]
+    double* t64 = row + (size_t)2 * n;                                                               // [2][n + 2]
     float* t32 = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(t64) +
-                                          dense_warp_align16((size_t)8 * (n + 2)));                  // [n + 12]
-    uint8_t* row_f32 = reinterpret_cast<uint8_t*>(t32) + dense_warp_align16((size_t)4 * (n + 12));  // [n]
+                                          dense_warp_align16((size_t)16 * (n + 2)));                 // [2][t32s]
+    const size_t t32s = dense_warp_align16((size_t)4 * (n + 12)) / 4;
+    uint8_t* row_f32 = reinterpret_cast<uint8_t*>(t32 + 2 * t32s);                                   // [n]
+    int* ctl = reinterpret_cast<int*>(row_f32 + dense_warp_align16((size_t)n));                      // flip, stop
     int8_t* gs = spins + (int64_t)r * n * Pq;
-    for (int64_t t = lane; t < (int64_t)n * Pq; t += 32) s[t] = gs[t];
-    // which rows give FP32 terms only (the upper triangle and diagonal the reference reads)
-    for (int i = 0; i < n; ++i) {
+    for (int64_t t = threadIdx.x; t < (int64_t)n * Pq; t += 64) s[t] = gs[t];
+    for (int i = warp; i < n; i += 2) {
         bool ok = true;
         for (int j = lane; j < n; j += 32) ok = ok && fp32_term_exact(j >= i ? J[(int64_t)i * n + j] : J[(int64_t)j * n + i]);
         ok = __all_sync(0xffffffffu, ok);
         if (lane == 0) row_f32[i] = ok ? 1 : 0;
     }
-    __syncwarp();
+    if (threadIdx.x < 4) ctl[threadIdx.x] = 0;
+    __syncthreads();
     const int32_t* pr = perms + (int64_t)r * nsched * mcsteps * n;
-    const int64_t cap = rand_stride;
-    UniformRing ring;
-    ring.init(rands + (int64_t)r * rand_stride, cap, lane);
-    int64_t used = 0;
-    bool bad = false, dead = false;
     const int64_t nsweeps = (int64_t)nsched * mcsteps;
-    // permutation entry of the position loaded next (counters stepped, no division)
+    const int64_t total = nsweeps * Pq * n;
+    // each warp walks the permutation entries itself (counters stepped, no division)
     int64_t q_sweep = 0;
     int q_k = 0, q_t = 0;
-    auto next_entry = [&](bool& has) -> int {
-        has = q_sweep < nsweeps;
+    auto next_entry = [&]() -> int {
+        const bool has = q_sweep < nsweeps;
         const int v = __ldg(pr + (has ? q_sweep * n + q_t : 0));
         if (++q_t == n) {
             q_t = 0;
@@ -978,138 +1003,198 @@ __global__ void __launch_bounds__(32) dense_reforder_warp_kernel(
         }
         return v;
     };
-    auto prefetch_row = [&](int i, int b) {
-        if ((unsigned)i >= (unsigned)n) i = 0;   // a bad entry stops the run when it is reached
-        double* dst = row + (size_t)b * n;
-        for (int j = lane; j < n; j += 32)
-            cp_async8(dst + j, j >= i ? J + (int64_t)i * n + j : J + (int64_t)j * n + i);
-        cp_async_commit();
+    auto safe = [&](int i) { return (unsigned)i < (unsigned)n ? i : 0; };
+    auto jp_of = [&](int g) -> double { return QA ? (double)per_step[g] : 0.0; };
+    auto f32_of = [&](int i, int g) -> bool {
+        return row_f32[safe(i)] && (!QA || fabs(jp_of(g)) <= 1.7014117331926443e38);
     };
-    if (nsweeps > 0 && n > 0) {
-        bool h0, h1, h2;
-        int i0 = next_entry(h0);
-        int i1 = next_entry(h1);
-        prefetch_row(i0, 0);
-        int buf = 0;
-        for (int g = 0; g < nsched && !dead; ++g) {
-            const float temp = QA ? temp_qa : per_step[g];
-            const double jp = QA ? (double)per_step[g] : 0.0;
-            const bool jp_ok = !QA || fabs(jp) <= 1.7014117331926443e38;   // +-2 J-perp is an FP32 value
-            const float rl = quick_scale(temp);
-            for (int step = 0; step < mcsteps && !dead; ++step) {
-                for (int k = 0; k < Pq && !dead; ++k) {
-                    int tl = P - 1, tr = 1;   // Q1 as shipped (piqmc/qmc.pyx:233-236)
-                    if (QA && (flags & PQ_FIX_Q1)) { tl = k == 0 ? P - 1 : k - 1; tr = k == P - 1 ? 0 : k + 1; }
-                    float ediff = 0.0f;       // QA, Q2 as shipped: reset once per slice
-                    for (int t = 0; t < n && !dead; ++t) {
-                        const int i = i0;
-                        if (h1) prefetch_row(i1, buf ^ 1);
-                        else cp_async_commit();
-                        const int i2 = next_entry(h2);
-                        cp_async_wait<1>();   // this position's row has landed
-                        __syncwarp();
-                        if ((unsigned)i >= (unsigned)n) {
-                            bad = dead = true;
-                            break;
-                        }
-                        // the terms, one per lane and column: FP32 when every term of the row is an
-                        // FP32 value (s_i s_j J_ij -> +-2 J_ij by sign bits and one exact multiply),
-                        // else FP64 as the reference forms them
-                        const int8_t si8 = s[(int64_t)i * Pq + k];
-                        const double* rw = row + (size_t)buf * n;
-                        const bool f32 = jp_ok && row_f32[i];
-                        if (f32) {
-                            const float m2si = si8 > 0 ? -2.0f : 2.0f;
-                            for (int j = lane; j < n; j += 32) {
-                                const float jf = f32_of_exact(rw[j]);
-                                const uint32_t sgn = j == i ? 0u : ((uint32_t)(int32_t)s[(int64_t)j * Pq + k] & 0x80000000u);
-                                t32[j] = __fmul_rn(__uint_as_float(__float_as_uint(m2si) ^ sgn), jf);
-                            }
-                            if (QA && lane == 0) {
-                                const float jpf = (float)jp;
-                                t32[n] = __fmul_rn(m2si, s[(int64_t)i * Pq + tl] > 0 ? jpf : -jpf);
-                                t32[n + 1] = __fmul_rn(m2si, s[(int64_t)i * Pq + tr] > 0 ? jpf : -jpf);
-                            }
-                        } else {
-                            const double m2si = -2.0 * (double)si8;
-                            for (int j = lane; j < n; j += 32) {
-                                const double jv = rw[j];
-                                t64[j] = j == i ? m2si * jv : m2si * (jv * (double)s[(int64_t)j * Pq + k]);
-                            }
-                            if (QA && lane == 0) {
-                                t64[n] = m2si * (jp * (double)s[(int64_t)i * Pq + tl]);
-                                t64[n + 1] = m2si * (jp * (double)s[(int64_t)i * Pq + tr]);
-                            }
-                        }
-                        __syncwarp();
-                        // the chain, in the reference's order (every lane, same values; the next
-                        // values are read while the current ones are added)
-                        if (!QA || (flags & PQ_FIX_Q2)) ediff = 0.0f;
-                        const int nt = QA ? n + 2 : n;
-                        if (f32) {
-                            // two vectors ahead: a shared-memory read outlasts one vector's four adds
-                            const float4* tv = reinterpret_cast<const float4*>(t32);
-                            const int nq = nt >> 2;
-                            float4 v = tv[0], v1 = tv[1];
-                            for (int q = 0; q < nq; ++q) {
-                                const float4 v2 = tv[q + 2];
-                                ediff = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(ediff, v.x), v.y), v.z), v.w);
-                                v = v1;
-                                v1 = v2;
-                            }
-                            for (int j = nq * 4; j < nt; ++j) ediff = __fadd_rn(ediff, t32[j]);
-                        } else {
-                            double v = t64[0];
-                            for (int j = 0; j < nt; ++j) {
-                                const double vn = t64[j + 1 < nt ? j + 1 : j];
-                                ediff = acc(ediff, v);
-                                v = vn;
-                            }
-                        }
-                        // Metropolis test (ref_accept's arithmetic; one uniform when ediff <= 0)
-                        bool flip = false;
-                        if (ediff > 0.0f) {
-                            flip = true;
-                        } else if (used >= cap) {
-                            if (lane == 0) pq_set_status(status, PQ_ERR_RAND_EXHAUSTED);
-                            dead = true;
-                            break;
-                        } else {
-                            const int32_t rv = ring.get(used);
-                            ++used;
-                            ring.advance(used, lane);
-                            const int fast = rl != 0.0f ? quick_decide(ediff, rl, rv) : -1;
-                            if (fast >= 0) {
-                                flip = fast != 0;
-                            } else {
-                                const float xf = __fdiv_rn(ediff, temp);
-                                const int quick = fp32_decide(xf, rv);
-                                if (quick >= 0) {
-                                    flip = quick != 0;
-                                } else {
-                                    const double q = (double)rv / 2147483647.0;   // glibc RAND_MAX
-                                    bool miss = false;
-                                    flip = patched_exp(xf, q, ep, &miss) > q;
-                                    if (miss && lane == 0) record_close(ep, xf, exp((double)xf));
-                                }
-                            }
-                        }
-                        if (flip && lane == 0) s[(int64_t)i * Pq + k] = (int8_t)-s[(int64_t)i * Pq + k];
-                        __syncwarp();
-                        i0 = i1; h0 = h1;
-                        i1 = i2; h1 = h2;
-                        buf ^= 1;
+    auto tl_of = [&](int k) { return (QA && (flags & PQ_FIX_Q1)) ? (k == 0 ? P - 1 : k - 1) : P - 1; };
+    auto tr_of = [&](int k) { return (QA && (flags & PQ_FIX_Q1)) ? (k == P - 1 ? 0 : k + 1) : 1; };
+    bool dead = false, bad = false;
+    int64_t used = 0;
+    if (total > 0) {
+        if (warp == 1) {
+            // ---- term warp ----
+            auto prefetch_row = [&](int i, int b) {
+                i = safe(i);
+                double* dst = row + (size_t)b * n;
+                for (int j = lane; j < n; j += 32)
+                    cp_async8(dst + j, j >= i ? J + (int64_t)i * n + j : J + (int64_t)j * n + i);
+                cp_async_commit();
+            };
+            auto form = [&](int i, int k, int g, const double* rw, float* o32, double* o64) {
+                const bool f32 = f32_of(i, g);
+                i = safe(i);
+                const int8_t si8 = s[(int64_t)i * Pq + k];
+                if (f32) {
+                    const float m2si = si8 > 0 ? -2.0f : 2.0f;
+                    for (int j = lane; j < n; j += 32) {
+                        const float jf = f32_of_exact(rw[j]);
+                        const uint32_t sgn = j == i ? 0u : ((uint32_t)(int32_t)s[(int64_t)j * Pq + k] & 0x80000000u);
+                        o32[j] = __fmul_rn(__uint_as_float(__float_as_uint(m2si) ^ sgn), jf);
+                    }
+                    if (QA && lane == 0) {
+                        const float jpf = (float)jp_of(g);
+                        o32[n] = __fmul_rn(m2si, s[(int64_t)i * Pq + tl_of(k)] > 0 ? jpf : -jpf);
+                        o32[n + 1] = __fmul_rn(m2si, s[(int64_t)i * Pq + tr_of(k)] > 0 ? jpf : -jpf);
+                    }
+                } else {
+                    const double m2si = -2.0 * (double)si8;
+                    for (int j = lane; j < n; j += 32) {
+                        const double jv = rw[j];
+                        o64[j] = j == i ? m2si * jv : m2si * (jv * (double)s[(int64_t)j * Pq + k]);
+                    }
+                    if (QA && lane == 0) {
+                        const double jp = jp_of(g);
+                        o64[n] = m2si * (jp * (double)s[(int64_t)i * Pq + tl_of(k)]);
+                        o64[n + 1] = m2si * (jp * (double)s[(int64_t)i * Pq + tr_of(k)]);
                     }
                 }
+            };
+            int e0 = next_entry(), e1 = next_entry(), e2 = next_entry(), e3 = next_entry();
+            DensePos nx{0, 0, 0, 0};   // the position whose terms are formed next
+            prefetch_row(e0, 0);
+            if (total > 1) prefetch_row(e1, 1);
+            else cp_async_commit();
+            cp_async_wait<1>();
+            __syncwarp();
+            form(e0, 0, 0, row, t32, t64);   // position 0
+            __syncwarp();
+            pair_barrier();                  // terms of position 0 are ready
+            for (int64_t p = 0; p < total; ++p) {
+                // terms of position p + 1 (the row of p + 2 is copied in meanwhile)
+                nx.next(n, Pq, mcsteps);
+                if (p + 2 < total) prefetch_row(e2, (int)(p & 1));
+                else cp_async_commit();
+                cp_async_wait<1>();
+                __syncwarp();
+                if (p + 1 < total)
+                    form(e1, nx.k, nx.g, row + (size_t)((p + 1) & 1) * n, t32 + (size_t)((p + 1) & 1) * t32s,
+                         t64 + (size_t)((p + 1) & 1) * (n + 2));
+                __syncwarp();
+                pair_barrier();              // the chain warp has decided position p
+                const int* c = ctl + 2 * (int)(p & 1);   // two slots: the chain warp writes p + 1's
+                if (c[1]) break;                         // only after the next barrier
+                if (lane == 0 && c[0] >= 0) {   // position p flipped: (i, k) packed
+                    const int fi = c[0] >> 8, fk = c[0] & 0xFF;
+                    s[(int64_t)fi * Pq + fk] = (int8_t)-s[(int64_t)fi * Pq + fk];
+                }
+                __syncwarp();
+                e1 = e2;
+                e2 = e3;
+                e3 = next_entry();
+            }
+            cp_async_wait<0>();
+        } else {
+            // ---- chain warp ----
+            UniformRing ring;
+            ring.init(rands + (int64_t)r * rand_stride, rand_stride, lane);
+            const int64_t cap = rand_stride;
+            int i0 = next_entry(), i1 = next_entry();
+            DensePos cur{0, 0, 0, 0};
+            float ediff = 0.0f;
+            pair_barrier();                  // terms of position 0 are ready
+            for (int64_t p = 0; p < total; ++p) {
+                DensePos nx = cur;
+                nx.next(n, Pq, mcsteps);
+                const int tb = (int)(p & 1);
+                const bool f32 = f32_of(i0, cur.g);
+                int flip_word = -1, stop = 0;
+                if ((unsigned)i0 >= (unsigned)n) {
+                    bad = dead = true;
+                    stop = 1;
+                } else {
+                    if (!QA || (flags & PQ_FIX_Q2) || cur.t == 0) ediff = 0.0f;   // QA, Q2 as shipped: per slice
+                    if (f32) {
+                        const float4* tv = reinterpret_cast<const float4*>(t32 + (size_t)tb * t32s);
+                        const int nq = nt >> 2;
+                        float4 v = tv[0], v1 = tv[1];
+                        for (int q = 0; q < nq; ++q) {
+                            const float4 v2 = tv[q + 2];
+                            ediff = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(ediff, v.x), v.y), v.z), v.w);
+                            v = v1;
+                            v1 = v2;
+                        }
+                        const float* c32 = t32 + (size_t)tb * t32s;
+                        for (int j = nq * 4; j < nt; ++j) ediff = __fadd_rn(ediff, c32[j]);
+                    } else {
+                        const double* c64 = t64 + (size_t)tb * (n + 2);
+                        double v = c64[0];
+                        for (int j = 0; j < nt; ++j) {
+                            const double vn = c64[j + 1 < nt ? j + 1 : j];
+                            ediff = acc(ediff, v);
+                            v = vn;
+                        }
+                    }
+                    const float temp = QA ? temp_qa : per_step[cur.g];
+                    bool flip = false;
+                    if (ediff > 0.0f) {
+                        flip = true;
+                    } else if (used >= cap) {
+                        if (lane == 0) pq_set_status(status, PQ_ERR_RAND_EXHAUSTED);
+                        dead = true;
+                        stop = 1;
+                    } else {
+                        const int32_t rv = ring.get(used);
+                        ++used;
+                        ring.advance(used, lane);
+                        const float rl = quick_scale(temp);
+                        const int fast = rl != 0.0f ? quick_decide(ediff, rl, rv) : -1;
+                        if (fast >= 0) {
+                            flip = fast != 0;
+                        } else {
+                            const float xf = __fdiv_rn(ediff, temp);
+                            const int quick = fp32_decide(xf, rv);
+                            if (quick >= 0) {
+                                flip = quick != 0;
+                            } else {
+                                const double qv = (double)rv / 2147483647.0;   // glibc RAND_MAX
+                                bool miss = false;
+                                flip = patched_exp(xf, qv, ep, &miss) > qv;
+                                if (miss && lane == 0) record_close(ep, xf, exp((double)xf));
+                            }
+                        }
+                    }
+                    if (flip) flip_word = (i0 << 8) | cur.k;
+                }
+                if (lane == 0) { ctl[2 * (int)(p & 1)] = flip_word; ctl[2 * (int)(p & 1) + 1] = stop; }
+                pair_barrier();              // the term warp has formed position p + 1
+                if (stop) break;
+                if (flip_word >= 0 && p + 1 < total && (unsigned)i1 < (unsigned)n) {
+                    // correct position p + 1's terms for this flip
+                    const int nb = (int)((p + 1) & 1);
+                    const bool f32n = f32_of(i1, nx.g);
+                    float* n32 = t32 + (size_t)nb * t32s;
+                    double* n64 = t64 + (size_t)nb * (n + 2);
+                    if (nx.k == cur.k) {
+                        if (i1 == i0) {
+                            for (int j = lane; j < n; j += 32) {
+                                if (f32n) n32[j] = -n32[j];
+                                else n64[j] = -n64[j];
+                            }
+                        } else if (lane == 0) {
+                            if (f32n) n32[i0] = -n32[i0];
+                            else n64[i0] = -n64[i0];
+                        }
+                    }
+                    if (QA && lane == 0 && i1 == i0) {
+                        if (tl_of(nx.k) == cur.k) { if (f32n) n32[n] = -n32[n]; else n64[n] = -n64[n]; }
+                        if (tr_of(nx.k) == cur.k) { if (f32n) n32[n + 1] = -n32[n + 1]; else n64[n + 1] = -n64[n + 1]; }
+                    }
+                    __syncwarp();
+                }
+                cur = nx;
+                i0 = i1;
+                i1 = next_entry();
             }
         }
-        (void)h0;
     }
-    cp_async_wait<0>();
-    __syncwarp();
-    if (bad && lane == 0) pq_set_status(status, PQ_ERR_BAD_INDEX);
-    if (lane == 0) rand_used[r] = dead ? -1 : used;
-    for (int64_t t = lane; t < (int64_t)n * Pq; t += 32) gs[t] = s[t];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (bad) pq_set_status(status, PQ_ERR_BAD_INDEX);
+        rand_used[r] = dead ? -1 : used;
+    }
+    for (int64_t t = threadIdx.x; t < (int64_t)n * Pq; t += 64) gs[t] = s[t];
 }
 
 // sa.Anneal_bipartite in reference order (piqmc/sa.pyx:411-500) with one warp per
@@ -1411,11 +1496,11 @@ int pq_qa_dense_reforder_ex(int8_t* spins, const double* J, int n, int P, int R,
     if (P < 2 || !spins || !J || !rand_used) return PQ_ERR_INVALID_ARG;
     if (R == 0) return PQ_OK;
     ExpPatch ep = make_patch(ov_x, ov_y, ov_n, close_x, close_y, close_cap, close_cnt);
-    const size_t wsmem = dense_warp_smem(n, P);
-    if (wsmem <= kRefSmemMax) {
-        PQ_CUDA_TRY(cudaFuncSetAttribute(dense_reforder_warp_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)wsmem));
-        dense_reforder_warp_kernel<true><<<R, 32, wsmem, (cudaStream_t)stream>>>(
+    const size_t psmem = dense_pair_smem(n, P);
+    if (psmem <= kRefSmemMax && P <= 256 && n <= (1 << 22)) {
+        PQ_CUDA_TRY(cudaFuncSetAttribute(dense_reforder_pair_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)psmem));
+        dense_reforder_pair_kernel<true><<<R, 64, psmem, (cudaStream_t)stream>>>(
             spins, J, n, P, R, jperp, nsched, mcsteps, temp, perms, rands, rand_stride, rand_used, flags, ep, status);
         return pq_launch_status();
     }
@@ -1492,11 +1577,11 @@ int pq_sa_dense_reforder_ex(int8_t* spins, const double* J, int n, int R, const 
     if (!spins || !J || !temps || !rand_used || (nsched * mcsteps > 0 && !perms)) return PQ_ERR_INVALID_ARG;
     if (R == 0) return PQ_OK;
     ExpPatch ep = make_patch(ov_x, ov_y, ov_n, close_x, close_y, close_cap, close_cnt);
-    const size_t wsmem = dense_warp_smem(n, 1);
-    if (wsmem <= kRefSmemMax) {
-        PQ_CUDA_TRY(cudaFuncSetAttribute(dense_reforder_warp_kernel<false>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsmem));
-        dense_reforder_warp_kernel<false><<<R, 32, wsmem, (cudaStream_t)stream>>>(
+    const size_t psmem = dense_pair_smem(n, 1);
+    if (psmem <= kRefSmemMax && n <= (1 << 22)) {
+        PQ_CUDA_TRY(cudaFuncSetAttribute(dense_reforder_pair_kernel<false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
+        dense_reforder_pair_kernel<false><<<R, 64, psmem, (cudaStream_t)stream>>>(
             spins, J, n, 1, R, temps, nsched, mcsteps, 1.0f, perms, rands, rand_stride, rand_used, 0, ep, status);
         return pq_launch_status();
     }
