@@ -151,6 +151,9 @@ struct UniformRing {
     }
 };
 
+// Barrier of the two warps of a replica's CTA (named barrier 1, 64 threads).
+__device__ __forceinline__ void pair_barrier() { asm volatile("bar.sync 1, 64;" ::: "memory"); }
+
 // Metropolis test of reference piqmc/qmc.pyx:130-133 (ge = false) and
 // piqmc/sa.pyx:114-117 (ge = true): deterministic accept on ediff > 0 (>= 0),
 // otherwise exp((double)(ediff / temp)) > rand() / (double)RAND_MAX.
@@ -299,229 +302,340 @@ struct RefBlockIn {
     float v[MAXNB];
 };
 
+// The same sweep with two warps per replica: the fold warp prepares block b + 1 --
+// neighbour rows, signed couplings and Trotter terms, records, in-block dependencies --
+// while the chain warp resolves block b (the walk, speculation and decisions above),
+// one 64-thread named barrier per block.  The fold warp reads spins before block b's
+// flips are known, so it also notes, per term, the position in block b of a neighbour
+// in the same slice, and per spin its own position in block b; after the barrier the
+// chain warp negates exactly the terms whose neighbour (or, for a Trotter term, whose
+// spin in the slice the term reads) flipped.  The fold warp owns the spins and the
+// position tables and applies each block's flips after the barrier; the flip mask of a
+// block travels in a control slot chosen by the block's parity.  Same spins, uniforms
+// and close calls as the single-thread kernel qa_sparse_reforder_kernel.
+struct SparseBlk {
+    int g, step, k, blk;
+    __device__ __forceinline__ void next(int nblk, int P, int mcsteps) {
+        if (++blk == nblk) {
+            blk = 0;
+            if (++k == P) {
+                k = 0;
+                if (++step == mcsteps) { step = 0; ++g; }
+            }
+        }
+    }
+};
+
+template <int MAXNB>
+struct SparsePairLayout {
+    size_t pos_of, rec, dep, pp, ppv, self, ctl, total;
+    __host__ __device__ SparsePairLayout(int n, int P) {
+        auto a16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
+        pos_of = a16((size_t)n * P);                 // [2][n]
+        rec = pos_of + a16((size_t)2 * n);           // float4 [2][33][2]
+        dep = rec + (size_t)2 * 33 * 2 * 16;         // uint32 [2][32]
+        pp = dep + (size_t)2 * 32 * 4;               // uint8 [2][32][MAXNB]
+        ppv = pp + a16((size_t)2 * 32 * MAXNB);      // uint8 [2][32][MAXNB]
+        self = ppv + a16((size_t)2 * 32 * MAXNB);    // uint8 [2][32]
+        ctl = self + 64;                             // int [2][2] + bad flag
+        total = ctl + 32;
+    }
+};
+
 template <bool FP64, int MAXNB, bool FIXQ2>
-__global__ void __launch_bounds__(32) qa_sparse_reforder_warp_kernel(
+__global__ void __launch_bounds__(64) qa_sparse_reforder_pair_kernel(
     int8_t* __restrict__ spins, const int32_t* __restrict__ nb_idx, const float* __restrict__ nb_j, int n, int nperm,
     int maxnb, int P, int R, const float* __restrict__ jperp, int nsched, int mcsteps, float temp,
     const int32_t* __restrict__ perms, const int32_t* __restrict__ rands, int64_t rand_stride,
     int64_t* __restrict__ rand_used, int flags, ExpPatch ep, int32_t* status) {
     static_assert(MAXNB + 3 <= 8, "record holds MAXNB terms, two Trotter terms and s2");
     extern __shared__ __align__(16) int8_t sh[];
-    int8_t* s = sh;                                                                             // [n][P]
-    uint8_t* pos_of = reinterpret_cast<uint8_t*>(sh + (((size_t)n * P + 15) & ~(size_t)15));   // [n]
-    // terms of the block's 32 positions (+ one spare so position l + 1 can be read ahead)
-    float4* rec = reinterpret_cast<float4*>(pos_of + (((size_t)n + 15) & ~(size_t)15));        // [33][2]
+    const SparsePairLayout<MAXNB> L(n, P);
+    int8_t* s = sh;                                                            // [n][P]
+    uint8_t* pos_of = reinterpret_cast<uint8_t*>(sh + L.pos_of);               // [2][n]
+    float4* rec = reinterpret_cast<float4*>(sh + L.rec);                       // [2][33][2]
+    uint32_t* mdep = reinterpret_cast<uint32_t*>(sh + L.dep);                  // [2][32]
+    uint8_t* mpp = reinterpret_cast<uint8_t*>(sh + L.pp);                      // [2][32][MAXNB]
+    uint8_t* mppv = reinterpret_cast<uint8_t*>(sh + L.ppv);                    // [2][32][MAXNB]
+    uint8_t* mself = reinterpret_cast<uint8_t*>(sh + L.self);                  // [2][32]
+    int* ctl = reinterpret_cast<int*>(sh + L.ctl);                             // [2][2], bad
     const int r = blockIdx.x;
     if (r >= R) return;
-    const int lane = threadIdx.x;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int8_t* gs = spins + (int64_t)r * n * P;
-    for (int64_t t = lane; t < (int64_t)n * P; t += 32) s[t] = gs[t];
-    for (int t = lane; t < n; t += 32) pos_of[t] = 0xFF;
-    __syncwarp();
-    const int32_t* pr = perms + (int64_t)r * nsched * mcsteps * nperm;
-    const int32_t* rr = rands + (int64_t)r * rand_stride;
-    const int64_t cap = rand_stride;
-    int64_t used = 0;
-    UniformRing ring;
-    ring.init(rr, cap, lane);
-    const float rl = quick_scale(temp);
-    bool bad = false, dead = false;
+    for (int64_t t = threadIdx.x; t < (int64_t)n * P; t += 64) s[t] = gs[t];
+    for (int t = threadIdx.x; t < 2 * n; t += 64) pos_of[t] = 0xFF;
+    if (threadIdx.x < 5) ctl[threadIdx.x] = 0;
+    __syncthreads();
     const int nblk = (nperm + 31) / 32;
     const int64_t total = (int64_t)nsched * mcsteps * P * nblk;   // blocks in the whole run
-
-    // This lane's inputs arrive in two steps, so that no load waits on another inside
-    // a block: its permutation entry two blocks ahead, its neighbour row one block ahead
-    // (from the entry loaded a block earlier).
-    // The block whose entry is loaded next is tracked by counters (permutation, slice,
-    // block within the permutation) stepped once per block: no 64-bit division.  The
-    // load is unconditional from a valid address (entry 0 stands in past the end).
-    int64_t q_sweep = 0;
-    int q_k = 0, q_blk = 0;
     const int64_t nsweeps = (int64_t)nsched * mcsteps;
-    auto perm_next = [&](bool& has) -> int {
-        const int t = q_blk * 32 + lane;
-        has = q_sweep < nsweeps && t < nperm;
-        const int v = __ldg(pr + (has ? q_sweep * nperm + t : 0));
-        if (++q_blk == nblk) {
-            q_blk = 0;
-            if (++q_k == P) { q_k = 0; ++q_sweep; }
-        }
-        return v;
-    };
-    auto rows_of = [&](bool has, int i, RefBlockIn<FP64, MAXNB>& in) {
-        in.i = -1;
-        if (!has) return;
-        if ((unsigned)i >= (unsigned)n) { bad = true; i = 0; }
-        in.i = i;
-#pragma unroll
-        for (int m = 0; m < MAXNB; ++m) {
-            in.j[m] = __ldg(nb_idx + (int64_t)i * maxnb + m);
-            in.v[m] = __ldg(nb_j + (int64_t)i * maxnb + m);
-        }
-    };
-    RefBlockIn<FP64, MAXNB> cur, nxt;
-    bool p_has = false;
-    int p_next = 0;
+    auto tl_of = [&](int k) { return (flags & PQ_FIX_Q1) ? (k == 0 ? P - 1 : k - 1) : P - 1; };   // Q1 as shipped:
+    auto tr_of = [&](int k) { return (flags & PQ_FIX_Q1) ? (k == P - 1 ? 0 : k + 1) : 1; };       // P - 1 and 1
+    bool dead = false;
+    int64_t used = 0;
     if (total > 0) {
-        p_next = perm_next(p_has);   // block 0
-        rows_of(p_has, p_next, cur);
-        p_next = perm_next(p_has);   // block 1
-    }
-    int64_t b = 0;
-    for (int g = 0; g < nsched && total > 0 && !dead; ++g) {
-        const float jpf = jperp[g];
-        for (int step = 0; step < mcsteps && !dead; ++step) {
-            for (int k = 0; k < P && !dead; ++k) {
-                int tl = P - 1, tr = 1;   // Q1 as shipped (piqmc/qmc.pyx:115-117)
-                if (flags & PQ_FIX_Q1) { tl = k == 0 ? P - 1 : k - 1; tr = k == P - 1 ? 0 : k + 1; }
-                float ediff = 0.0f;       // Q2 as shipped: reset once per slice (piqmc/qmc.pyx:134-135)
-                for (int blk = 0; blk < nblk && !dead; ++blk, ++b) {
-                    rows_of(p_has, p_next, nxt);     // block b + 1
-                    p_next = perm_next(p_has);       // block b + 2
-                    const int nb = min(32, nperm - blk * 32);
-                    const int i = cur.i;
-                    if (lane < nb) pos_of[i] = (uint8_t)lane;
-                    __syncwarp();
-                    // this lane's position: its terms (signed couplings, or with FP32 the
-                    // exact products s2 v), which earlier positions of the block they depend on
-                    // (dep, pp) -- kept in registers and published in rec for the walk
-                    float x[8];
-                    uint8_t pp[MAXNB];
-                    uint32_t dep = 0;
+        if (warp == 1) {
+            // ---- fold warp ----
+            const int32_t* pr = perms + (int64_t)r * nsched * mcsteps * nperm;
+            bool bad = false;
+            int64_t q_sweep = 0;
+            int q_k = 0, q_blk = 0;
+            auto perm_next = [&](bool& has) -> int {
+                const int t = q_blk * 32 + lane;
+                has = q_sweep < nsweeps && t < nperm;
+                const int v = __ldg(pr + (has ? q_sweep * nperm + t : 0));
+                if (++q_blk == nblk) {
+                    q_blk = 0;
+                    if (++q_k == P) { q_k = 0; ++q_sweep; }
+                }
+                return v;
+            };
+            auto rows_of = [&](bool has, int i, RefBlockIn<FP64, MAXNB>& in) {
+                in.i = -1;
+                if (!has) return;
+                if ((unsigned)i >= (unsigned)n) { bad = true; i = 0; }
+                in.i = i;
 #pragma unroll
-                    for (int m = 0; m < 8; ++m) x[m] = 0.0f;
+                for (int m = 0; m < MAXNB; ++m) {
+                    in.j[m] = __ldg(nb_idx + (int64_t)i * maxnb + m);
+                    in.v[m] = __ldg(nb_j + (int64_t)i * maxnb + m);
+                }
+            };
+            // fold block f (rows in `in`) into buffer fb; the block resolved meanwhile has
+            // its positions in pos_of[pb] and slice kp (kp < 0: none)
+            auto fold = [&](const SparseBlk& f, const RefBlockIn<FP64, MAXNB>& in, int fb, int pb, int kp) {
+                const int nb = min(32, nperm - f.blk * 32);
+                const int k = f.k, tl = tl_of(k), tr = tr_of(k);
+                const float jpf = jperp[f.g];
+                const int i = in.i;
+                uint8_t* po = pos_of + (size_t)fb * n;
+                const uint8_t* pv = pos_of + (size_t)pb * n;
+                if (lane < nb) po[i] = (uint8_t)lane;
+                __syncwarp();
+                float x[8];
+                uint8_t pp[MAXNB], ppv[MAXNB];
+                uint32_t dep = 0;
 #pragma unroll
-                    for (int m = 0; m < MAXNB; ++m) pp[m] = 0xFF;
-                    if (lane < nb) {
-                        const int8_t* si_p = s + (int64_t)i * P;
+                for (int m = 0; m < 8; ++m) x[m] = 0.0f;
 #pragma unroll
-                        for (int m = 0; m < MAXNB; ++m) {
-                            int j = cur.j[m];
-                            if ((unsigned)j >= (unsigned)n) { bad = true; j = i; }
-                            float v = cur.v[m];
-                            if (j != i) {
-                                if (s[(int64_t)j * P + k] <= 0) v = -v;
-                                const uint8_t q = pos_of[j];
-                                if (q < lane) { pp[m] = q; dep |= 1u << q; }
-                            }
-                            x[m] = v;
+                for (int m = 0; m < MAXNB; ++m) { pp[m] = 0xFF; ppv[m] = 0xFF; }
+                uint8_t self = 0xFF;
+                if (lane < nb) {
+                    const int8_t* si_p = s + (int64_t)i * P;
+#pragma unroll
+                    for (int m = 0; m < MAXNB; ++m) {
+                        int j = in.j[m];
+                        if ((unsigned)j >= (unsigned)n) { bad = true; j = i; }
+                        float v = in.v[m];
+                        if (j != i) {
+                            if (s[(int64_t)j * P + k] <= 0) v = -v;
+                            const uint8_t q = po[j];
+                            if (q < lane) { pp[m] = q; dep |= 1u << q; }
+                            if (kp == k) ppv[m] = pv[j];
                         }
-                        x[MAXNB] = si_p[tl] > 0 ? jpf : -jpf;
-                        x[MAXNB + 1] = si_p[tr] > 0 ? jpf : -jpf;
-                        x[MAXNB + 2] = -2.0f * (float)si_p[k];
-                        if constexpr (!FP64) {
-                            // the FP32 path stores the terms s2 v themselves (exact: no 2J overflows here)
+                        x[m] = v;
+                    }
+                    if (kp >= 0) self = pv[i];
+                    x[MAXNB] = si_p[tl] > 0 ? jpf : -jpf;
+                    x[MAXNB + 1] = si_p[tr] > 0 ? jpf : -jpf;
+                    x[MAXNB + 2] = -2.0f * (float)si_p[k];
+                    if constexpr (!FP64) {
 #pragma unroll
-                            for (int m = 0; m < MAXNB + 2; ++m) x[m] = __fmul_rn(x[MAXNB + 2], x[m]);
+                        for (int m = 0; m < MAXNB + 2; ++m) x[m] = __fmul_rn(x[MAXNB + 2], x[m]);
+                    }
+                }
+                float4* rc = rec + (size_t)fb * 66;
+                rc[2 * lane] = make_float4(x[0], x[1], x[2], x[3]);
+                rc[2 * lane + 1] = make_float4(x[4], x[5], x[6], x[7]);
+                mdep[fb * 32 + lane] = dep;
+#pragma unroll
+                for (int m = 0; m < MAXNB; ++m) {
+                    mpp[(fb * 32 + lane) * MAXNB + m] = pp[m];
+                    mppv[(fb * 32 + lane) * MAXNB + m] = ppv[m];
+                }
+                mself[fb * 32 + lane] = self;
+                __syncwarp();
+            };
+            RefBlockIn<FP64, MAXNB> cur, nxt;
+            bool p_has = false;
+            int p_next = perm_next(p_has);   // block 0
+            rows_of(p_has, p_next, cur);
+            p_next = perm_next(p_has);       // block 1
+            rows_of(p_has, p_next, nxt);
+            p_next = perm_next(p_has);       // block 2
+            SparseBlk held{0, 0, 0, 0};      // the block the chain warp resolves
+            fold(held, cur, 0, 1, -1);
+            int held_i = cur.i;
+            pair_barrier();                  // block 0 is folded
+            for (int64_t bb = 0; bb < total; ++bb) {
+                SparseBlk f = held;
+                f.next(nblk, P, mcsteps);
+                int fold_i = -1;
+                if (bb + 1 < total) {
+                    fold(f, nxt, (int)((bb + 1) & 1), (int)(bb & 1), held.k);
+                    fold_i = nxt.i;
+                    cur = nxt;
+                    rows_of(p_has, p_next, nxt);   // block bb + 2
+                    p_next = perm_next(p_has);     // block bb + 3
+                }
+                pair_barrier();                    // the chain warp has resolved block bb
+                const int* c = ctl + 2 * (int)(bb & 1);
+                const uint32_t fm = (uint32_t)c[0];   // the decisions that stand, also in a block
+                const int nb = min(32, nperm - held.blk * 32);   // the stream ran out in
+                if (lane < nb) {
+                    if ((fm >> lane) & 1u) s[(int64_t)held_i * P + held.k] = (int8_t)-s[(int64_t)held_i * P + held.k];
+                    pos_of[(size_t)(bb & 1) * n + held_i] = 0xFF;
+                }
+                __syncwarp();
+                if (c[1]) break;
+                held = f;
+                held_i = fold_i;
+            }
+            bad = __any_sync(0xffffffffu, bad);
+            if (lane == 0 && bad) ctl[4] = 1;
+        } else {
+            // ---- chain warp ----
+            const int64_t cap = rand_stride;
+            UniformRing ring;
+            ring.init(rands + (int64_t)r * rand_stride, cap, lane);
+            const float rl = quick_scale(temp);
+            SparseBlk cb{0, 0, 0, 0};
+            uint32_t fm_prev = 0;
+            int k_prev = -1;
+            float ediff = 0.0f;
+            pair_barrier();                  // block 0 is folded
+            for (int64_t bb = 0; bb < total; ++bb) {
+                const int buf = (int)(bb & 1);
+                const int nb = min(32, nperm - cb.blk * 32);
+                const int k = cb.k, tl = tl_of(k), tr = tr_of(k);
+                if (cb.blk == 0) ediff = 0.0f;   // Q2 as shipped: reset once per slice (piqmc/qmc.pyx:134-135)
+                float4* rc = rec + (size_t)buf * 66;
+                const float4 r0 = rc[2 * lane], r1 = rc[2 * lane + 1];
+                float x[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
+                const uint32_t dep = mdep[buf * 32 + lane];
+                uint8_t pp[MAXNB];
+#pragma unroll
+                for (int m = 0; m < MAXNB; ++m) pp[m] = mpp[(buf * 32 + lane) * MAXNB + m];
+                // the previous block's flips, folded into this block's terms
+                if (lane < nb && fm_prev) {
+                    bool ch = false;
+#pragma unroll
+                    for (int m = 0; m < MAXNB; ++m) {
+                        const uint8_t q = mppv[(buf * 32 + lane) * MAXNB + m];
+                        if (q != 0xFF && ((fm_prev >> q) & 1u)) { x[m] = -x[m]; ch = true; }
+                    }
+                    const uint8_t q = mself[buf * 32 + lane];
+                    if (q != 0xFF && ((fm_prev >> q) & 1u)) {
+                        if (k_prev == tl) { x[MAXNB] = -x[MAXNB]; ch = true; }
+                        if (k_prev == tr) { x[MAXNB + 1] = -x[MAXNB + 1]; ch = true; }
+                    }
+                    if (ch) {
+                        rc[2 * lane] = make_float4(x[0], x[1], x[2], x[3]);
+                        rc[2 * lane + 1] = make_float4(x[4], x[5], x[6], x[7]);
+                    }
+                }
+                __syncwarp();
+                uint32_t flipmask = 0;
+                uint32_t applied = 0;
+                int cc = 0;
+                float my_e = 0.0f;
+                int my_c = 0;
+                int l = 0;
+                int stop = 0;
+                while (l < nb) {
+                    const int start = l;
+                    if (lane >= start && lane < nb) {
+                        const uint32_t nf = dep & flipmask & ~applied;
+                        if (nf) {
+#pragma unroll
+                            for (int m = 0; m < MAXNB; ++m)
+                                if (pp[m] != 0xFF && ((nf >> pp[m]) & 1u)) x[m] = -x[m];
+                            rc[2 * lane] = make_float4(x[0], x[1], x[2], x[3]);
+                            rc[2 * lane + 1] = make_float4(x[4], x[5], x[6], x[7]);
+                            applied |= nf;
                         }
-                        rec[2 * lane] = make_float4(x[0], x[1], x[2], x[3]);
-                        rec[2 * lane + 1] = make_float4(x[4], x[5], x[6], x[7]);
                     }
                     __syncwarp();
-                    uint32_t flipmask = 0;   // flips of this block that stand
-                    uint32_t applied = 0;    // of those, the ones already folded into this lane's terms
-                    int c = 0;               // uniforms consumed in this block so far
-                    float my_e = 0.0f;       // this lane's position: its sum ...
-                    int my_c = 0;            // ... and the uniforms consumed before it
-                    int l = 0;
-                    while (l < nb) {
-                        const int start = l;
-                        // open positions fold in the flips that stand (a flipped neighbour's term
-                        // is the exact negation)
-                        if (lane >= start && lane < nb) {
-                            const uint32_t nf = dep & flipmask & ~applied;
-                            if (nf) {
+                    float4 ra = rc[2 * l], rb = rc[2 * l + 1];
+                    for (; l < nb; ++l) {
+                        const float4 ra_n = rc[2 * l + 2], rb_n = rc[2 * l + 3];
+                        const float y[8] = {ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w};
+                        ra = ra_n;
+                        rb = rb_n;
+                        if (FIXQ2) ediff = 0.0f;
+                        if constexpr (FP64) {
+                            const float s2 = y[MAXNB + 2];
 #pragma unroll
-                                for (int m = 0; m < MAXNB; ++m)
-                                    if (pp[m] != 0xFF && ((nf >> pp[m]) & 1u)) x[m] = -x[m];
-                                rec[2 * lane] = make_float4(x[0], x[1], x[2], x[3]);
-                                rec[2 * lane + 1] = make_float4(x[4], x[5], x[6], x[7]);
-                                applied |= nf;
-                            }
+                            for (int m = 0; m < MAXNB + 2; ++m) ediff = acc2<true>(ediff, s2, y[m]);
+                        } else {
+#pragma unroll
+                            for (int m = 0; m < MAXNB + 2; ++m) ediff = __fadd_rn(ediff, y[m]);
                         }
-                        __syncwarp();
-                        // walk every open position, taking its undecided in-block neighbours as
-                        // not flipping; records of position l + 1 are read while l's sum is chained
-                        float4 ra = rec[2 * l], rb = rec[2 * l + 1];
-                        for (; l < nb; ++l) {
-                            const float4 ra_n = rec[2 * l + 2], rb_n = rec[2 * l + 3];
-                            const float y[8] = {ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w};
-                            ra = ra_n;
-                            rb = rb_n;
-                            if (FIXQ2) ediff = 0.0f;
-                            if constexpr (FP64) {
-                                const float s2 = y[MAXNB + 2];
-#pragma unroll
-                                for (int m = 0; m < MAXNB + 2; ++m) ediff = acc2<true>(ediff, s2, y[m]);
+                        if (lane == l) { my_e = ediff; my_c = cc; }
+                        cc += ediff > 0.0f ? 0 : 1;
+                    }
+                    const int32_t rv = ring.get(used + my_c);
+                    bool flip = false, out = false, miss = false;
+                    float xf = 0.0f;
+                    if (lane >= start && lane < nb) {
+                        if (my_e > 0.0f) {
+                            flip = true;
+                        } else if (used + my_c >= cap) {
+                            out = true;
+                        } else {
+                            const int fast = rl != 0.0f ? quick_decide(my_e, rl, rv) : -1;
+                            if (fast >= 0) {
+                                flip = fast != 0;
                             } else {
-#pragma unroll
-                                for (int m = 0; m < MAXNB + 2; ++m) ediff = __fadd_rn(ediff, y[m]);
-                            }
-                            if (lane == l) { my_e = ediff; my_c = c; }
-                            c += ediff > 0.0f ? 0 : 1;
-                        }
-                        // decisions of positions [start, nb), one per lane
-                        const int32_t rv = ring.get(used + my_c);
-                        bool flip = false, out = false, miss = false;
-                        float xf = 0.0f;
-                        if (lane >= start && lane < nb) {
-                            if (my_e > 0.0f) {
-                                flip = true;
-                            } else if (used + my_c >= cap) {
-                                out = true;
-                            } else {
-                                const int fast = rl != 0.0f ? quick_decide(my_e, rl, rv) : -1;
-                                if (fast >= 0) {
-                                    flip = fast != 0;
+                                xf = __fdiv_rn(my_e, temp);
+                                const int quick = fp32_decide(xf, rv);
+                                if (quick >= 0) {
+                                    flip = quick != 0;
                                 } else {
-                                    xf = __fdiv_rn(my_e, temp);
-                                    const int quick = fp32_decide(xf, rv);
-                                    if (quick >= 0) {
-                                        flip = quick != 0;
-                                    } else {
-                                        const double q = (double)rv / 2147483647.0;   // glibc RAND_MAX
-                                        flip = patched_exp(xf, q, ep, &miss) > q;
-                                    }
+                                    const double q = (double)rv / 2147483647.0;   // glibc RAND_MAX
+                                    flip = patched_exp(xf, q, ep, &miss) > q;
                                 }
                             }
                         }
-                        // the walk stands up to the first position whose in-block neighbour
-                        // flipped in this round; from there it is taken again
-                        const uint32_t fl = __ballot_sync(0xffffffffu, flip);
-                        const uint32_t wrong = __ballot_sync(0xffffffffu, lane > start && lane < nb && (dep & fl));
-                        const int p = wrong ? __ffs(wrong) - 1 : nb;
-                        if (__any_sync(0xffffffffu, out && lane < p)) {
-                            if (lane == 0) pq_set_status(status, PQ_ERR_RAND_EXHAUSTED);
-                            dead = true;
-                            break;
-                        }
-                        if (miss && lane < p) record_close(ep, xf, exp((double)xf));
-                        flipmask |= fl & (p >= 32 ? 0xffffffffu : ((1u << p) - 1u));
-                        if (p < nb) {
-                            ediff = __shfl_sync(0xffffffffu, my_e, p - 1);   // the chain before position p
-                            c = __shfl_sync(0xffffffffu, my_c, p);           // the uniforms consumed before p
-                            l = p;
-                        }
                     }
-                    used += c;
-                    ring.advance(used, lane);
-                    if (lane < nb) {
-                        if ((flipmask >> lane) & 1u) s[(int64_t)i * P + k] = (int8_t)-s[(int64_t)i * P + k];
-                        pos_of[i] = 0xFF;
+                    const uint32_t fl = __ballot_sync(0xffffffffu, flip);
+                    const uint32_t wrong = __ballot_sync(0xffffffffu, lane > start && lane < nb && (dep & fl));
+                    const int p = wrong ? __ffs(wrong) - 1 : nb;
+                    if (__any_sync(0xffffffffu, out && lane < p)) {
+                        if (lane == 0) pq_set_status(status, PQ_ERR_RAND_EXHAUSTED);
+                        dead = true;
+                        stop = 1;
+                        break;
                     }
-                    __syncwarp();
-                    cur = nxt;
+                    if (miss && lane < p) record_close(ep, xf, exp((double)xf));
+                    flipmask |= fl & (p >= 32 ? 0xffffffffu : ((1u << p) - 1u));
+                    if (p < nb) {
+                        ediff = __shfl_sync(0xffffffffu, my_e, p - 1);
+                        cc = __shfl_sync(0xffffffffu, my_c, p);
+                        l = p;
+                    }
                 }
+                if (!stop) {
+                    used += cc;
+                    ring.advance(used, lane);
+                }
+                if (lane == 0) { ctl[2 * buf] = (int)flipmask; ctl[2 * buf + 1] = stop; }
+                pair_barrier();                  // the fold warp has folded block bb + 1
+                if (stop) break;
+                fm_prev = flipmask;
+                k_prev = k;
+                cb.next(nblk, P, mcsteps);
             }
         }
     }
-    bad = __any_sync(0xffffffffu, bad);   // each lane saw its own positions' indices
-    if (lane == 0) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const bool bad = ctl[4] != 0;
         if (bad) pq_set_status(status, PQ_ERR_BAD_INDEX);
         rand_used[r] = (dead || bad) ? -1 : used;
     }
-    __syncwarp();
-    for (int64_t t = lane; t < (int64_t)n * P; t += 32) gs[t] = s[t];
+    for (int64_t t = threadIdx.x; t < (int64_t)n * P; t += 64) gs[t] = s[t];
 }
 
 __global__ void qa_dense_reforder_kernel(int8_t* __restrict__ spins, const double* __restrict__ J, int n,
@@ -956,8 +1070,6 @@ __host__ __device__ inline size_t dense_pair_smem(int n, int P) {
            2 * dense_warp_align16((size_t)4 * (n + 12)) + dense_warp_align16((size_t)n) + 16;
 }
 
-__device__ __forceinline__ void pair_barrier() { asm volatile("bar.sync 1, 64;" ::: "memory"); }
-
 template <bool QA>
 __global__ void __launch_bounds__(64) dense_reforder_pair_kernel(
     int8_t* __restrict__ spins, const double* __restrict__ J, int n, int P, int R,
@@ -1384,28 +1496,23 @@ int launch_qa_sparse_t(int8_t* spins, const int32_t* nb_idx, const float* nb_j, 
 }
 
 template <bool FP64, int MAXNB>
-size_t warp_kernel_smem(int n, int P) {
-    return (((size_t)n * P + 15) & ~(size_t)15) + (((size_t)n + 15) & ~(size_t)15) + 33 * 32;
-}
-
-template <bool FP64, int MAXNB>
 int launch_qa_sparse_s(int8_t* spins, const int32_t* nb_idx, const float* nb_j, int n, int nperm, int maxnb, int P,
                        int R, const float* jperp, int nsched, int mcsteps, float temp, const int32_t* perms,
                        const int32_t* rands, int64_t rand_stride, int64_t* rand_used, int flags, const ExpPatch& ep,
                        int32_t* status, cudaStream_t stream) {
     if constexpr (MAXNB > 0) {
-        const size_t smem = warp_kernel_smem<FP64, MAXNB>(n, P);
-        if (smem <= kRefSmemMax + 8192) {
+        const size_t psmem = SparsePairLayout<MAXNB>(n, P).total;
+        if (psmem <= kRefSmemMax + 8192) {
             if (flags & PQ_FIX_Q2) {
-                PQ_CUDA_TRY(cudaFuncSetAttribute(qa_sparse_reforder_warp_kernel<FP64, MAXNB, true>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-                qa_sparse_reforder_warp_kernel<FP64, MAXNB, true><<<R, 32, smem, stream>>>(
+                PQ_CUDA_TRY(cudaFuncSetAttribute(qa_sparse_reforder_pair_kernel<FP64, MAXNB, true>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
+                qa_sparse_reforder_pair_kernel<FP64, MAXNB, true><<<R, 64, psmem, stream>>>(
                     spins, nb_idx, nb_j, n, nperm, maxnb, P, R, jperp, nsched, mcsteps, temp, perms, rands,
                     rand_stride, rand_used, flags, ep, status);
             } else {
-                PQ_CUDA_TRY(cudaFuncSetAttribute(qa_sparse_reforder_warp_kernel<FP64, MAXNB, false>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-                qa_sparse_reforder_warp_kernel<FP64, MAXNB, false><<<R, 32, smem, stream>>>(
+                PQ_CUDA_TRY(cudaFuncSetAttribute(qa_sparse_reforder_pair_kernel<FP64, MAXNB, false>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
+                qa_sparse_reforder_pair_kernel<FP64, MAXNB, false><<<R, 64, psmem, stream>>>(
                     spins, nb_idx, nb_j, n, nperm, maxnb, P, R, jperp, nsched, mcsteps, temp, perms, rands,
                     rand_stride, rand_used, flags, ep, status);
             }
