@@ -88,7 +88,7 @@ __device__ __forceinline__ int fp32_decide(float xf, int32_t rv) {
     return -1;
 }
 
-// The same decision from a cheaper estimate, for the warp kernels: x' = e * rl with
+// The same decision from a cheaper estimate, for the warp-level kernels: x' = e * rl with
 // rl = fl(fl(1 / T) * fl(log2 e)) (set once per temperature) and 2^x' by ex2.approx.
 // Against exp((double)fl(e / T)) the estimate errs by under 5e-5 (relative) wherever
 // exp > 1e-30: ex2.approx of a once-rounded argument is within 2e-5 of expf_neg there
