@@ -810,193 +810,6 @@ __global__ void sa_bipartite_reforder_kernel(int8_t* __restrict__ spins, const d
     rand_used[r] = rng.used;
 }
 
-// sa.Anneal with the warp sharing the work (spins in shared memory, maxnb <= 8).
-// The energy difference is reset for every spin (piqmc/sa.pyx:119), so the sums
-// of a block's 32 positions are independent except through neighbours flipped
-// earlier in the same block.  Each pass takes every open position, with in-block
-// neighbours still undecided taken as not flipping: their sums are computed in
-// parallel (each lane its own FP32 chain in the reference's term order), the
-// uniforms they consume are numbered by a ballot prefix count (a position consumes
-// one when ediff < 0, :114-117), and they decide in parallel with ref_accept's
-// arithmetic.  The decisions stand up to the first position with an in-block
-// neighbour that flipped in the pass, where the next pass starts.  Same results,
-// uniforms and close calls as sa_sparse_reforder_kernel.
-template <bool FP64>
-__global__ void __launch_bounds__(32) sa_sparse_reforder_warp_kernel(
-    int8_t* __restrict__ spins, const int32_t* __restrict__ nb_idx, const float* __restrict__ nb_j, int n, int maxnb,
-    int R, const float* __restrict__ temps, int nsched, int mcsteps, const int32_t* __restrict__ perms,
-    const int32_t* __restrict__ rands, int64_t rand_stride, int64_t* __restrict__ rand_used, ExpPatch ep,
-    int32_t* status) {
-    constexpr int MAXNB = 8;
-    extern __shared__ __align__(16) int8_t sh[];
-    int8_t* s = sh;                                                                      // [n]
-    uint8_t* pos_of = reinterpret_cast<uint8_t*>(sh + (((size_t)n + 15) & ~(size_t)15));  // [n]
-    const int r = blockIdx.x;
-    if (r >= R) return;
-    const int lane = threadIdx.x;
-    int8_t* gs = spins + (int64_t)r * n;
-    for (int t = lane; t < n; t += 32) { s[t] = gs[t]; pos_of[t] = 0xFF; }
-    __syncwarp();
-    const int32_t* pr = perms + (int64_t)r * nsched * mcsteps * n;
-    const int32_t* rr = rands + (int64_t)r * rand_stride;
-    const int64_t cap = rand_stride;
-    int64_t used = 0;
-    UniformRing ring;
-    ring.init(rr, cap, lane);
-    bool bad = false, dead = false;
-    const int nblk = (n + 31) / 32;
-    const int64_t total = (int64_t)nsched * mcsteps * nblk;
-    struct In { int i; int j[MAXNB]; float v[MAXNB]; };
-    // permutation entry two blocks ahead, neighbour row one block ahead (see the QA kernel)
-    int64_t q_sweep = 0;
-    int q_blk = 0;
-    const int64_t nsweeps = (int64_t)nsched * mcsteps;
-    auto perm_next = [&](bool& has) -> int {
-        const int t = q_blk * 32 + lane;
-        has = q_sweep < nsweeps && t < n;
-        const int v = __ldg(pr + (has ? q_sweep * n + t : 0));
-        if (++q_blk == nblk) { q_blk = 0; ++q_sweep; }
-        return v;
-    };
-    auto rows_of = [&](bool has, int i, In& in) {
-        in.i = -1;
-        if (!has) return;
-        if ((unsigned)i >= (unsigned)n) { bad = true; i = 0; }
-        in.i = i;
-        if (maxnb <= 0) {
-#pragma unroll
-            for (int m = 0; m < MAXNB; ++m) { in.j[m] = i; in.v[m] = 0.0f; }
-            return;
-        }
-        // entries m >= maxnb repeat the last one: the fold never reads them
-#pragma unroll
-        for (int m = 0; m < MAXNB; ++m) {
-            const int mm = m < maxnb ? m : maxnb - 1;
-            in.j[m] = __ldg(nb_idx + (int64_t)i * maxnb + mm);
-            in.v[m] = __ldg(nb_j + (int64_t)i * maxnb + mm);
-        }
-    };
-    In cur, nxt;
-    bool p_has = false;
-    int p_next = 0;
-    if (total > 0) {
-        p_next = perm_next(p_has);   // block 0
-        rows_of(p_has, p_next, cur);
-        p_next = perm_next(p_has);   // block 1
-    }
-    int64_t b = 0;
-    for (int g = 0; g < nsched && total > 0 && !dead; ++g) {
-        const float temp = temps[g];
-        const float rl = quick_scale(temp);
-        for (int step = 0; step < mcsteps && !dead; ++step) {
-            for (int blk = 0; blk < nblk && !dead; ++blk, ++b) {
-                rows_of(p_has, p_next, nxt);     // block b + 1
-                p_next = perm_next(p_has);       // block b + 2
-                const int nb = min(32, n - blk * 32);
-                const int i = cur.i;
-                if (lane < nb) pos_of[i] = (uint8_t)lane;
-                __syncwarp();
-                float x[MAXNB];
-                uint8_t pp[MAXNB];
-                uint32_t dep = 0;
-                float s2 = 0.0f;
-                if (lane < nb) {
-                    s2 = -2.0f * (float)s[i];
-#pragma unroll
-                    for (int m = 0; m < MAXNB; ++m) {
-                        int j = cur.j[m];
-                        float v = cur.v[m];
-                        pp[m] = 0xFF;
-                        if (m < maxnb && j != i) {
-                            if ((unsigned)j >= (unsigned)n) { bad = true; j = i; }
-                            else {
-                                if (s[j] <= 0) v = -v;
-                                const uint8_t q = pos_of[j];
-                                if (q < lane) { pp[m] = q; dep |= 1u << q; }
-                            }
-                        }
-                        x[m] = v;
-                    }
-                }
-                uint32_t flipmask = 0;   // flips of this block that stand
-                int c = 0;
-                int start = 0;
-                while (start < nb) {
-                    // every open position sums its terms; in-block neighbours still undecided
-                    // are taken as not flipping (checked below)
-                    const bool mine = lane >= start && lane < nb;
-                    float ediff = 0.0f;
-                    if (mine) {
-#pragma unroll
-                        for (int m = 0; m < MAXNB; ++m) {
-                            if (m < maxnb) {
-                                const float v = (pp[m] != 0xFF && ((flipmask >> pp[m]) & 1u)) ? -x[m] : x[m];
-                                ediff = acc2<FP64>(ediff, s2, v);
-                            }
-                        }
-                    }
-                    const bool consume = mine && !(ediff >= 0.0f);
-                    const uint32_t cons = __ballot_sync(0xffffffffu, consume);
-                    const int my_c = c + __popc(cons & ((1u << lane) - 1u));
-                    const int32_t rv = ring.get(used + my_c);
-                    bool flip = false, out = false, miss = false;
-                    float xf = 0.0f;
-                    if (mine) {
-                        if (!consume) {
-                            flip = true;
-                        } else if (used + my_c >= cap) {
-                            out = true;
-                        } else {
-                            const int fast = rl != 0.0f ? quick_decide(ediff, rl, rv) : -1;
-                            if (fast >= 0) {
-                                flip = fast != 0;
-                            } else {
-                                xf = __fdiv_rn(ediff, temp);
-                                const int quick = fp32_decide(xf, rv);
-                                if (quick >= 0) {
-                                    flip = quick != 0;
-                                } else {
-                                    const double q = (double)rv / 2147483647.0;   // glibc RAND_MAX
-                                    flip = patched_exp(xf, q, ep, &miss) > q;
-                                }
-                            }
-                        }
-                    }
-                    // decisions stand up to the first position with an in-block neighbour that
-                    // flipped in this pass; the next pass starts there
-                    const uint32_t fl = __ballot_sync(0xffffffffu, flip);
-                    const uint32_t wrong = __ballot_sync(0xffffffffu, lane > start && lane < nb && (dep & fl));
-                    const int p = wrong ? __ffs(wrong) - 1 : nb;
-                    const uint32_t keep = p >= 32 ? 0xffffffffu : ((1u << p) - 1u);
-                    if (__any_sync(0xffffffffu, out && lane < p)) {
-                        if (lane == 0) pq_set_status(status, PQ_ERR_RAND_EXHAUSTED);
-                        dead = true;
-                        break;
-                    }
-                    if (miss && lane < p) record_close(ep, xf, exp((double)xf));
-                    flipmask |= fl & keep;
-                    c += __popc(cons & keep);
-                    start = p;
-                }
-                used += c;
-                ring.advance(used, lane);
-                if (lane < nb) {
-                    if ((flipmask >> lane) & 1u) s[i] = (int8_t)-s[i];
-                    pos_of[i] = 0xFF;
-                }
-                __syncwarp();
-                cur = nxt;
-            }
-        }
-    }
-    bad = __any_sync(0xffffffffu, bad);
-    if (lane == 0) {
-        if (bad) pq_set_status(status, PQ_ERR_BAD_INDEX);
-        rand_used[r] = (dead || bad) ? -1 : used;
-    }
-    __syncwarp();
-    for (int t = lane; t < n; t += 32) gs[t] = s[t];
-}
 
 // Dense reference-order sweeps (QuantumAnneal_dense, piqmc/qmc.pyx:181-242, and
 // sa.Anneal_dense, piqmc/sa.pyx:126-187) by warps: for each position of the
@@ -1458,6 +1271,294 @@ __global__ void __launch_bounds__(32) sa_bipartite_reforder_warp_kernel(
     for (int t = lane; t < nl + nr; t += 32) gs[t] = sh[t];
 }
 
+// sa.Anneal with warps sharing the work (spins in shared memory, maxnb <= 8).
+// The energy difference is reset for every spin (piqmc/sa.pyx:119), so the sums
+// of a block's 32 positions are independent except through neighbours flipped
+// earlier in the same block.  Each pass takes every open position, with in-block
+// neighbours still undecided taken as not flipping: their sums are computed in
+// parallel (each lane its own FP32 chain in the reference's term order), the
+// uniforms they consume are numbered by a ballot prefix count (a position consumes
+// one when ediff < 0, :114-117), and they decide in parallel with ref_accept's
+// arithmetic.  The decisions stand up to the first position with an in-block
+// neighbour that flipped in the pass, where the next pass starts.
+// Two warps per replica, as in qa_sparse_reforder_pair_kernel: the fold warp prepares
+// block b + 1 (signed couplings, s2, in-block dependencies, and the positions in
+// block b of each neighbour and of the spin itself) while the chain warp resolves
+// block b; after the block barrier the chain warp negates exactly the couplings whose
+// neighbour flipped in block b, and s2 when the spin itself did (a new sweep can
+// revisit a spin of the previous block).  Same results, uniforms and close calls as
+// sa_sparse_reforder_kernel.
+struct SaPairLayout {
+    size_t pos_of, xs, s2, dep, pp, ppv, self, ctl, total;
+    __host__ __device__ explicit SaPairLayout(int n) {
+        auto a16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
+        pos_of = a16((size_t)n);                     // int8 spins [n], then uint8 [2][n]
+        xs = pos_of + a16((size_t)2 * n);            // float [2][32][8]
+        s2 = xs + (size_t)2 * 32 * 8 * 4;            // float [2][32]
+        dep = s2 + (size_t)2 * 32 * 4;               // uint32 [2][32]
+        pp = dep + (size_t)2 * 32 * 4;               // uint8 [2][32][8]
+        ppv = pp + (size_t)2 * 32 * 8;               // uint8 [2][32][8]
+        self = ppv + (size_t)2 * 32 * 8;             // uint8 [2][32]
+        ctl = self + 64;                             // int [2][2], bad
+        total = ctl + 32;
+    }
+};
+
+template <bool FP64>
+__global__ void __launch_bounds__(64) sa_sparse_reforder_pair_kernel(
+    int8_t* __restrict__ spins, const int32_t* __restrict__ nb_idx, const float* __restrict__ nb_j, int n, int maxnb,
+    int R, const float* __restrict__ temps, int nsched, int mcsteps, const int32_t* __restrict__ perms,
+    const int32_t* __restrict__ rands, int64_t rand_stride, int64_t* __restrict__ rand_used, ExpPatch ep,
+    int32_t* status) {
+    constexpr int MAXNB = 8;
+    extern __shared__ __align__(16) int8_t sh[];
+    const SaPairLayout L(n);
+    int8_t* s = sh;                                                          // [n]
+    uint8_t* pos_of = reinterpret_cast<uint8_t*>(sh + L.pos_of);             // [2][n]
+    float* mxs = reinterpret_cast<float*>(sh + L.xs);                        // [2][32][8]
+    float* ms2 = reinterpret_cast<float*>(sh + L.s2);                        // [2][32]
+    uint32_t* mdep = reinterpret_cast<uint32_t*>(sh + L.dep);                // [2][32]
+    uint8_t* mpp = reinterpret_cast<uint8_t*>(sh + L.pp);                    // [2][32][8]
+    uint8_t* mppv = reinterpret_cast<uint8_t*>(sh + L.ppv);                  // [2][32][8]
+    uint8_t* mself = reinterpret_cast<uint8_t*>(sh + L.self);                // [2][32]
+    int* ctl = reinterpret_cast<int*>(sh + L.ctl);                           // [2][2], bad
+    const int r = blockIdx.x;
+    if (r >= R) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int8_t* gs = spins + (int64_t)r * n;
+    for (int t = threadIdx.x; t < n; t += 64) s[t] = gs[t];
+    for (int t = threadIdx.x; t < 2 * n; t += 64) pos_of[t] = 0xFF;
+    if (threadIdx.x < 5) ctl[threadIdx.x] = 0;
+    __syncthreads();
+    const int nblk = (n + 31) / 32;
+    const int64_t total = (int64_t)nsched * mcsteps * nblk;
+    const int64_t nsweeps = (int64_t)nsched * mcsteps;
+    bool dead = false;
+    int64_t used = 0;
+    if (total > 0) {
+        if (warp == 1) {
+            // ---- fold warp ----
+            const int32_t* pr = perms + (int64_t)r * nsched * mcsteps * n;
+            bool bad = false;
+            struct In { int i; int j[MAXNB]; float v[MAXNB]; };
+            int64_t q_sweep = 0;
+            int q_blk = 0;
+            auto perm_next = [&](bool& has) -> int {
+                const int t = q_blk * 32 + lane;
+                has = q_sweep < nsweeps && t < n;
+                const int v = __ldg(pr + (has ? q_sweep * n + t : 0));
+                if (++q_blk == nblk) { q_blk = 0; ++q_sweep; }
+                return v;
+            };
+            auto rows_of = [&](bool has, int i, In& in) {
+                in.i = -1;
+                if (!has) return;
+                if ((unsigned)i >= (unsigned)n) { bad = true; i = 0; }
+                in.i = i;
+                if (maxnb <= 0) {
+#pragma unroll
+                    for (int m = 0; m < MAXNB; ++m) { in.j[m] = i; in.v[m] = 0.0f; }
+                    return;
+                }
+#pragma unroll
+                for (int m = 0; m < MAXNB; ++m) {   // entries m >= maxnb repeat the last one, never read
+                    const int mm = m < maxnb ? m : maxnb - 1;
+                    in.j[m] = __ldg(nb_idx + (int64_t)i * maxnb + mm);
+                    in.v[m] = __ldg(nb_j + (int64_t)i * maxnb + mm);
+                }
+            };
+            auto fold = [&](int blk, const In& in, int fb, int pb, bool has_prev) {
+                const int nb = min(32, n - blk * 32);
+                const int i = in.i;
+                uint8_t* po = pos_of + (size_t)fb * n;
+                const uint8_t* pv = pos_of + (size_t)pb * n;
+                if (lane < nb) po[i] = (uint8_t)lane;
+                __syncwarp();
+                float x[MAXNB];
+                uint8_t pp[MAXNB], ppv[MAXNB];
+                uint32_t dep = 0;
+                float s2 = 0.0f;
+                uint8_t self = 0xFF;
+#pragma unroll
+                for (int m = 0; m < MAXNB; ++m) { x[m] = 0.0f; pp[m] = 0xFF; ppv[m] = 0xFF; }
+                if (lane < nb) {
+                    s2 = -2.0f * (float)s[i];
+#pragma unroll
+                    for (int m = 0; m < MAXNB; ++m) {
+                        int j = in.j[m];
+                        float v = in.v[m];
+                        if (m < maxnb && j != i) {
+                            if ((unsigned)j >= (unsigned)n) { bad = true; j = i; }
+                            else {
+                                if (s[j] <= 0) v = -v;
+                                const uint8_t q = po[j];
+                                if (q < lane) { pp[m] = q; dep |= 1u << q; }
+                                if (has_prev) ppv[m] = pv[j];
+                            }
+                        }
+                        x[m] = v;
+                    }
+                    if (has_prev) self = pv[i];
+                }
+                const int o = fb * 32 + lane;
+#pragma unroll
+                for (int m = 0; m < MAXNB; ++m) {
+                    mxs[o * MAXNB + m] = x[m];
+                    mpp[o * MAXNB + m] = pp[m];
+                    mppv[o * MAXNB + m] = ppv[m];
+                }
+                ms2[o] = s2;
+                mdep[o] = dep;
+                mself[o] = self;
+                __syncwarp();
+            };
+            In cur, nxt;
+            bool p_has = false;
+            int p_next = perm_next(p_has);   // block 0
+            rows_of(p_has, p_next, cur);
+            p_next = perm_next(p_has);       // block 1
+            rows_of(p_has, p_next, nxt);
+            p_next = perm_next(p_has);       // block 2
+            int held_blk = 0;
+            fold(0, cur, 0, 1, false);
+            int held_i = cur.i;
+            pair_barrier();                  // block 0 is folded
+            for (int64_t bb = 0; bb < total; ++bb) {
+                const int fblk = held_blk + 1 == nblk ? 0 : held_blk + 1;
+                int fold_i = -1;
+                if (bb + 1 < total) {
+                    fold(fblk, nxt, (int)((bb + 1) & 1), (int)(bb & 1), true);
+                    fold_i = nxt.i;
+                    cur = nxt;
+                    rows_of(p_has, p_next, nxt);   // block bb + 2
+                    p_next = perm_next(p_has);     // block bb + 3
+                }
+                pair_barrier();                    // the chain warp has resolved block bb
+                const int* c = ctl + 2 * (int)(bb & 1);
+                const uint32_t fm = (uint32_t)c[0];
+                const int nb = min(32, n - held_blk * 32);
+                if (lane < nb) {
+                    if ((fm >> lane) & 1u) s[held_i] = (int8_t)-s[held_i];
+                    pos_of[(size_t)(bb & 1) * n + held_i] = 0xFF;
+                }
+                __syncwarp();
+                if (c[1]) break;
+                held_blk = fblk;
+                held_i = fold_i;
+            }
+            bad = __any_sync(0xffffffffu, bad);
+            if (lane == 0 && bad) ctl[4] = 1;
+        } else {
+            // ---- chain warp ----
+            const int64_t cap = rand_stride;
+            UniformRing ring;
+            ring.init(rands + (int64_t)r * rand_stride, cap, lane);
+            int blk = 0, g = 0, step = 0;
+            uint32_t fm_prev = 0;
+            pair_barrier();                  // block 0 is folded
+            for (int64_t bb = 0; bb < total; ++bb) {
+                const int buf = (int)(bb & 1);
+                const int nb = min(32, n - blk * 32);
+                const float temp = temps[g];
+                const float rl = quick_scale(temp);
+                const int o = buf * 32 + lane;
+                float x[MAXNB];
+                uint8_t pp[MAXNB];
+#pragma unroll
+                for (int m = 0; m < MAXNB; ++m) { x[m] = mxs[o * MAXNB + m]; pp[m] = mpp[o * MAXNB + m]; }
+                float s2 = ms2[o];
+                const uint32_t dep = mdep[o];
+                if (lane < nb && fm_prev) {   // the previous block's flips
+#pragma unroll
+                    for (int m = 0; m < MAXNB; ++m) {
+                        const uint8_t q = mppv[o * MAXNB + m];
+                        if (q != 0xFF && ((fm_prev >> q) & 1u)) x[m] = -x[m];
+                    }
+                    const uint8_t q = mself[o];
+                    if (q != 0xFF && ((fm_prev >> q) & 1u)) s2 = -s2;
+                }
+                uint32_t flipmask = 0;
+                int cc = 0;
+                int start = 0;
+                int stop = 0;
+                while (start < nb) {
+                    const bool mine = lane >= start && lane < nb;
+                    float ediff = 0.0f;
+                    if (mine) {
+#pragma unroll
+                        for (int m = 0; m < MAXNB; ++m) {
+                            if (m < maxnb) {
+                                const float v = (pp[m] != 0xFF && ((flipmask >> pp[m]) & 1u)) ? -x[m] : x[m];
+                                ediff = acc2<FP64>(ediff, s2, v);
+                            }
+                        }
+                    }
+                    const bool consume = mine && !(ediff >= 0.0f);
+                    const uint32_t cons = __ballot_sync(0xffffffffu, consume);
+                    const int my_c = cc + __popc(cons & ((1u << lane) - 1u));
+                    const int32_t rv = ring.get(used + my_c);
+                    bool flip = false, out = false, miss = false;
+                    float xf = 0.0f;
+                    if (mine) {
+                        if (!consume) {
+                            flip = true;
+                        } else if (used + my_c >= cap) {
+                            out = true;
+                        } else {
+                            const int fast = rl != 0.0f ? quick_decide(ediff, rl, rv) : -1;
+                            if (fast >= 0) {
+                                flip = fast != 0;
+                            } else {
+                                xf = __fdiv_rn(ediff, temp);
+                                const int quick = fp32_decide(xf, rv);
+                                if (quick >= 0) {
+                                    flip = quick != 0;
+                                } else {
+                                    const double q = (double)rv / 2147483647.0;   // glibc RAND_MAX
+                                    flip = patched_exp(xf, q, ep, &miss) > q;
+                                }
+                            }
+                        }
+                    }
+                    const uint32_t fl = __ballot_sync(0xffffffffu, flip);
+                    const uint32_t wrong = __ballot_sync(0xffffffffu, lane > start && lane < nb && (dep & fl));
+                    const int p = wrong ? __ffs(wrong) - 1 : nb;
+                    const uint32_t keep = p >= 32 ? 0xffffffffu : ((1u << p) - 1u);
+                    if (__any_sync(0xffffffffu, out && lane < p)) {
+                        if (lane == 0) pq_set_status(status, PQ_ERR_RAND_EXHAUSTED);
+                        dead = true;
+                        stop = 1;
+                        break;
+                    }
+                    if (miss && lane < p) record_close(ep, xf, exp((double)xf));
+                    flipmask |= fl & keep;
+                    cc += __popc(cons & keep);
+                    start = p;
+                }
+                if (!stop) {
+                    used += cc;
+                    ring.advance(used, lane);
+                }
+                if (lane == 0) { ctl[2 * buf] = (int)flipmask; ctl[2 * buf + 1] = stop; }
+                pair_barrier();              // the fold warp has folded block bb + 1
+                if (stop) break;
+                fm_prev = flipmask;
+                if (++blk == nblk) {
+                    blk = 0;
+                    if (++step == mcsteps) { step = 0; ++g; }
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const bool bad = ctl[4] != 0;
+        if (bad) pq_set_status(status, PQ_ERR_BAD_INDEX);
+        rand_used[r] = (dead || bad) ? -1 : used;
+    }
+    for (int t = threadIdx.x; t < n; t += 64) gs[t] = s[t];
+}
+
 __global__ void exp_probe_kernel(const float* __restrict__ x, double* __restrict__ y, int64_t n) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) y[i] = exp((double)x[i]);
@@ -1637,19 +1738,19 @@ int pq_sa_sparse_reforder_ex(int8_t* spins, const int32_t* nb_idx, const float* 
     if (maxnb < 0 || !spins || !rand_used || (maxnb > 0 && (!nb_idx || !nb_j))) return PQ_ERR_INVALID_ARG;
     if (R == 0) return PQ_OK;
     ExpPatch ep = make_patch(ov_x, ov_y, ov_n, close_x, close_y, close_cap, close_cnt);
-    const size_t wsmem = (((size_t)n + 15) & ~(size_t)15) * 2;
-    if (maxnb <= 8 && wsmem <= kRefSmemMax) {
+    const size_t psmem = SaPairLayout(n).total;
+    if (maxnb <= 8 && psmem <= kRefSmemMax) {
         cudaStream_t st = (cudaStream_t)stream;
         if (flags & PQ_ACC_FP64) {
-            PQ_CUDA_TRY(cudaFuncSetAttribute(sa_sparse_reforder_warp_kernel<true>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsmem));
-            sa_sparse_reforder_warp_kernel<true><<<R, 32, wsmem, st>>>(spins, nb_idx, nb_j, n, maxnb, R, temps, nsched,
+            PQ_CUDA_TRY(cudaFuncSetAttribute(sa_sparse_reforder_pair_kernel<true>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
+            sa_sparse_reforder_pair_kernel<true><<<R, 64, psmem, st>>>(spins, nb_idx, nb_j, n, maxnb, R, temps, nsched,
                                                                        mcsteps, perms, rands, rand_stride, rand_used,
                                                                        ep, status);
         } else {
-            PQ_CUDA_TRY(cudaFuncSetAttribute(sa_sparse_reforder_warp_kernel<false>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsmem));
-            sa_sparse_reforder_warp_kernel<false><<<R, 32, wsmem, st>>>(spins, nb_idx, nb_j, n, maxnb, R, temps,
+            PQ_CUDA_TRY(cudaFuncSetAttribute(sa_sparse_reforder_pair_kernel<false>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
+            sa_sparse_reforder_pair_kernel<false><<<R, 64, psmem, st>>>(spins, nb_idx, nb_j, n, maxnb, R, temps,
                                                                         nsched, mcsteps, perms, rands, rand_stride,
                                                                         rand_used, ep, status);
         }
