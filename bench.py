@@ -731,6 +731,37 @@ def reforder_workload(args, torch):
         out["dense_replicas_%d" % R] = {"value": float(nd) * Pd * dsteps * R / min(times), "unit": "updates/s",
                                         "ms": 1e3 * min(times),
                                         "workload": "dense N=512, P=32, %d field steps, reference order" % dsteps}
+    # sa.Anneal_bipartite's reference-order sweep: 512 + 512 spins, J ~ N(0, 1/512), biases ~ N(0, 0.1), FP64
+    nl = nr = 512
+    Jb = torch.from_numpy(g.normal(0.0, 1.0 / np.sqrt(nl), (nl, nr))).cuda()
+    lb = torch.from_numpy(g.normal(0.0, 0.1, nl)).cuda()
+    rb = torch.from_numpy(g.normal(0.0, 0.1, nr)).cuda()
+    for R, bsteps in ((1, 4), (256, 2)):
+        btemps = torch.from_numpy(np.linspace(3.0, 0.05, bsteps).astype(np.float32)).cuda()
+        cap = (nl + nr) * bsteps
+        rands = torch.from_numpy(g.integers(0, 2 ** 31 - 1, size=(R, cap), dtype=np.int64).astype(np.int32)).cuda()
+        s0 = torch.from_numpy(np.where(g.random((R, nl + nr)) < 0.5, -1, 1).astype(np.int8)).cuda()
+        used = torch.zeros(R, dtype=torch.int64, device="cuda")
+        status = torch.zeros(1, dtype=torch.int32, device="cuda")
+        times = []
+        for it in range(2):
+            sp = s0.clone()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            rc = lib.pq_sa_bipartite_reforder_ex(_device.ptr(sp), _device.ptr(Jb), nl, nr, _device.ptr(lb),
+                                                 _device.ptr(rb), R, _device.ptr(btemps), bsteps, 1, _device.ptr(rands),
+                                                 cap, _device.ptr(used), None, None, 0, None, None, 0, None,
+                                                 _device.ptr(status), _device.stream_handle())
+            e1.record()
+            torch.cuda.synchronize()
+            _native.check(rc, "pq_sa_bipartite_reforder_ex")
+            if int(status.item()) or int(used.min().item()) < 0:
+                raise RuntimeError("reference-order bipartite bench: status %d" % int(status.item()))
+            times.append(e0.elapsed_time(e1) * 1e-3)
+        out["bipartite_replicas_%d" % R] = {"value": float(nl + nr) * bsteps * R / min(times), "unit": "updates/s",
+                                            "ms": 1e3 * min(times),
+                                            "workload": "sa.Anneal_bipartite 512+512, FP64 weights, %d steps" % bsteps}
     return out
 
 
