@@ -674,6 +674,39 @@ def reforder_workload(args, torch):
             times.append(e0.elapsed_time(e1) * 1e-3)
         out["replicas_%d" % R] = {"value": float(n) * P * steps * R / min(times), "unit": "updates/s",
                                   "ms": 1e3 * min(times)}
+    # the same sweep on the headline's 80x80 instance (P = 20), one replica, 20 field steps
+    n80 = L_SIDE * L_SIDE
+    r80, c80, v80 = instance_arrays()
+    i80, j80 = reforder.split_neighbors(neighbors_from_keys(n80, r80, c80, v80, 4))
+    s80 = schedule(NSCHED)[:: NSCHED // 20][:20]
+    jp80 = torch.from_numpy(reforder.jperp_schedule(s80, P, TEMP)).cuda()
+    perms = torch.from_numpy(np.stack([g.permutation(n80) for _ in range(len(s80))])[None].astype(np.int32)).cuda()
+    cap = n80 * P * len(s80)
+    rands = torch.from_numpy(g.integers(0, 2 ** 31 - 1, size=(1, cap), dtype=np.int64).astype(np.int32)).cuda()
+    sp0 = torch.from_numpy(np.repeat(np.where(g.random((1, n80)) < 0.5, -1, 1).astype(np.int8)[:, :, None], P,
+                                     axis=2)).cuda()
+    d_i80, d_j80 = torch.from_numpy(i80).cuda(), torch.from_numpy(j80).cuda()
+    used = torch.zeros(1, dtype=torch.int64, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    times = []
+    for it in range(2):
+        sp = sp0.clone()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        rc = lib.pq_qa_sparse_reforder(_device.ptr(sp), _device.ptr(d_i80), _device.ptr(d_j80), n80, n80,
+                                       i80.shape[1], P, 1, _device.ptr(jp80), len(s80), 1, float(np.float32(TEMP)),
+                                       _device.ptr(perms), _device.ptr(rands), cap, _device.ptr(used), 0,
+                                       _device.ptr(status), _device.stream_handle())
+        e1.record()
+        torch.cuda.synchronize()
+        _native.check(rc, "pq_qa_sparse_reforder")
+        if int(status.item()) or int(used.min().item()) < 0:
+            raise RuntimeError("reference-order 80x80 bench: status %d" % int(status.item()))
+        times.append(e0.elapsed_time(e1) * 1e-3)
+    out["replicas_1_80x80"] = {"value": float(n80) * P * len(s80) / min(times), "unit": "updates/s",
+                               "ms": 1e3 * min(times),
+                               "workload": "80x80 periodic, J~N(0,1) fp32, P=20, 20 field steps, reference order"}
     # sa.Anneal's reference-order sweep, one replica, 100 temperatures 5 -> 0.05
     temps = torch.from_numpy(np.linspace(5.0, 0.05, steps).astype(np.float32)).cuda()
     perms = torch.from_numpy(np.stack([g.permutation(n) for _ in range(steps)])[None].astype(np.int32)).cuda()
