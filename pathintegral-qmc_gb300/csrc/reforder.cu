@@ -880,7 +880,34 @@ struct DensePos {
 // FP32 terms (FP32 padded for the chain's read-ahead), one flag per row, control words.
 __host__ __device__ inline size_t dense_pair_smem(int n, int P) {
     return dense_warp_align16((size_t)n * P) + (size_t)16 * n + dense_warp_align16((size_t)16 * (n + 2)) +
-           2 * dense_warp_align16((size_t)4 * (n + 12)) + dense_warp_align16((size_t)n) + 16;
+           6 * dense_warp_align16((size_t)4 * (n + 12)) + dense_warp_align16((size_t)n) + 32;
+}
+
+// One step of the FP64 chain, (float)((double)e + t), from FP32 pieces t = t1 + t2 + t3
+// (exact): c = fl32(s + fl32(fl32(a + t2) + t3)) with s + a = e + t1 exactly (TwoSum),
+// and ok when a bound on |fl64(e + t) - c| is strictly below the half-gap of c's
+// rounding interval, so that c is the reference's value.  The bound adds up the
+// rounding errors of the tail's sum (<= 2^-23 (|a| + |t2| + |t3|)), of d = fl32((s - c)
+// + tail) (s - c exact by Sterbenz's lemma when |tail| <= |s| / 4, checked), and of the
+// FP64 rounding of the exact sum (<= 2^-52 |c|), each with a margin of 2 to 4 that also
+// covers the rounding of the bound itself.  When ok is false the caller takes the
+// reference's FP64 step instead.
+__device__ __forceinline__ float chain_step32(float e, float t1, float t2, float t3, bool& ok) {
+    const float s = __fadd_rn(e, t1);
+    const float bb = __fsub_rn(s, e);
+    const float a = __fadd_rn(__fsub_rn(e, __fsub_rn(s, bb)), __fsub_rn(t1, bb));
+    const float wf = __fadd_rn(__fadd_rn(a, t2), t3);
+    const float c = __fadd_rn(s, wf);
+    const float d = __fadd_rn(__fsub_rn(s, c), wf);
+    const float sum_abs = __fadd_rn(__fadd_rn(fabsf(a), fabsf(t2)), fabsf(t3));
+    const float bound = __fadd_rn(__fadd_rn(__fmul_rn(fabsf(d), 1.0000005f), __fmul_rn(sum_abs, 4.76837158203125e-7f)),
+                                  __fadd_rn(__fmul_rn(fabsf(c), 4.44089209850062616e-16f), 1.17549435e-38f));
+    const uint32_t cb = __float_as_uint(c) & 0x7FFFFFFFu;
+    const uint32_t E = cb >> 23;
+    const uint32_t hb = ((cb & 0x7FFFFFu) == 0 ? (E - 25u) : (E - 24u)) << 23;   // half-gap (a power of two:
+    ok = E >= 26u && E <= 253u && fabsf(wf) <= __fmul_rn(0.25f, fabsf(s)) &&     // the gap below is half)
+         bound < __uint_as_float(hb);
+    return c;
 }
 
 template <bool QA>
@@ -901,8 +928,11 @@ __global__ void __launch_bounds__(64) dense_reforder_pair_kernel(
     float* t32 = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(t64) +
                                           dense_warp_align16((size_t)16 * (n + 2)));                 // [2][t32s]
     const size_t t32s = dense_warp_align16((size_t)4 * (n + 12)) / 4;
-    uint8_t* row_f32 = reinterpret_cast<uint8_t*>(t32 + 2 * t32s);                                   // [n]
-    int* ctl = reinterpret_cast<int*>(row_f32 + dense_warp_align16((size_t)n));                      // flip, stop
+    float* q2 = t32 + 2 * t32s;                                                                       // [2][t32s]
+    float* q3 = q2 + 2 * t32s;                                                                        // [2][t32s]
+    uint8_t* row_f32 = reinterpret_cast<uint8_t*>(q3 + 2 * t32s);                                    // [n]
+    int* ctl = reinterpret_cast<int*>(row_f32 + dense_warp_align16((size_t)n));   // flip, stop; split ok
+    if (threadIdx.x < 8) ctl[threadIdx.x] = 0;
     int8_t* gs = spins + (int64_t)r * n * Pq;
     for (int64_t t = threadIdx.x; t < (int64_t)n * Pq; t += 64) s[t] = gs[t];
     for (int i = warp; i < n; i += 2) {
@@ -911,7 +941,6 @@ __global__ void __launch_bounds__(64) dense_reforder_pair_kernel(
         ok = __all_sync(0xffffffffu, ok);
         if (lane == 0) row_f32[i] = ok ? 1 : 0;
     }
-    if (threadIdx.x < 4) ctl[threadIdx.x] = 0;
     __syncthreads();
     const int32_t* pr = perms + (int64_t)r * nsched * mcsteps * n;
     const int64_t nsweeps = (int64_t)nsched * mcsteps;
@@ -947,7 +976,11 @@ __global__ void __launch_bounds__(64) dense_reforder_pair_kernel(
                     cp_async8(dst + j, j >= i ? J + (int64_t)i * n + j : J + (int64_t)j * n + i);
                 cp_async_commit();
             };
-            auto form = [&](int i, int k, int g, const double* rw, float* o32, double* o64) {
+            auto form = [&](int i, int k, int g, const double* rw, int b) {
+                float* o32 = t32 + (size_t)b * t32s;
+                double* o64 = t64 + (size_t)b * (n + 2);
+                float* o2 = q2 + (size_t)b * t32s;
+                float* o3 = q3 + (size_t)b * t32s;
                 const bool f32 = f32_of(i, g);
                 i = safe(i);
                 const int8_t si8 = s[(int64_t)i * Pq + k];
@@ -964,16 +997,34 @@ __global__ void __launch_bounds__(64) dense_reforder_pair_kernel(
                         o32[n + 1] = __fmul_rn(m2si, s[(int64_t)i * Pq + tr_of(k)] > 0 ? jpf : -jpf);
                     }
                 } else {
+                    // FP64 terms, and each split exactly into FP32 pieces t1 + t2 + t3 for the
+                    // chain's FP32 steps (t - t1 and the next remainder are exact in FP64)
                     const double m2si = -2.0 * (double)si8;
-                    for (int j = lane; j < n; j += 32) {
+                    bool ok = true;
+                    auto split = [&](int j, double tt) {
+                        o64[j] = tt;
+                        const float a1 = __double2float_rn(tt);
+                        const double r1 = __dsub_rn(tt, (double)a1);
+                        const float a2 = __double2float_rn(r1);
+                        const double r2 = __dsub_rn(r1, (double)a2);
+                        const float a3 = __double2float_rn(r2);
+                        ok &= ((double)a3 == r2) & (fabsf(a1) <= 3.0e38f);
+                        o32[j] = a1;
+                        o2[j] = a2;
+                        o3[j] = a3;
+                    };
+#pragma unroll 4
+                    for (int j = lane; j < n; j += 32) {   // unrolled: independent FP64 chains overlap
                         const double jv = rw[j];
-                        o64[j] = j == i ? m2si * jv : m2si * (jv * (double)s[(int64_t)j * Pq + k]);
+                        split(j, j == i ? m2si * jv : m2si * (jv * (double)s[(int64_t)j * Pq + k]));
                     }
                     if (QA && lane == 0) {
                         const double jp = jp_of(g);
-                        o64[n] = m2si * (jp * (double)s[(int64_t)i * Pq + tl_of(k)]);
-                        o64[n + 1] = m2si * (jp * (double)s[(int64_t)i * Pq + tr_of(k)]);
+                        split(n, m2si * (jp * (double)s[(int64_t)i * Pq + tl_of(k)]));
+                        split(n + 1, m2si * (jp * (double)s[(int64_t)i * Pq + tr_of(k)]));
                     }
+                    ok = __all_sync(0xffffffffu, ok);
+                    if (lane == 0) ctl[4 + b] = ok ? 1 : 0;
                 }
             };
             int e0 = next_entry(), e1 = next_entry(), e2 = next_entry(), e3 = next_entry();
@@ -983,7 +1034,7 @@ __global__ void __launch_bounds__(64) dense_reforder_pair_kernel(
             else cp_async_commit();
             cp_async_wait<1>();
             __syncwarp();
-            form(e0, 0, 0, row, t32, t64);   // position 0
+            form(e0, 0, 0, row, 0);          // position 0
             __syncwarp();
             pair_barrier();                  // terms of position 0 are ready
             for (int64_t p = 0; p < total; ++p) {
@@ -993,9 +1044,7 @@ __global__ void __launch_bounds__(64) dense_reforder_pair_kernel(
                 else cp_async_commit();
                 cp_async_wait<1>();
                 __syncwarp();
-                if (p + 1 < total)
-                    form(e1, nx.k, nx.g, row + (size_t)((p + 1) & 1) * n, t32 + (size_t)((p + 1) & 1) * t32s,
-                         t64 + (size_t)((p + 1) & 1) * (n + 2));
+                if (p + 1 < total) form(e1, nx.k, nx.g, row + (size_t)((p + 1) & 1) * n, (int)((p + 1) & 1));
                 __syncwarp();
                 pair_barrier();              // the chain warp has decided position p
                 const int* c = ctl + 2 * (int)(p & 1);   // two slots: the chain warp writes p + 1's
@@ -1042,6 +1091,34 @@ __global__ void __launch_bounds__(64) dense_reforder_pair_kernel(
                         }
                         const float* c32 = t32 + (size_t)tb * t32s;
                         for (int j = nq * 4; j < nt; ++j) ediff = __fadd_rn(ediff, c32[j]);
+                    } else if (ctl[4 + tb]) {
+                        // FP32 steps on the split terms, walked ahead; a step whose check fails is
+                        // redone as the reference's FP64 step and the walk resumes after it
+                        const float* c1 = t32 + (size_t)tb * t32s;
+                        const float* c2 = q2 + (size_t)tb * t32s;
+                        const float* c3 = q3 + (size_t)tb * t32s;
+                        const double* c64 = t64 + (size_t)tb * (n + 2);
+                        int j0 = 0;
+                        while (j0 < nt) {
+                            int bad = -1;
+                            float e_bad = 0.0f, ee = ediff;
+                            float x1 = c1[j0], x2 = c2[j0], x3 = c3[j0];   // the next step's pieces
+#pragma unroll 4
+                            for (int j = j0; j < nt; ++j) {                 // are read a step ahead;
+                                                                            // unrolled so that a step's
+                                                                            // check overlaps the next adds
+                                const int jn = j + 1 < nt ? j + 1 : j;
+                                const float y1 = c1[jn], y2 = c2[jn], y3 = c3[jn];
+                                bool ok;
+                                const float c = chain_step32(ee, x1, x2, x3, ok);
+                                if (!ok && bad < 0) { bad = j; e_bad = ee; }
+                                ee = c;
+                                x1 = y1; x2 = y2; x3 = y3;
+                            }
+                            if (bad < 0) { ediff = ee; break; }
+                            ediff = acc(e_bad, c64[bad]);
+                            j0 = bad + 1;
+                        }
                     } else {
                         const double* c64 = t64 + (size_t)tb * (n + 2);
                         double v = c64[0];
@@ -1087,24 +1164,28 @@ __global__ void __launch_bounds__(64) dense_reforder_pair_kernel(
                 if (stop) break;
                 if (flip_word >= 0 && p + 1 < total && (unsigned)i1 < (unsigned)n) {
                     // correct position p + 1's terms for this flip
+                    // (every form of a term is negated: FP32, FP64 and the FP32 pieces)
                     const int nb = (int)((p + 1) & 1);
-                    const bool f32n = f32_of(i1, nx.g);
                     float* n32 = t32 + (size_t)nb * t32s;
+                    float* n2 = q2 + (size_t)nb * t32s;
+                    float* n3 = q3 + (size_t)nb * t32s;
                     double* n64 = t64 + (size_t)nb * (n + 2);
+                    auto negate = [&](int j) {
+                        n32[j] = -n32[j];
+                        n2[j] = -n2[j];
+                        n3[j] = -n3[j];
+                        n64[j] = -n64[j];
+                    };
                     if (nx.k == cur.k) {
                         if (i1 == i0) {
-                            for (int j = lane; j < n; j += 32) {
-                                if (f32n) n32[j] = -n32[j];
-                                else n64[j] = -n64[j];
-                            }
+                            for (int j = lane; j < n; j += 32) negate(j);
                         } else if (lane == 0) {
-                            if (f32n) n32[i0] = -n32[i0];
-                            else n64[i0] = -n64[i0];
+                            negate(i0);
                         }
                     }
                     if (QA && lane == 0 && i1 == i0) {
-                        if (tl_of(nx.k) == cur.k) { if (f32n) n32[n] = -n32[n]; else n64[n] = -n64[n]; }
-                        if (tr_of(nx.k) == cur.k) { if (f32n) n32[n + 1] = -n32[n + 1]; else n64[n + 1] = -n64[n + 1]; }
+                        if (tl_of(nx.k) == cur.k) negate(n);
+                        if (tr_of(nx.k) == cur.k) negate(n + 1);
                     }
                     __syncwarp();
                 }
