@@ -1214,7 +1214,7 @@ __global__ void __launch_bounds__(64) dense_reforder_pair_kernel(
 __host__ __device__ inline size_t bipartite_warp_smem(int nl, int nr) {
     const size_t m = (size_t)(nl > nr ? nl : nr);
     return dense_warp_align16((size_t)nl + nr) + 16 * m + dense_warp_align16(8 * (m + 1)) +
-           dense_warp_align16(4 * (m + 12));
+           3 * dense_warp_align16(4 * (m + 12));
 }
 
 __global__ void __launch_bounds__(32) sa_bipartite_reforder_warp_kernel(
@@ -1233,6 +1233,8 @@ __global__ void __launch_bounds__(32) sa_bipartite_reforder_warp_kernel(
     double* t64 = vec + (size_t)2 * m;                                                               // [m + 1]
     float* t32 = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(t64) +
                                           dense_warp_align16((size_t)8 * (m + 1)));                 // [m + 12]
+    float* p2 = t32 + dense_warp_align16((size_t)4 * (m + 12)) / 4;                                // [m + 12]
+    float* p3 = p2 + dense_warp_align16((size_t)4 * (m + 12)) / 4;                                 // [m + 12]
     int8_t* gs = spins + (int64_t)r * (nl + nr);
     for (int t = lane; t < nl + nr; t += 32) sh[t] = gs[t];
     __syncwarp();
@@ -1281,17 +1283,27 @@ __global__ void __launch_bounds__(32) sa_bipartite_reforder_warp_kernel(
                 const int8_t* other = side == 0 ? rv : lv;
                 const int no = side == 0 ? nr : nl;
                 const double si = (double)self[i];
-                bool exact = true;
-                for (int j = lane; j < no; j += 32) {
+                bool exact = true, split_ok = true;
+#pragma unroll 4
+                for (int j = lane; j < no; j += 32) {   // unrolled: independent FP64 chains overlap
                     const double sj = (double)other[j];
                     const double t = side == 0 ? 2.0 * si * jv[j] * sj + lbias[i] * si + rbias[j] * sj
                                                : 2.0 * si * jv[j] * sj + lbias[j] * sj + rbias[i] * si;
+                    // t = tf + a2 + a3 exactly in FP32 pieces (see chain_step32)
                     const float tf = __double2float_rn(t);
-                    exact = exact && (double)tf == t;
+                    const double r1 = __dsub_rn(t, (double)tf);
+                    const float a2 = __double2float_rn(r1);
+                    const double r2 = __dsub_rn(r1, (double)a2);
+                    const float a3 = __double2float_rn(r2);
+                    exact &= r1 == 0.0;
+                    split_ok &= ((double)a3 == r2) & (fabsf(tf) <= 3.0e38f);
                     t64[j] = t;
                     t32[j] = tf;
+                    p2[j] = a2;
+                    p3[j] = a3;
                 }
                 const bool f32 = __all_sync(0xffffffffu, exact);
+                const bool split = __all_sync(0xffffffffu, split_ok);
                 __syncwarp();
                 float ediff = 0.0f;
                 if (f32) {
@@ -1305,6 +1317,28 @@ __global__ void __launch_bounds__(32) sa_bipartite_reforder_warp_kernel(
                         v1 = v2;
                     }
                     for (int j = nq * 4; j < no; ++j) ediff = __fsub_rn(ediff, t32[j]);
+                } else if (split) {
+                    // FP32 steps on the negated pieces, walked ahead; a failing step is redone
+                    // as the reference's FP64 step and the walk resumes after it
+                    int j0 = 0;
+                    while (j0 < no) {
+                        int bad = -1;
+                        float e_bad = 0.0f, ee = ediff;
+                        float x1 = t32[j0], x2 = p2[j0], x3 = p3[j0];
+#pragma unroll 4
+                        for (int j = j0; j < no; ++j) {
+                            const int jn = j + 1 < no ? j + 1 : j;
+                            const float y1 = t32[jn], y2 = p2[jn], y3 = p3[jn];
+                            bool ok;
+                            const float c = chain_step32(ee, -x1, -x2, -x3, ok);
+                            if (!ok && bad < 0) { bad = j; e_bad = ee; }
+                            ee = c;
+                            x1 = y1; x2 = y2; x3 = y3;
+                        }
+                        if (bad < 0) { ediff = ee; break; }
+                        ediff = __double2float_rn(__dsub_rn((double)e_bad, t64[bad]));
+                        j0 = bad + 1;
+                    }
                 } else {
                     for (int j = 0; j < no; ++j) ediff = __double2float_rn(__dsub_rn((double)ediff, t64[j]));
                 }
