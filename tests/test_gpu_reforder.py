@@ -359,3 +359,68 @@ def test_edge_cases(piqmc):
     out, used = rf.quantum_anneal(sp[None], idx, jv, np.linspace(1, 0.1, 4), 2, 0.2, perms[None], rands[None],
                                   nperm=10)
     np.testing.assert_array_equal(out.cpu().numpy()[0], confs.astype(np.int8))
+
+
+def test_single_thread_kernels_beyond_shared_memory(piqmc):
+    """Problems too large for the warp kernels' shared memory run the single-thread kernels,
+    with the same results as the oracle (sizes just past each warp kernel's limit)."""
+    from piqmc import reforder, tools
+    g = np.random.default_rng(77)
+    # QuantumAnneal_dense, n = 3500, P = 2 (the pair kernel holds n <= ~3470 at P = 2)
+    n, P = 3500, 2
+    J = np.triu(g.normal(0, 1 / np.sqrt(n), (n, n)), 1) + np.diag(g.normal(0, 0.1, n))
+    sched = np.array([1.5])
+    spins = np.where(g.random((1, n, P)) < 0.5, -1, 1).astype(np.int8)
+    perms = oracle.reference_perms(np.random.RandomState(1), n, 1)[None]
+    rands = g.integers(0, 2 ** 31 - 1, size=(1, n * P + 1), dtype=np.int64).astype(np.int32)
+    out, used = reforder.quantum_anneal_dense(spins, J, sched, 1, 0.5, perms, rands)
+    sp = spins[0].copy()
+    assert used[0] == oracle.qa_dense(sp, J, sched, 1, 0.5, perms[0], rands[0])
+    np.testing.assert_array_equal(out.cpu().numpy()[0], sp)
+    # sa.Anneal_dense, n = 3550
+    n = 3550
+    J = np.triu(g.normal(0, 1 / np.sqrt(n), (n, n)), 1) + np.diag(g.normal(0, 0.1, n))
+    spins = np.where(g.random((1, n)) < 0.5, -1, 1).astype(np.int8)
+    perms = oracle.reference_perms(np.random.RandomState(2), n, 1)[None]
+    rands = g.integers(0, 2 ** 31 - 1, size=(1, n + 1), dtype=np.int64).astype(np.int32)
+    out, used = reforder.anneal_dense(spins, J, np.array([0.7]), 1, perms, rands)
+    sp = spins[0].copy()
+    assert used[0] == oracle.sa_dense(sp, J, np.array([0.7]), 1, perms[0], rands[0])
+    np.testing.assert_array_equal(out.cpu().numpy()[0], sp)
+    # QuantumAnneal (sparse), 100 x 100 periodic with fields, P = 21
+    L, P = 100, 21
+    Js = lattice(L, True, g, dist=lambda r: r.normal(), fields=lambda r: r.normal(0, 0.5))
+    n = L * L
+    nbs = tools.GenerateNeighbors(n, Js, 5)   # (tested against the oracle elsewhere; fast)
+    idx, jv = reforder.split_neighbors(nbs)
+    sched = np.linspace(2.0, 1.0, 2)
+    spins = np.where(g.random((1, n, P)) < 0.5, -1, 1).astype(np.int8)
+    perms = oracle.reference_perms(np.random.RandomState(3), n, 2)[None]
+    rands = g.integers(0, 2 ** 31 - 1, size=(1, n * P * 2 + 1), dtype=np.int64).astype(np.int32)
+    out, used = reforder.quantum_anneal(spins, idx, jv, sched, 1, 0.3, perms, rands)
+    sp = spins[0].copy()
+    assert used[0] == oracle.qa_sparse(sp, nbs, sched, 1, 0.3, perms[0], rands[0])
+    np.testing.assert_array_equal(out.cpu().numpy()[0], sp)
+    # sa.Anneal (sparse), 260 x 260 periodic
+    L = 260
+    Js = lattice(L, True, g, dist=lambda r: r.normal())
+    n = L * L
+    nbs = tools.GenerateNeighbors(n, Js, 4)
+    idx, jv = reforder.split_neighbors(nbs)
+    spins = np.where(g.random((1, n)) < 0.5, -1, 1).astype(np.int8)
+    perms = oracle.reference_perms(np.random.RandomState(4), n, 1)[None]
+    rands = g.integers(0, 2 ** 31 - 1, size=(1, n + 1), dtype=np.int64).astype(np.int32)
+    out, used = reforder.anneal(spins, idx, jv, np.array([0.8]), 1, perms, rands)
+    sp = spins[0].copy()
+    assert used[0] == oracle.sa_sparse(sp, nbs, np.array([0.8]), 1, perms[0], rands[0])
+    np.testing.assert_array_equal(out.cpu().numpy()[0], sp)
+    # sa.Anneal_bipartite, 5400 + 2 spins
+    nl, nr = 5400, 2
+    Jb, lb, rb = g.normal(0, 1, (nl, nr)), g.normal(0, 0.5, nl), g.normal(0, 0.5, nr)
+    spins = np.where(g.random((1, nl + nr)) < 0.5, -1, 1).astype(np.int8)
+    rands = g.integers(0, 2 ** 31 - 1, size=(1, 2 * (nl + nr) + 1), dtype=np.int64).astype(np.int32)
+    out, used = reforder.anneal_bipartite(spins, nl, Jb, lb, rb, np.array([2.0, 0.5]), 1, rands)
+    lv, rv = spins[0, :nl].copy(), spins[0, nl:].copy()
+    assert used[0] == oracle.sa_bipartite(lv, rv, Jb, lb, rb, np.array([2.0, 0.5]), 1, rands[0])
+    np.testing.assert_array_equal(out.cpu().numpy()[0, :nl], lv)
+    np.testing.assert_array_equal(out.cpu().numpy()[0, nl:], rv)
