@@ -145,9 +145,10 @@ __device__ __forceinline__ void load_site(const W* rw, int i, int n, int maxdeg,
 // Metropolis decision for sum = e + t (ediff = -2 sum): flip when sum < 0, else
 // when u < expf_neg(fl(sum * m2beta)) with m2beta = -2 beta.  The hardware 2^x
 // (argument fl(sum * m2blog2e), m2blog2e = fl(-2 beta log2 e)) settles it outside
-// a 1e-4 relative guard band -- its error against expf_neg is below 2e-5 for every
-// argument above -87 -- and expf_neg itself settles the rest, so the result is
-// exactly the specification's.
+// a 1e-4 relative guard band -- its error against expf_neg is under 5e-5 for every
+// argument above -87 (checked exhaustively on the GPU; measured below 2e-5), and the
+// rounding of its argument adds under 1.7e-5 -- and expf_neg itself settles the
+// rest, so the result is exactly the specification's.
 __device__ __forceinline__ bool decide(float sum, float u, float m2beta, float m2blog2e) {
     if (sum < 0.0f) return true;
     const float pf = pq_ex2_approx(__fmul_rn(sum, m2blog2e));
