@@ -110,3 +110,40 @@ def test_powers_of_two_and_extremes():
         e = (g.normal(0, 1, m) * 1e38).astype(f32)
         t = g.normal(0, 1, m) * 1e38
         check(e, t)
+
+
+def f32_of_exact(d):
+    """The device's bit conversion of an FP64 value that is zero or a normal FP32 number."""
+    b = d.view(np.uint64)
+    hi = (b >> np.uint64(32)).astype(np.uint32)
+    e = (hi >> np.uint32(20)) & np.uint32(0x7FF)
+    sign = hi & np.uint32(0x80000000)
+    man = ((b >> np.uint64(29)) & np.uint64(0x7FFFFF)).astype(np.uint32)
+    with np.errstate(over="ignore"):
+        bits = np.where(e == 0, sign, sign | ((e - np.uint32(896)) << np.uint32(23)) | man).astype(np.uint32)
+    return bits.view(f32)
+
+
+def fp32_term_exact(v):
+    a = np.abs(v)
+    with np.errstate(over="ignore"):
+        return (v == 0.0) | ((a >= 1.1754943508222875e-38) & (a <= 1.7014117331926443e38) &
+                             (v.astype(f32).astype(f64) == v))
+
+
+def test_fp32_row_conversion():
+    """Rows marked FP32-valued convert bit for bit, and +-2J of them is an FP32 value."""
+    g = np.random.default_rng(3)
+    m = 1_000_000
+    x = (g.normal(0, 1, m) * np.exp(g.uniform(-80, 80, m))).astype(f32)
+    x = np.concatenate([x, np.array([0.0, -0.0, 1.17549435e-38, -3.4e38, 1.7e38], dtype=f32)])
+    d = x.astype(f64)
+    ok = fp32_term_exact(d)
+    got = f32_of_exact(d[ok])
+    assert np.array_equal(got.view(np.uint32), x[ok].view(np.uint32))
+    with np.errstate(over="ignore"):
+        assert np.all(np.isfinite(2 * got)) and np.array_equal((2 * got).astype(f64), 2 * d[ok])
+    # values that are not FP32 numbers (or FP32 subnormals) are never marked
+    y = g.normal(0, 1, m)
+    assert not fp32_term_exact(y[y.astype(f32).astype(f64) != y]).any()
+    assert not fp32_term_exact(np.array([1e-40, 3.0e38])).any()
