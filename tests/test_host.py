@@ -261,3 +261,44 @@ def test_autotune_plan_balances_the_batch():
     pairs[(8, 1, 2)] = 3.5e11
     tiles, _ = autotune.plan(shapes, [small] * 200 + [pairs], slots)
     assert tiles[200] == (8, 1, 2)
+
+
+def test_pack_tasks_invariants():
+    """Every item lands in exactly one task; a task holds one kind (warps per item, lanes per
+    site, compiled sweep), at most WARPS // gwarps items and at most the shared-memory budget;
+    tasks come longest item first."""
+    from piqmc import batch
+    g = np.random.default_rng(5)
+    items = []
+    for k in range(3000):
+        gw = int(g.choice([1, 2, 4, 8]))
+        kind = (gw, int(g.choice([1, 2])), int(g.choice([0, 1, 16, 20, 32, 64])))
+        smem = int(g.integers(1, batch.SMEM_TASK_BUDGET // 2))
+        items.append((float(g.exponential(1.0)), kind, smem, k))
+    tasks = batch.pack_tasks(items)
+    seen = [it[3] for _, lst in tasks for it in lst]
+    assert sorted(seen) == list(range(len(items)))
+    for kind, lst in tasks:
+        assert all(it[1] == kind for it in lst)
+        assert 1 <= len(lst) <= batch.WARPS // kind[0]
+        assert sum(batch._align(it[2]) for it in lst) <= batch.SMEM_TASK_BUDGET
+    longest = [max(it[0] for it in lst) for _, lst in tasks]
+    assert longest == sorted(longest, reverse=True)
+    assert batch.pack_tasks([]) == []
+
+
+def test_tile_normalisation_and_sweep_variants():
+    from piqmc import batch
+
+    class Pb:
+        maxdeg = 4
+    pb = Pb()
+    assert batch.normalise_tile((2, 4), pb, 20) == (2, 4, 1)
+    assert batch.normalise_tile((2, 4, 2), pb, 20) == (2, 4, 1)      # lane pairs need P = 64
+    assert batch.normalise_tile((2, 4, 2), pb, 64) == (2, 4, 2)
+    pb.maxdeg = 6
+    assert batch.normalise_tile((1, 1, 2), pb, 64) == (1, 1, 1)      # and four couplings
+    for bad in ((3, 1), (1, 0), (1, 1, 3)):
+        with pytest.raises(ValueError):
+            batch.normalise_tile(bad, pb, 20)
+    assert [batch.sweep_variant(P) for P in (1, 16, 20, 31, 32, 33, 64)] == [0, 16, 20, 0, 32, 1, 64]
