@@ -51,8 +51,10 @@ const char* pq_strerror(int status);
 
 /* ---------------------------------------------------------------------------
  * Reference-order sweeps: the reference's exact update order and arithmetic.
- * One thread walks one replica; R replicas run concurrently, each with its own
- * spin orders (perms) and uniform stream (rands).
+ * Each replica runs on a pair of warps (one forms the next spin's energy terms,
+ * the other walks the accumulation chain and decides), or on one thread when the
+ * problem is larger than the pair kernel's shared memory; R replicas run
+ * concurrently, each with its own spin orders (perms) and uniform stream (rands).
  *   perms     int32 [R][nsweeps][n], nsweeps = nsched*mcsteps: the spin order of
  *             each sweep (the successive rng.permutation results).
  *   rands     int32 [R][rand_stride]: successive libc rand() values.
@@ -169,10 +171,11 @@ int64_t pq_host_exp_compare(uint32_t first_bits, int64_t count, const double* de
 int pq_generate_neighbors(int nspins, int64_t nkeys, const int64_t* rows, const int64_t* cols,
                           const double* vals, int maxnb, double* out);
 
-/* Greedy colouring of the neighbour graph in spin order; color[i] in [0, ncolors).
- * nb_idx is host int32 [n][maxnb] (self entries and padding are ignored when
- * nb_j == 0 or index == i).  Returns the number of colours (> 0), or minus a
- * status. */
+/* Colouring of the neighbour graph; color[i] in [0, ncolors).  Greedy in spin
+ * order; when that needs more than two colours, DSatur too, and the one with
+ * fewer colours is kept.  nb_idx is host int32 [n][maxnb] (self entries and
+ * padding are ignored when nb_j == 0 or index == i; duplicate edges count once).
+ * Returns the number of colours (> 0), or minus a status. */
 int pq_color_graph(int n, int maxnb, const int32_t* nb_idx, const float* nb_j, int32_t* color);
 
 /* ---------------------------------------------------------------------------
@@ -180,7 +183,7 @@ int pq_color_graph(int n, int maxnb, const int32_t* nb_idx, const float* nb_j, i
  * qmc.QuantumAnneal with both reference quirks corrected).
  *
  * The graph is in "device order": spins are split into M update classes
- * (independent sets: each colour of a greedy colouring cut into sub-classes),
+ * (independent sets: each colour of pq_color_graph cut into sub-classes),
  * class c occupying device slots [c*S, c*S + class_size[c]) of a padded index
  * space of n = M*S slots (unused slots are never read or written).  Couplings
  * in SoA: nbr[m*n + i] (int32 device slot) and cpl[m*n + i] (float), m <
@@ -238,8 +241,8 @@ int pq_qa_fast_ex(void* words, const int32_t* nbr, const float* cpl, const float
  * instance whose words start at byte word_off of words_pool, and runs on a group
  * of `gwarps` warps of a CTA using shared memory from byte smem_off of the CTA's
  * dynamic shared memory (pq_batch_smem_bytes each).  A task = items
- * [item0, item0 + nitems), all with the same gwarps, nitems * gwarps <= warps of
- * the CTA.  Persistent CTAs pop tasks from *queue_head (scratch, reset by the
+ * [item0, item0 + nitems), all with the task's gwarps and lanes_per_site,
+ * nitems * gwarps <= warps of the CTA.  Persistent CTAs pop tasks from *queue_head (scratch, reset by the
  * call).  Results equal pq_qa_fast on each instance with key0/key1 as its seed
  * and replica0 as its replica_base.
  * ------------------------------------------------------------------------- */
