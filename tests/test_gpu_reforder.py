@@ -219,7 +219,7 @@ def _dense_j(g, n, kind):
 @pytest.mark.parametrize("kind", ["fp32", "fp64", "mixed"])
 @pytest.mark.parametrize("flags", [0, 1, 2, 3])
 def test_random_dense_cases_vs_oracle(piqmc, flags, kind):
-    """QuantumAnneal_dense in reference order (one warp per replica) against the oracle: every
+    """QuantumAnneal_dense in reference order (two warps per replica) against the oracle: every
     Q1/Q2 flag, FP32-valued, general FP64 and mixed J, n across 32-lane chunks, hot and cold."""
     from piqmc import reforder
     g = np.random.default_rng(100 + flags)
@@ -242,7 +242,7 @@ def test_random_dense_cases_vs_oracle(piqmc, flags, kind):
 
 @pytest.mark.parametrize("kind", ["fp32", "fp64"])
 def test_random_sa_dense_cases_vs_oracle(piqmc, kind):
-    """sa.Anneal_dense in reference order (one warp per replica) against the oracle."""
+    """sa.Anneal_dense in reference order (two warps per replica) against the oracle."""
     from piqmc import reforder
     g = np.random.default_rng(7)
     for n in (45, 96, 3):
