@@ -93,7 +93,7 @@ __device__ __forceinline__ int fp32_decide(float xf, int32_t rv) {
 // Against exp((double)fl(e / T)) the estimate errs by under 8e-5 (relative) wherever
 // exp > 1e-30: ex2.approx of a once-rounded argument is within 5e-5 of expf_neg there
 // (pq_guard_band_probe checks every such FP32 input against that bound; measured
-// below 2e-5), the three extra roundings of the argument add under 2.1e-5 and the
+// 3.6e-6), the three extra roundings of the argument add under 2.1e-5 and the
 // quotient's own rounding 5.2e-6.  Below that
 // both sides are under about 1e-30, far below any nonzero uniform (>= 2^-31).  A 1e-4
 // band around the FP32 uniform therefore leaves only decisions that the exact path

@@ -93,3 +93,49 @@ def test_tiny_uniforms_and_deep_exponents():
     assert check(e, T, g.integers(1, RAND_MAX + 1, m)) > 0.99
     # rv == 0 and e > 0 are left to the exact path
     assert (quick_decide(np.array([-1.0, 0.5], f32), quick_scale(f32(1)), np.array([0, 5]), 0.0) == -1).all()
+
+
+def _orc_expf(y):
+    import oracle
+    f = np.frompyfunc(lambda v: float(oracle.lib().orc_expf(float(v))), 1, 1)
+    return f(y).astype(f32)
+
+
+def packed_decide(s, u, m2beta, eps):
+    """decide() of the packed sweep (csrc/sweep_core.cuh): flip when s < 0, else the guard
+    band around the hardware 2^x (modelled exact * (1 + eps), flushed below FLT_MIN), else
+    u < expf_neg(fl(s * m2beta))."""
+    m2blog2e = m2beta * f32(1.44269502162933349609375)
+    with np.errstate(over="ignore", under="ignore"):
+        pf = (np.exp2((s * m2blog2e).astype(f64)) * (1.0 + eps)).astype(f32)
+    pf = np.where(pf < f32(1.17549435e-38), f32(0), pf)
+    rej = u > pf * f32(1.0001)
+    acc = (u < pf * f32(0.9999)) & (pf > f32(1e-30))
+    quick = np.where(rej, 0, np.where(acc, 1, -1))
+    quick = np.where(s < 0, 1, quick)
+    return quick
+
+
+def test_packed_sweep_decision_band():
+    """The packed sweep's quick decision equals the oracle's rule u < expf_neg(fl(-2 sum beta))
+    (oracle/fast_oracle.c) wherever it decides."""
+    g = np.random.default_rng(3)
+    m = 150_000
+    for beta in (f32(0.3), f32(1.0), f32(20.0), f32(1.0e3)):
+        m2beta = f32(-2.0) * beta
+        s = np.abs(g.normal(0, 1, m) * np.exp(g.uniform(-12, 4, m))).astype(f32) / beta
+        y = s * m2beta
+        ex = _orc_expf(y)
+        # uniforms of the kernel (k 2^-23): random, and the grid points next to expf_neg
+        k = np.floor(ex.astype(f64) * 2 ** 23)
+        us = [g.integers(0, 2 ** 23, m) * 2.0 ** -23]
+        us += [np.clip(k + d, 0, 2 ** 23 - 1) * 2.0 ** -23 for d in (-2, -1, 0, 1, 2)]
+        for u in us:
+            u = u.astype(f32)
+            want = u < ex
+            for eps in (-EX2_BOUND, 0.0, EX2_BOUND):
+                d = packed_decide(s, u, m2beta, eps)
+                bad = (d >= 0) & ((d == 1) != want)
+                assert not bad.any(), (beta, s[bad][:4], u[bad][:4], ex[bad][:4])
+    # negative sums always flip
+    assert (packed_decide(np.array([-1e-30, -5.0], f32), np.array([0.9, 0.0], f32), f32(-2), 0.0) == 1).all()
