@@ -139,3 +139,33 @@ def test_packed_sweep_decision_band():
                 assert not bad.any(), (beta, s[bad][:4], u[bad][:4], ex[bad][:4])
     # negative sums always flip
     assert (packed_decide(np.array([-1e-30, -5.0], f32), np.array([0.9, 0.0], f32), f32(-2), 0.0) == 1).all()
+
+
+def fp32_decide(x, rv):
+    """fp32_decide of the reference-order kernels: expf_neg (the oracle's orc_expf, the same
+    function bit for bit) against the FP32 uniform with a 2e-6 band; -1 undecided."""
+    ef = _orc_expf(x)
+    qf = rv.astype(f32) * f32(4.656612873077392578125e-10)
+    out = np.where(ef > qf * f32(1.000002), 1, np.where(ef < qf * f32(0.999998), 0, -1))
+    return np.where((rv <= 0) | ~(x <= 0), -1, out)
+
+
+def test_fp32_decision_band():
+    """Wherever fp32_decide decides, it equals exp((double)x) > rv / RAND_MAX and the case is
+    not a close call of the FP64 path."""
+    g = np.random.default_rng(4)
+    m = 200_000
+    x = (-np.abs(g.normal(0, 1, m)) * np.exp(g.uniform(-12, 4.5, m))).astype(f32)
+    ex = np.exp(x.astype(f64))
+    rvs = [g.integers(0, RAND_MAX + 1, m)]
+    k = np.floor(ex * RAND_MAX)
+    # offsets past the FP32 rounding of rv (up to 64 units near 2^31)
+    rvs += [np.clip(k + d, 0, RAND_MAX).astype(np.int64) for d in (-100, -63, -31, -1, 0, 1, 2, 32, 64, 100)]
+    for rv in rvs:
+        q = rv / RAND_MAX
+        close = (np.abs(ex - q) <= 1e-15 * np.maximum(ex, q)) | ((q == 0.0) & (ex < 1e-300))
+        d = fp32_decide(x, rv)
+        m_ = d >= 0
+        assert not (m_ & ((d == 1) != (ex > q))).any()
+        assert not (m_ & close).any()
+    assert (fp32_decide(np.array([-1.0, 0.5], f32), np.array([0, 5])) == -1).all()
