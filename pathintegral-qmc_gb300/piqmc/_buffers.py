@@ -43,6 +43,17 @@ def as_c_float(v, name):
         raise TypeError("must be real number, not %s (argument %s)" % (type(v).__name__, name))
 
 
+def first_spin_order(rng, nspins):
+    """``rng.permutation(range(nspins))`` taken into an int64 buffer as the reference does
+    (piqmc/qmc.pyx:90-91, :194-195; piqmc/sa.pyx:91-92, :158-159).  For nspins == 0 numpy
+    returns an empty float64 array (drawing nothing), and the reference's buffer assignment
+    raises ValueError there, before the schedule is read."""
+    cur = rng.permutation(range(nspins))
+    if cur.dtype.kind not in "iu":
+        raise ValueError("Buffer dtype mismatch, expected 'int_t' but got '%s' (first spin order)" % cur.dtype)
+    return cur
+
+
 def check_pm1(a, name):
     """The GPU kernels keep spins as int8 +-1; other values are rejected."""
     if a.size and not np.all((a == 1.0) | (a == -1.0)):

@@ -71,15 +71,12 @@ def _qa_reference(sched, mcsteps, slices, temp, nspins, confs, nbs, rng):
     bad = ((live < 0) | (live >= n_rows)) & (live != np.arange(nspins)[:, None])
     if np.any(bad):
         raise ValueError("neighbour index outside [0, %d)" % n_rows)
-    cur = rng.permutation(range(nspins))
+    cur = _buffers.first_spin_order(rng, nspins)
     nsched = sched.size
     if nsched == 0:
         return None
     if np.float32(slices) * temp == 0:
         raise ZeroDivisionError("float division")
-    if nspins == 0:
-        _reference_perms(rng, cur, nsched * mcsteps, 0)
-        return None
     jp = reforder.jperp_schedule(sched, slices, temp)
     spins = torch.from_numpy(np.ascontiguousarray(confs[:, :slices]).astype(np.int8)[None]).to(_device.device())
     upd_per_g = max(1, nspins * slices * mcsteps)
@@ -138,15 +135,12 @@ def QuantumAnneal_dense(sched, mcsteps, slices, temp, nspins, confs, J, rng, *, 
         raise ValueError("J must be at least nspins x nspins")
     if mode == "fast":
         return _qa_dense_fast(sched, mcsteps, slices, temp, nspins, confs, J, rng, seed, recompute_every)
-    cur = rng.permutation(range(nspins))
+    cur = _buffers.first_spin_order(rng, nspins)
     nsched = sched.size
     if nsched == 0:
         return None
     if np.float32(slices) * temp == 0:
         raise ZeroDivisionError("float division")
-    if nspins == 0:
-        _reference_perms(rng, cur, nsched * mcsteps, 0)
-        return None
     jp = reforder.jperp_schedule(sched, slices, temp)
     Jn = np.ascontiguousarray(J[:nspins, :nspins])
     spins = torch.from_numpy(np.ascontiguousarray(confs[:nspins, :slices]).astype(np.int8)[None]).to(

@@ -87,11 +87,9 @@ def Anneal(sched, mcsteps, svec, nbs, rng, *, mode="reference", seed=None):
     bad = ((idx < 0) | (idx >= nspins)) & (idx != np.arange(nspins)[:, None])
     if np.any(bad):
         raise ValueError("neighbour index outside [0, %d)" % nspins)
-    cur = rng.permutation(range(nspins))
+    cur = _buffers.first_spin_order(rng, nspins)
     nsched = sched.size
-    if nsched == 0 or nspins == 0:
-        for _ in range(nsched * mcsteps if nspins == 0 else 0):
-            cur = rng.permutation(cur)
+    if nsched == 0:
         return None
     spins = torch.from_numpy(svec.astype(np.int8)[None]).to(_device.device())
     gchunk = max(1, CHUNK_UPDATES // max(1, nspins * mcsteps))
@@ -144,11 +142,9 @@ def Anneal_dense(sched, mcsteps, svec, J, rng):
     _buffers.check_pm1(svec, "svec")
     if nspins and (J.shape[0] < nspins or J.shape[1] < nspins):
         raise ValueError("J is %r, smaller than svec.size=%d" % (J.shape, nspins))
-    cur = rng.permutation(range(nspins))
+    cur = _buffers.first_spin_order(rng, nspins)
     nsched = sched.size
-    if nsched == 0 or nspins == 0:
-        for _ in range(nsched * mcsteps if nspins == 0 else 0):
-            cur = rng.permutation(cur)
+    if nsched == 0:
         return None
     Jc = np.ascontiguousarray(J[:nspins, :nspins])
     spins = torch.from_numpy(svec.astype(np.int8)[None]).to(_device.device())
