@@ -51,8 +51,8 @@ def QuantumAnneal(sched, mcsteps, slices, temp, nspins, confs, nbs, rng, *, mode
 
 def _validate(sched, mcsteps, slices, nspins, confs):
     n_rows, ncols = confs.shape
-    if mcsteps < 0 or nspins < 0:
-        raise ValueError("mcsteps and nspins must be non-negative")
+    if nspins < 0:
+        raise ValueError("nspins must be non-negative")
     if slices < 2:
         raise ValueError("slices must be >= 2 (the reference reads slices P-1 and 1)")
     if nspins > n_rows or slices > ncols:
@@ -77,6 +77,8 @@ def _qa_reference(sched, mcsteps, slices, temp, nspins, confs, nbs, rng):
         return None
     if np.float32(slices) * temp == 0:
         raise ZeroDivisionError("float division")
+    if mcsteps <= 0:  # the reference's sweep loop runs no sweep and draws no order
+        return None
     jp = reforder.jperp_schedule(sched, slices, temp)
     spins = torch.from_numpy(np.ascontiguousarray(confs[:, :slices]).astype(np.int8)[None]).to(_device.device())
     upd_per_g = max(1, nspins * slices * mcsteps)
@@ -141,6 +143,8 @@ def QuantumAnneal_dense(sched, mcsteps, slices, temp, nspins, confs, J, rng, *, 
         return None
     if np.float32(slices) * temp == 0:
         raise ZeroDivisionError("float division")
+    if mcsteps <= 0:  # the reference's sweep loop runs no sweep and draws no order
+        return None
     jp = reforder.jperp_schedule(sched, slices, temp)
     Jn = np.ascontiguousarray(J[:nspins, :nspins])
     spins = torch.from_numpy(np.ascontiguousarray(confs[:nspins, :slices]).astype(np.int8)[None]).to(
@@ -166,6 +170,8 @@ def _qa_dense_fast(sched, mcsteps, slices, temp, nspins, confs, J, rng, seed, re
         raise ValueError("mode='fast' needs 1 <= slices <= 32")
     if temp <= 0:
         raise ValueError("mode='fast' needs temp > 0")
+    if mcsteps < 0:
+        raise ValueError("mode='fast' needs mcsteps >= 0")
     if nspins == 0 or sched.size == 0 or mcsteps == 0:
         return None
     _buffers.check_pm1(confs[:, :slices], "confs")

@@ -74,8 +74,6 @@ def Anneal(sched, mcsteps, svec, nbs, rng, *, mode="reference", seed=None):
     svec = _buffers.float64_buffer(svec, 1, "svec", writable=True)
     nbs = _buffers.float64_buffer(nbs, 3, "nbs")
     nspins = svec.size
-    if mcsteps < 0:
-        raise ValueError("mcsteps must be non-negative")
     _buffers.check_pm1(svec, "svec")
     if nspins and nbs.shape[0] < nspins:
         raise ValueError("nbs has %d rows, fewer than svec.size=%d" % (nbs.shape[0], nspins))
@@ -89,7 +87,7 @@ def Anneal(sched, mcsteps, svec, nbs, rng, *, mode="reference", seed=None):
         raise ValueError("neighbour index outside [0, %d)" % nspins)
     cur = _buffers.first_spin_order(rng, nspins)
     nsched = sched.size
-    if nsched == 0:
+    if nsched == 0 or mcsteps <= 0:  # the reference's sweep loop runs no sweep and draws no order
         return None
     spins = torch.from_numpy(svec.astype(np.int8)[None]).to(_device.device())
     gchunk = max(1, CHUNK_UPDATES // max(1, nspins * mcsteps))
@@ -109,6 +107,8 @@ def Anneal(sched, mcsteps, svec, nbs, rng, *, mode="reference", seed=None):
 
 def _anneal_fast(sched, mcsteps, svec, nbs, rng, seed):
     nspins = svec.size
+    if mcsteps < 0:
+        raise ValueError("mode='fast' needs mcsteps >= 0")
     if nspins == 0:
         return None
     temps = np.asarray(sched, dtype=np.float64).astype(np.float32)
@@ -137,14 +137,12 @@ def Anneal_dense(sched, mcsteps, svec, J, rng):
     svec = _buffers.float64_buffer(svec, 1, "svec", writable=True)
     J = _buffers.float64_buffer(J, 2, "J")
     nspins = svec.size
-    if mcsteps < 0:
-        raise ValueError("mcsteps must be non-negative")
     _buffers.check_pm1(svec, "svec")
     if nspins and (J.shape[0] < nspins or J.shape[1] < nspins):
         raise ValueError("J is %r, smaller than svec.size=%d" % (J.shape, nspins))
     cur = _buffers.first_spin_order(rng, nspins)
     nsched = sched.size
-    if nsched == 0:
+    if nsched == 0 or mcsteps <= 0:  # the reference's sweep loop runs no sweep and draws no order
         return None
     Jc = np.ascontiguousarray(J[:nspins, :nspins])
     spins = torch.from_numpy(svec.astype(np.int8)[None]).to(_device.device())
@@ -180,14 +178,12 @@ def Anneal_bipartite(sched, mcsteps, lvec, rvec, J, lbias, rbias, rng):
     lbias = _buffers.float64_buffer(lbias, 1, "lbias")
     rbias = _buffers.float64_buffer(rbias, 1, "rbias")
     nl, nr = lvec.size, rvec.size
-    if mcsteps < 0:
-        raise ValueError("mcsteps must be non-negative")
     _buffers.check_pm1(lvec, "lvec")
     _buffers.check_pm1(rvec, "rvec")
     if nl and nr and (J.shape[0] < nl or J.shape[1] < nr or lbias.size < nl or rbias.size < nr):
         raise ValueError("J must be at least (%d, %d) and the biases as long as the spin vectors" % (nl, nr))
     nsched = sched.size
-    if nsched == 0 or mcsteps == 0 or nl + nr == 0:
+    if nsched == 0 or mcsteps <= 0 or nl + nr == 0:
         return None
     spins = torch.from_numpy(np.concatenate([lvec, rvec]).astype(np.int8)[None]).to(_device.device())
     Jc = np.ascontiguousarray(J[:nl, :nr]) if nl and nr else np.zeros((max(nl, 1), max(nr, 1)))

@@ -68,6 +68,14 @@ def _cases():
         "qa_no_spins": ("QuantumAnneal", [sched, 2, P, 0.05, 0, confs, nbs, RNG]),
         "qa_no_spins_empty_sched": ("QuantumAnneal", [np.zeros(0), 2, P, 0.0, 0, confs, nbs, RNG]),
         "qa_mcsteps_str": ("QuantumAnneal", [sched, "1", P, 0.05, N, confs, nbs, RNG]),
+        "qa_mcsteps_0": ("QuantumAnneal", [sched, 0, P, 0.05, N, confs, nbs, RNG]),
+        "qa_mcsteps_neg": ("QuantumAnneal", [sched, -2, P, 0.05, N, confs, nbs, RNG]),
+        "qa_mcsteps_0_zero_temp": ("QuantumAnneal", [sched, 0, P, 0.0, N, confs, nbs, RNG]),
+        "qad_mcsteps_neg": ("QuantumAnneal_dense", [sched, -1, P, 0.05, N, confs, Jd, RNG]),
+        "sa_mcsteps_neg": ("Anneal", [sched, -3, svec, nbs, RNG]),
+        "sad_mcsteps_0": ("Anneal_dense", [sched, 0, svec, Jd, RNG]),
+        "sab_mcsteps_neg": ("Anneal_bipartite", [sched, -1, svec[:6].copy(), svec[6:].copy(), Jd[:6, 6:].copy(),
+                                                 Jd[0, :6].copy(), Jd[1, 6:].copy(), RNG]),
         "qa_temp_str": ("QuantumAnneal", [sched, 1, P, "hot", N, confs, nbs, RNG]),
         # QuantumAnneal_dense (reference piqmc/qmc.pyx:141)
         "qad_J_float32": ("QuantumAnneal_dense", [sched, 1, P, 0.05, N, confs, f32(Jd), RNG]),
