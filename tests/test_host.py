@@ -302,3 +302,27 @@ def test_tile_normalisation_and_sweep_variants():
         with pytest.raises(ValueError):
             batch.normalise_tile(bad, pb, 20)
     assert [batch.sweep_variant(P) for P in (1, 16, 20, 31, 32, 33, 64)] == [0, 16, 20, 0, 32, 1, 64]
+
+
+def test_autotune_cache_round_trip(tmp_path, monkeypatch):
+    """Rate tables persist as JSON keyed "gwarps,rpc,lanes"; older "gwarps,rpc" keys load as lanes 1."""
+    import json
+    from piqmc import autotune
+    path = tmp_path / "tune.json"
+    path.write_text(json.dumps({"GPU|64|16|4|8": {"1,8": 3.0e11, "2,1,2": 2.5e11}}))
+    monkeypatch.setenv("PIQMC_TUNE_CACHE", str(path))
+    monkeypatch.setattr(autotune, "_cache", {})
+    monkeypatch.setattr(autotune, "_loaded", False)
+    assert autotune.table() == {"GPU|64|16|4|8": {(1, 8, 1): 3.0e11, (2, 1, 2): 2.5e11}}
+    autotune._cache["GPU|128|20|4|8"] = {(8, 1, 1): 1.0e11}
+    autotune._save()
+    monkeypatch.setattr(autotune, "_cache", {})
+    monkeypatch.setattr(autotune, "_loaded", False)
+    tab = autotune.table()
+    assert tab["GPU|128|20|4|8"] == {(8, 1, 1): 1.0e11}
+    assert tab["GPU|64|16|4|8"][(1, 8, 1)] == 3.0e11
+    # an unreadable cache is ignored
+    path.write_text("{not json")
+    monkeypatch.setattr(autotune, "_cache", {})
+    monkeypatch.setattr(autotune, "_loaded", False)
+    assert autotune.table() == {}
