@@ -326,3 +326,29 @@ def test_autotune_cache_round_trip(tmp_path, monkeypatch):
     monkeypatch.setattr(autotune, "_cache", {})
     monkeypatch.setattr(autotune, "_loaded", False)
     assert autotune.table() == {}
+
+
+def test_product_has_no_fallback_and_no_oracle(monkeypatch, tmp_path):
+    """The package never reaches the oracle or working files, a missing library raises, and a
+    compute call without a CUDA device raises instead of running anywhere else."""
+    pkg = os.path.join(ROOT, "pathintegral-qmc_gb300")
+    pat = re.compile(r"^\s*(import|from)\s+(oracle|_work)\b|['\"/](oracle|_work)/", re.M)
+    for base, _, files in os.walk(pkg):
+        for f in files:
+            if f.endswith((".py", ".cu", ".cuh", ".cpp", ".h")):
+                text = open(os.path.join(base, f)).read()
+                assert not pat.search(text), os.path.join(base, f)
+    from piqmc import _native
+    monkeypatch.setattr(_native, "_lib", None)
+    monkeypatch.setattr(_native, "LIB_PATH", str(tmp_path / "missing.so"))
+    with pytest.raises(_native.NativeLibraryMissing):
+        _native.lib()
+    monkeypatch.undo()
+    import torch
+    if not torch.cuda.is_available():
+        from piqmc import qmc
+        g = np.random.default_rng(0)
+        nbs = oracle.generate_neighbors(16, lattice(4, True, g), 4)
+        with pytest.raises(_native.PiqmcError):
+            qmc.QuantumAnneal(np.linspace(1, 0.1, 3), 1, 4, 0.1, 16, np.ones((16, 4)), nbs,
+                              np.random.RandomState(0))
