@@ -117,3 +117,71 @@ def test_dense_fast_matches_corrected_reference():
     diff = f.mean() - r.mean()
     se = np.sqrt(f.var(ddof=1) / len(f) + r.var(ddof=1) / len(r))
     assert abs(diff) < 2.576 * se, (f.mean(), r.mean(), se)
+
+
+def _ci_agrees(f, r):
+    diff = f.mean() - r.mean()
+    se = np.sqrt(f.var(ddof=1) / len(f) + r.var(ddof=1) / len(r))
+    return abs(diff) < 2.576 * se, (f.mean(), r.mean(), se)
+
+
+def test_odd_slices_with_fields_match_corrected_reference():
+    """P = 7 (three slice classes: even k < 6, odd k, k = 6), fields, T = 0.3: the packed
+    algorithm against the corrected reference, 400 seeds, best-slice and slice-mean energies."""
+    from piqmc import fast, tools
+    g = np.random.default_rng(11)
+    J = lattice(6, True, g, dist=lambda r: r.normal(), fields=lambda r: r.normal(0.0, 0.5))
+    nbs = tools.GenerateNeighbors(36, J, 5)
+    prob = fast.Problem(nbs, on_device=False)
+    P, T, ns, n = 7, 0.3, 60, 36
+    sched = np.linspace(2.0, 1e-8, ns)
+    res = {"fast": [], "corrected": []}
+    for seed in range(400):
+        rs = np.random.default_rng(7000 + seed)
+        s0 = np.where(rs.random((n, P)) < 0.5, -1, 1).astype(np.int8)
+        w = np.zeros(prob.nslots, np.uint64)
+        w[prob.perm] = ((s0 < 0).astype(np.uint64) << np.arange(P, dtype=np.uint64)).sum(axis=1).astype(np.uint64)
+        oracle.fast_anneal(prob.nbr_host, prob.cpl_host, prob.field_host, prob.class_size, prob.class_stride, w,
+                           P, oracle.jperp(sched, P, T), 1, np.float32(1) / np.float32(T), seed, replica=seed)
+        sp = np.where((w[prob.perm][:, None] >> np.arange(P, dtype=np.uint64)) & 1, -1, 1)
+        res["fast"].append(_energies(J, P, sp))
+        sp = s0.copy()
+        perms = oracle.reference_perms(np.random.RandomState(seed), n, ns)
+        rands = rs.integers(0, 2 ** 31 - 1, size=n * P * ns, dtype=np.int64).astype(np.int32)
+        oracle.qa_sparse(sp, nbs, sched, 1, T, perms, rands, flags=3)
+        res["corrected"].append(_energies(J, P, sp))
+    f, r = np.array(res["fast"]), np.array(res["corrected"])
+    for stat in (lambda a: a.min(1), lambda a: a.mean(1)):
+        ok, info = _ci_agrees(stat(f), stat(r))
+        assert ok, info
+
+
+def test_packed_classical_annealer_matches_sa_anneal():
+    """P = 1 with a per-step inverse temperature (the packed form of sa.Anneal) against the
+    reference's sa.Anneal (no quirks to correct), 400 seeds; energies after a short and a full
+    schedule."""
+    from piqmc import fast, tools
+    g = np.random.default_rng(12)
+    J = lattice(8, True, g, fields=lambda r: r.uniform(-1.0, 1.0))
+    nbs = tools.GenerateNeighbors(64, J, 5)
+    prob = fast.Problem(nbs, on_device=False)
+    n = 64
+    for tsched in (np.linspace(5.0, 0.5, 8), np.linspace(5.0, 0.05, 60)):
+        betas = np.float32(1) / tsched.astype(np.float32)
+        res = {"fast": [], "sa": []}
+        for seed in range(400):
+            rs = np.random.default_rng(9000 + seed)
+            s0 = np.where(rs.random(n) < 0.5, -1, 1).astype(np.int8)
+            w = np.zeros(prob.nslots, np.uint64)
+            w[prob.perm] = (s0 < 0).astype(np.uint64)
+            oracle.fast_anneal(prob.nbr_host, prob.cpl_host, prob.field_host, prob.class_size, prob.class_stride, w,
+                               1, np.zeros(len(tsched), np.float32), 1, betas[0], seed, replica=seed, betas=betas)
+            sf = np.where(w[prob.perm] & 1, -1, 1)
+            res["fast"].append(oracle.classical_energy(sf.astype(np.float64), J))
+            s = s0.copy()
+            perms = oracle.reference_perms(np.random.RandomState(seed), n, len(tsched))
+            rands = rs.integers(0, 2 ** 31 - 1, size=n * len(tsched), dtype=np.int64).astype(np.int32)
+            oracle.sa_sparse(s, nbs, tsched, 1, perms, rands)
+            res["sa"].append(oracle.classical_energy(s.astype(np.float64), J))
+        ok, info = _ci_agrees(np.array(res["fast"]), np.array(res["sa"]))
+        assert ok, (tsched[-1], info)
