@@ -71,3 +71,36 @@ def test_packed_sweep_samples_the_exact_distribution(P, global_moves):
     means = np.array(means)
     est, se = means.mean(0), means.std(0, ddof=1) / np.sqrt(R)
     assert np.all(np.abs(est - exact) < 4.5 * se + 1e-3), (est, exact, se)
+
+
+@pytest.mark.parametrize("P", [2, 3, 4])
+def test_dense_sweep_samples_the_exact_distribution(P):
+    """The dense packed sweep (affine spin orders, incremental FP32 fields) on the same
+    triangle as a dense matrix: the same exact expectations."""
+    import math
+    J, _ = _problem()
+    Jd = np.asarray(J.todense())
+    up = np.triu(Jd, 1)
+    K = (up + up.T).astype(np.float32)
+    h = np.diag(Jd)
+    T, G = 1.0, 2.5
+    jp32 = oracle.jperp(np.array([G]), P, T).astype(np.float32)
+    exact = _exact(Jd, float(jp32[0]), P, T)
+    units = np.array([a for a in range(1, N) if math.gcd(a, N) == 1], np.int32)
+    R, burn, sweeps = 96, 100, 400
+    g = np.random.default_rng(500 + P)
+    means = []
+    for r in range(R):
+        s0 = np.where(g.random((N, P)) < 0.5, -1, 1)
+        w = ((s0 < 0).astype(np.uint32) << np.arange(P, dtype=np.uint32)).sum(1).astype(np.uint32)
+        F = (s0.T.astype(np.float64) @ K.T.astype(np.float64) + h[None, :]).astype(np.float32)
+        acc = []
+        for it in range(burn + sweeps):
+            _, F = oracle.dense_sweep(F, K, units, w, P, jp32, 1, np.float32(1) / np.float32(T), 91,
+                                      sweep_base=it, replica=r)
+            if it >= burn:
+                acc.append(np.where((w[:, None] >> np.arange(P, dtype=np.uint32)) & 1, -1.0, 1.0))
+        means.append(_observables(np.array(acc), Jd, float(jp32[0])).mean(0))
+    means = np.array(means)
+    est, se = means.mean(0), means.std(0, ddof=1) / np.sqrt(R)
+    assert np.all(np.abs(est - exact) < 4.5 * se + 1e-3), (est, exact, se)
