@@ -73,10 +73,11 @@ def test_packed_sweep_samples_the_exact_distribution(P, global_moves):
     assert np.all(np.abs(est - exact) < 4.5 * se + 1e-3), (est, exact, se)
 
 
-@pytest.mark.parametrize("P", [2, 3, 4])
-def test_dense_sweep_samples_the_exact_distribution(P):
-    """The dense packed sweep (affine spin orders, incremental FP32 fields) on the same
-    triangle as a dense matrix: the same exact expectations."""
+@pytest.mark.parametrize("P,per_slice", [(2, False), (3, False), (4, False), (4, True), (3, True)])
+def test_dense_sweep_samples_the_exact_distribution(P, per_slice):
+    """The dense packed sweep (affine spin orders shared by the slices or one per slice,
+    incremental FP32 fields) on the same triangle as a dense matrix: the same exact
+    expectations."""
     import math
     J, _ = _problem()
     Jd = np.asarray(J.todense())
@@ -97,7 +98,7 @@ def test_dense_sweep_samples_the_exact_distribution(P):
         acc = []
         for it in range(burn + sweeps):
             _, F = oracle.dense_sweep(F, K, units, w, P, jp32, 1, np.float32(1) / np.float32(T), 91,
-                                      sweep_base=it, replica=r)
+                                      sweep_base=it, replica=r, per_slice_order=per_slice)
             if it >= burn:
                 acc.append(np.where((w[:, None] >> np.arange(P, dtype=np.uint32)) & 1, -1.0, 1.0))
         means.append(_observables(np.array(acc), Jd, float(jp32[0])).mean(0))
