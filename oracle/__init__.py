@@ -55,7 +55,7 @@ def lib():
         L = ctypes.CDLL(LIB)
         P = ctypes.c_void_p
         i32, i64, f32 = ctypes.c_int, ctypes.c_int64, ctypes.c_float
-        L.orc_qa_sparse.argtypes = [i32, i32, i32, P, P, P, i32, i32, f32, P, P, i64, P, i32]
+        L.orc_qa_sparse.argtypes = [i32, i32, i32, i32, P, P, P, i32, i32, f32, P, P, i64, P, i32]
         L.orc_qa_sparse.restype = i64
         L.orc_qa_dense.argtypes = [i32, i32, P, P, i32, i32, f32, P, P, i64, P, i32]
         L.orc_qa_dense.restype = i64
@@ -155,7 +155,9 @@ def jperp(sched, P, temp):
 def qa_sparse(spins, nbs, sched, mcsteps, temp, perms, rands, flags=0):
     """Run the QuantumAnneal restatement on int8 spins (n, P), in place.
 
-    Returns the number of ``rands`` consumed (-1 when the stream ran out).
+    ``perms`` is (sweeps, nperm): each sweep updates the nperm <= n spins it lists (the
+    reference's ``nspins``); rows past them stay fixed.  Returns the number of ``rands``
+    consumed (-1 when the stream ran out).
     """
     n, P = spins.shape
     assert spins.dtype == np.int8 and spins.flags.c_contiguous
@@ -163,8 +165,8 @@ def qa_sparse(spins, nbs, sched, mcsteps, temp, perms, rands, flags=0):
     jp = jperp(sched, P, temp)
     perms = np.ascontiguousarray(perms, dtype=np.int64)
     rands = np.ascontiguousarray(rands, dtype=np.int32)
-    assert perms.shape == (len(sched) * mcsteps, n)
-    return lib().orc_qa_sparse(n, P, idx.shape[1], _p(idx), _p(jv), _p(jp), len(sched), mcsteps,
+    assert perms.ndim == 2 and perms.shape[0] == len(sched) * mcsteps and perms.shape[1] <= n
+    return lib().orc_qa_sparse(n, perms.shape[1], P, idx.shape[1], _p(idx), _p(jv), _p(jp), len(sched), mcsteps,
                                float(np.float32(temp)), _p(perms), _p(rands), len(rands),
                                _p(spins), flags)
 

@@ -47,8 +47,11 @@ static inline int metropolis(float ediff, float temp, int ge, const int32_t* ran
 
 /* qmc.QuantumAnneal, reference piqmc/qmc.pyx:30-136. flags = 0 reproduces the
  * shipped code (Q1: tidx never assigned, so tleft = P-1 and tright = 1 for
- * every slice, :115-117; Q2: ediff reset once per slice, :134-135). */
-int64_t orc_qa_sparse(int n, int P, int maxnb, const int32_t* nb_idx, const float* nb_j,
+ * every slice, :115-117; Q2: ediff reset once per slice, :134-135).  n rows of
+ * spins and neighbours; each sweep updates the nperm <= n spins its order lists
+ * (the reference's nspins argument, :91), so rows past them are read-only
+ * boundary spins; perms is [nsched*mcsteps][nperm]. */
+int64_t orc_qa_sparse(int n, int nperm, int P, int maxnb, const int32_t* nb_idx, const float* nb_j,
                       const float* jperp, int nsched, int mcsteps, float temp,
                       const int64_t* perms, const int32_t* rands, int64_t nrand,
                       int8_t* s, int flags) {
@@ -57,12 +60,12 @@ int64_t orc_qa_sparse(int n, int P, int maxnb, const int32_t* nb_idx, const floa
     for (int g = 0; g < nsched; ++g) {
         const float jp = jperp[g];
         for (int step = 0; step < mcsteps; ++step) {
-            const int64_t* perm = perms + (int64_t)(g * mcsteps + step) * n;
+            const int64_t* perm = perms + (int64_t)(g * mcsteps + step) * nperm;
             for (int k = 0; k < P; ++k) {
                 float ediff = 0.0f;
                 int tl = P - 1, tr = 1;
                 if (flags & ORC_FIX_Q1) { tl = (k + P - 1) % P; tr = (k + 1) % P; }
-                for (int t = 0; t < n; ++t) {
+                for (int t = 0; t < nperm; ++t) {
                     const int i = (int)perm[t];
                     if (flags & ORC_FIX_Q2) ediff = 0.0f;
                     const double si = (double)s[(int64_t)i * P + k];

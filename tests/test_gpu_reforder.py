@@ -359,6 +359,10 @@ def test_edge_cases(piqmc):
     out, used = rf.quantum_anneal(sp[None], idx, jv, np.linspace(1, 0.1, 4), 2, 0.2, perms[None], rands[None],
                                   nperm=10)
     np.testing.assert_array_equal(out.cpu().numpy()[0], confs.astype(np.int8))
+    # and the oracle (checked against the compiled reference for nspins < rows on the CPU)
+    so = np.ascontiguousarray(c2.astype(np.int8))
+    assert oracle.qa_sparse(so, nbs, np.linspace(1, 0.1, 4), 2, 0.2, perms, rands) == int(used[0])
+    np.testing.assert_array_equal(so, confs.astype(np.int8))
 
 
 def test_single_thread_kernels_beyond_shared_memory(piqmc):

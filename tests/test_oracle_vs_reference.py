@@ -178,3 +178,34 @@ def test_anneal_bipartite_random(case):
     np.testing.assert_array_equal(ls, lv.astype(np.int8))
     np.testing.assert_array_equal(rs, rv.astype(np.int8))
     assert rands[used] == next_rand
+
+
+@pytest.mark.parametrize("case", range(12))
+def test_quantum_anneal_fewer_spins_than_rows(case):
+    """nspins < rows: the sweep visits the first nspins spins only; the rows past them are
+    boundary spins that neighbours read and nothing writes (reference piqmc/qmc.pyx:91)."""
+    g = np.random.default_rng(6000 + case)
+    n, P = int(g.integers(4, 30)), int(g.integers(2, 7))
+    nspins = int(g.integers(1, n))
+    T = float(g.choice([0.05, 0.5, 2.0]))
+    J = _random_graph(g, n, fields=case % 2 == 1)
+    maxnb = int(max(np.count_nonzero(J.toarray()[i]) + np.count_nonzero(J.toarray()[:, i]) for i in range(n))) + 1
+    nbs = np.asarray(tools.GenerateNeighbors(n, J, maxnb))
+    sched = _temp_sched(g, 1e-6, 3.0)
+    conf0 = np.where(g.random((n, P)) < 0.5, -1.0, 1.0)
+    confs = np.asfortranarray(conf0.copy())
+    cseed, rseed = 57 + case, 570 + case
+    libc.srand(cseed)
+    rng = np.random.RandomState(rseed)
+    qmc.QuantumAnneal(sched, 2, P, T, nspins, confs, nbs, rng)
+    next_rand, next_rng = libc.rand(), rng.randint(2 ** 31)
+
+    rng = np.random.RandomState(rseed)
+    perms = oracle.reference_perms(rng, nspins, len(sched) * 2)
+    rands = oracle.libc_stream(cseed, nspins * P * len(sched) * 2 + 1)
+    sp = np.ascontiguousarray(conf0.astype(np.int8))
+    used = oracle.qa_sparse(sp, nbs, sched, 2, T, perms, rands)
+    np.testing.assert_array_equal(sp, confs.astype(np.int8))
+    np.testing.assert_array_equal(sp[nspins:], conf0[nspins:].astype(np.int8))
+    assert rands[used] == next_rand
+    assert rng.randint(2 ** 31) == next_rng
