@@ -9,7 +9,8 @@ consumed).  The instances are seeded synthetic ones with the shapes of the
 workloads the library is measured on; nothing is read from the reference's
 data files.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # every vector
+    python tests/golden/make_golden.py boundary   # only qa_boundary_rows.npz
 """
 import ctypes
 import os
@@ -187,5 +188,27 @@ def main():
     print("golden vectors written to", HERE)
 
 
+def boundary():
+    """QuantumAnneal with nspins below the row count: 6x6 periodic lattice, the first 24 spins
+    swept, the last 12 rows fixed boundary spins (reference piqmc/qmc.pyx:91)."""
+    g = np.random.default_rng(20150117)
+    J = lattice(6, True, lambda r: r.normal(), g, fields=lambda r: r.normal(0.0, 0.3))
+    nbs = np.asarray(tools.GenerateNeighbors(36, J, 5))
+    conf0 = np.where(g.random((36, 5)) < 0.5, -1.0, 1.0)
+    confs = np.asfortranarray(conf0.copy())
+    sched = np.linspace(2.0, 1e-6, 30)
+    libc.srand(71)
+    rng = np.random.RandomState(72)
+    qmc.QuantumAnneal(sched, 2, 5, 0.2, 24, confs, nbs, rng)
+    np.savez_compressed(os.path.join(HERE, "qa_boundary_rows.npz"), nbs=nbs, nspins=24, P=5, T=0.2, sched=sched,
+                        mcsteps=2, conf0=conf0, final=confs.astype(np.int8), cseed=71, rseed=72,
+                        next_rand=libc.rand(), next_rng=rng.randint(2 ** 31))
+    print("boundary-row vector written to", HERE)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["boundary"]:
+        boundary()
+    else:
+        main()
+        boundary()

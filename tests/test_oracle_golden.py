@@ -154,3 +154,20 @@ def test_expf_error_bound_sampled():
     L.orc_expf_max_relerr.restype = ctypes.c_double
     hi = int(np.array([-87.0], np.float32).view(np.uint32)[0])
     assert L.orc_expf_max_relerr(0x80000000, hi, 101) < 1e-7
+
+
+def test_qa_boundary_rows():
+    """nspins below the row count: the oracle sweeps the listed spins only and leaves the
+    boundary rows as they were, like the reference."""
+    g = golden("qa_boundary_rows")
+    nspins, P, sched, mcsteps, T = int(g["nspins"]), int(g["P"]), g["sched"], int(g["mcsteps"]), float(g["T"])
+    rng = np.random.RandomState(int(g["rseed"]))
+    perms = oracle.reference_perms(rng, nspins, len(sched) * mcsteps)
+    rands = oracle.libc_stream(int(g["cseed"]), nspins * P * len(sched) * mcsteps + 1)
+    sp = np.ascontiguousarray(g["conf0"].astype(np.int8))
+    used = oracle.qa_sparse(sp, g["nbs"], sched, mcsteps, T, perms, rands)
+    np.testing.assert_array_equal(sp, g["final"])
+    np.testing.assert_array_equal(sp[nspins:], g["conf0"][nspins:].astype(np.int8))
+    assert (sp[:nspins] != g["conf0"][:nspins]).any()
+    assert rands[used] == g["next_rand"]
+    assert rng.randint(2 ** 31) == g["next_rng"]
