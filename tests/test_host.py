@@ -352,3 +352,22 @@ def test_product_has_no_fallback_and_no_oracle(monkeypatch, tmp_path):
         with pytest.raises(_native.PiqmcError):
             qmc.QuantumAnneal(np.linspace(1, 0.1, 3), 1, 4, 0.1, 16, np.ones((16, 4)), nbs,
                               np.random.RandomState(0))
+
+
+def test_integration_bindings_match_the_header():
+    """Every ctypes argtypes list written out in INTEGRATION.md has one entry per parameter of the
+    header's declaration, of the matching kind (V pointer, I int, L int64_t, F float)."""
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    header = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "piqmc_gb300.h")).read(), flags=re.S)
+    bound = re.findall(r"lib\.(pq_\w+)\.argtypes = \[([^\]]*)\]", doc)
+    assert len(bound) >= 4
+    for name, items in bound:
+        decl = re.search(r"\b%s\s*\(([^)]*)\)\s*;" % name, header)
+        assert decl, name
+        params = [p.strip() for p in decl.group(1).split(",") if p.strip() and p.strip() != "void"]
+        want = []
+        for p in params:
+            t = p.rsplit(None, 1)[0] if "*" not in p else "*"
+            want.append("V" if "*" in p else {"int": "I", "int64_t": "L", "float": "F"}[t])
+        got = [x.strip() for x in items.split(",")]
+        assert got == want, (name, got, want)
