@@ -371,3 +371,30 @@ def test_integration_bindings_match_the_header():
             want.append("V" if "*" in p else {"int": "I", "int64_t": "L", "float": "F"}[t])
         got = [x.strip() for x in items.split(",")]
         assert got == want, (name, got, want)
+
+
+def test_ctypes_signatures_match_the_header():
+    """The package's ctypes table binds every header entry point with one argument per C
+    parameter of the matching kind and the declared return type."""
+    import ctypes
+    from piqmc import _native
+    header = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "piqmc_gb300.h")).read(), flags=re.S)
+    decls = {m.group(2): (m.group(1).strip(), m.group(3))
+             for m in re.finditer(r"([\w\s\*]+?)\b(pq_\w+)\s*\(([^)]*)\)\s*;", header)}
+    kinds = {"int": ctypes.c_int, "int64_t": ctypes.c_int64, "uint32_t": ctypes.c_uint32,
+             "uint64_t": ctypes.c_uint64, "float": ctypes.c_float}
+    assert set(decls) == set(_native.SIGNATURES), set(decls) ^ set(_native.SIGNATURES)
+    for name, (ret, plist) in decls.items():
+        res, args = _native.SIGNATURES[name]
+        params = [p.strip() for p in plist.split(",") if p.strip() and p.strip() != "void"]
+        assert len(args) == len(params), name
+        for p, a in zip(params, args):
+            if "*" in p:
+                assert a is ctypes.c_void_p or issubclass(a, ctypes._Pointer), (name, p, a)
+            else:
+                assert a is kinds[p.rsplit(None, 1)[0].replace("const ", "")], (name, p, a)
+        ret = ret.split()[-1]
+        want = {"int": ctypes.c_int, "int64_t": ctypes.c_int64, "char*": ctypes.c_char_p}.get(ret)
+        if ret.endswith("*"):
+            want = ctypes.c_char_p
+        assert res is want, (name, ret, res)
