@@ -398,3 +398,41 @@ def test_ctypes_signatures_match_the_header():
         if ret.endswith("*"):
             want = ctypes.c_char_p
         assert res is want, (name, ret, res)
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """Sizes and field offsets of the header's structs (compiled with gcc) against the ctypes
+    structures and numpy dtypes the package fills."""
+    import ctypes
+    import subprocess
+    from piqmc import _native, batch
+    fields = {
+        "pq_fast_params": [f for f, _ in _native.FastParams._fields_],
+        "pq_batch_run": [f for f, _ in _native.BatchRun._fields_],
+        "pq_batch_inst": ["tab_off", "field_off", "csize_off", "jperp_off", "n", "P", "maxdeg", "nclass", "stride",
+                          "key0", "key1", "pad_"],
+        "pq_batch_item": list(batch.ITEM_DTYPE.names),
+        "pq_batch_task": list(batch.TASK_DTYPE.names),
+    }
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "piqmc_gb300.h"', "int main(void) {"]
+    for s, fs in fields.items():
+        lines.append('printf("%s %%zu\\n", sizeof(%s));' % (s, s))
+        for f in fs:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (s, f, s, f))
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.check_call(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    got = dict(line.split() for line in subprocess.check_output([str(exe)]).decode().split("\n") if line)
+    got = {k: int(v) for k, v in got.items()}
+    for cls, s in ((_native.FastParams, "pq_fast_params"), (_native.BatchRun, "pq_batch_run")):
+        assert ctypes.sizeof(cls) == got[s], s
+        for f, _ in cls._fields_:
+            assert getattr(cls, f).offset == got["%s.%s" % (s, f)], (s, f)
+    for dt, s in ((batch.INST_DTYPE, "pq_batch_inst"), (batch.ITEM_DTYPE, "pq_batch_item"),
+                  (batch.TASK_DTYPE, "pq_batch_task")):
+        assert dt.itemsize == got[s], s
+        c_fields = fields[s]
+        for name, cf in zip(dt.names, c_fields):
+            assert dt.fields[name][1] == got["%s.%s" % (s, cf)], (s, name, cf)
