@@ -209,3 +209,22 @@ def test_quantum_anneal_fewer_spins_than_rows(case):
     np.testing.assert_array_equal(sp[nspins:], conf0[nspins:].astype(np.int8))
     assert rands[used] == next_rand
     assert rng.randint(2 ** 31) == next_rng
+
+
+@pytest.mark.parametrize("nl,nr", [(0, 7), (5, 0), (1, 1), (1, 30)])
+def test_anneal_bipartite_empty_and_tiny_sides(nl, nr):
+    g = np.random.default_rng(nl * 100 + nr)
+    Jb = g.normal(0.0, 1.0, (nl, nr))
+    lb, rb = g.normal(0.0, 0.3, nl), g.normal(0.0, 0.3, nr)
+    tsched = _temp_sched(g, 0.01, 5.0)
+    l0, r0 = np.where(g.random(nl) < 0.5, -1.0, 1.0), np.where(g.random(nr) < 0.5, -1.0, 1.0)
+    lv, rv = l0.copy(), r0.copy()
+    libc.srand(81)
+    sa.Anneal_bipartite(tsched, 2, lv, rv, Jb, lb, rb, np.random.RandomState(0))
+    next_rand = libc.rand()
+    rands = oracle.libc_stream(81, (nl + nr) * len(tsched) * 2 + 1)
+    ls, rs = l0.astype(np.int8), r0.astype(np.int8)
+    used = oracle.sa_bipartite(ls, rs, Jb, lb, rb, tsched, 2, rands)
+    np.testing.assert_array_equal(ls, lv.astype(np.int8))
+    np.testing.assert_array_equal(rs, rv.astype(np.int8))
+    assert rands[used] == next_rand
