@@ -11,10 +11,21 @@ Reference semantics restated here (file:line within hadsed/pathintegral-qmc):
 * ``qa_sparse``  -- ``qmc.QuantumAnneal``        piqmc/qmc.pyx:30-136
 * ``qa_dense``   -- ``qmc.QuantumAnneal_dense``  piqmc/qmc.pyx:141-242
 * ``sa_sparse``  -- ``sa.Anneal``                piqmc/sa.pyx:50-120
+* ``sa_dense``   -- ``sa.Anneal_dense``          piqmc/sa.pyx:126-187
+* ``sa_bipartite`` -- ``sa.Anneal_bipartite``    piqmc/sa.pyx:411-500
 * ``jperp``      -- J-perp formula               piqmc/qmc.pyx:95, piqmc/qmc.c:2063-2075
 * ``classical_energy`` -- ``sa.ClassicalIsingEnergy`` piqmc/sa.pyx:25-44
 * ``generate_neighbors`` -- ``tools.GenerateNeighbors`` piqmc/tools.pyx:28-96
 * ``reference_perms`` -- the ``rng.permutation`` calls of piqmc/qmc.pyx:90-91,136
+
+Pinned to the reference itself: the golden vectors in tests/golden/ were recorded from
+its compiled Cython code, and where that code is built here (oracle/build_ref.py)
+tests/test_oracle_vs_reference.py compares the two on random cases.
+
+``fast_oracle.c`` (``fast_anneal``, ``dense_sweep``, ``philox4x32_10``, ``expf_neg``)
+restates this library's own packed algorithms, which have no reference counterpart:
+it is the bit-exact check of those kernels, pinned by Philox's published known-answer
+vectors and, statistically, by the reference (tests/test_statistics.py).
 """
 import ctypes
 import os
