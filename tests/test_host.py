@@ -436,3 +436,18 @@ def test_struct_layouts_match_the_header(tmp_path):
         c_fields = fields[s]
         for name, cf in zip(dt.names, c_fields):
             assert dt.fields[name][1] == got["%s.%s" % (s, cf)], (s, name, cf)
+
+
+def test_documented_python_api_exists():
+    """Every ``module.name`` the Python examples in INTEGRATION.md and README.md use exists in
+    the package (file citations such as piqmc/qmc.pyx are not API references)."""
+    import importlib
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read() + open(os.path.join(ROOT, "README.md")).read()
+    mods = ("qmc", "sa", "tools", "fast", "batch", "autotune", "dense", "learned", "reforder", "tensor")
+    refs = set()
+    for block in re.findall(r"```python\n(.*?)```", text, re.S):
+        refs.update(re.findall(r"(?<![/\w])(%s)\.([A-Za-z_]\w*)(?!\w*:\d)" % "|".join(mods), block))
+    refs = {(m, a) for m, a in refs if a != "pyx"}
+    assert len(refs) >= 10
+    for m, a in sorted(refs):
+        assert hasattr(importlib.import_module("piqmc." + m), a), "%s.%s" % (m, a)
