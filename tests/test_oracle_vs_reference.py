@@ -228,3 +228,30 @@ def test_anneal_bipartite_empty_and_tiny_sides(nl, nr):
     np.testing.assert_array_equal(ls, lv.astype(np.int8))
     np.testing.assert_array_equal(rs, rv.astype(np.int8))
     assert rands[used] == next_rand
+
+
+@pytest.mark.parametrize("case", range(6))
+def test_quantum_anneal_dense_fewer_spins_than_rows(case):
+    """QuantumAnneal_dense with nspins < rows reads only the leading nspins x nspins block of J
+    and the first nspins rows of confs (reference piqmc/qmc.pyx:206), the cut the drop-in makes."""
+    g = np.random.default_rng(6500 + case)
+    n, P = int(g.integers(4, 25)), int(g.integers(2, 6))
+    nspins = int(g.integers(1, n))
+    Jd = np.triu(g.normal(0.0, 1.0, (n, n)), 1) + np.diag(g.normal(0.0, 0.5, n))
+    sched = _temp_sched(g, 1e-6, 3.0)
+    conf0 = np.where(g.random((n, P)) < 0.5, -1.0, 1.0)
+    confs = np.asfortranarray(conf0.copy())
+    libc.srand(91 + case)
+    rng = np.random.RandomState(910 + case)
+    qmc.QuantumAnneal_dense(sched, 1, P, 0.3, nspins, confs, Jd, rng)
+    next_rand, next_rng = libc.rand(), rng.randint(2 ** 31)
+
+    rng = np.random.RandomState(910 + case)
+    perms = oracle.reference_perms(rng, nspins, len(sched))
+    rands = oracle.libc_stream(91 + case, nspins * P * len(sched) + 1)
+    sp = np.ascontiguousarray(conf0[:nspins].astype(np.int8))
+    used = oracle.qa_dense(sp, np.ascontiguousarray(Jd[:nspins, :nspins]), sched, 1, 0.3, perms, rands)
+    np.testing.assert_array_equal(sp, confs[:nspins].astype(np.int8))
+    np.testing.assert_array_equal(confs[nspins:], conf0[nspins:])
+    assert rands[used] == next_rand
+    assert rng.randint(2 ** 31) == next_rng
