@@ -96,6 +96,10 @@ def _setup_fast(L):
     L.orc_philox4x32_10.restype = None
     L.orc_expf.argtypes = [f32]
     L.orc_expf.restype = f32
+    L.orc_u01.argtypes = [ctypes.c_uint32]
+    L.orc_u01.restype = f32
+    L.orc_expf_max.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
+    L.orc_expf_max.restype = f32
     L.orc_fast_anneal.argtypes = [i32, i32, i32, P, P, P, i32, i32, P, i32, P, i32, i32, f32, u64,
                                   i64, i32, i32, P, P]
     L.orc_fast_anneal.restype = i64
@@ -241,6 +245,18 @@ def philox4x32_10(ctr, key):
 
 def expf_neg(x):
     return np.float32(lib().orc_expf(float(np.float32(x))))
+
+
+def u01(r):
+    """The packed sweeps' uniform of a 32-bit Philox word: ((r >> 9) + 1/2) * 2^-23."""
+    return np.float32(lib().orc_u01(int(r) & 0xFFFFFFFF))
+
+
+def expf_neg_max(x_hi, x_lo):
+    """Largest expf_neg(x) over every FP32 x in [x_lo, x_hi] (both negative)."""
+    hi = int(np.float32(x_hi).view(np.uint32))
+    lo = int(np.float32(x_lo).view(np.uint32))
+    return np.float32(lib().orc_expf_max(hi, lo))
 
 
 def fast_anneal(nbr, cpl, field, class_size, class_stride, words, P, jperp, mcsteps, beta, seed,

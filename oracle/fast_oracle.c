@@ -22,7 +22,7 @@
  *  - update of spin i, slice k (FP32, one rounding per op, in order):
  *      e = s_i h_i; e += J_m s_i s_jm (m = 0..maxdeg-1); t = jp s_i s_{k-1} + jp s_i s_{k+1};
  *      ediff = -2 (e + t); flip if ediff > 0 or u < expf_neg(ediff * beta).
- *  - u = (r >> 9) * 2^-23, r = word (m & 3) of Philox4x32-10(ctr = {i, sweep, replica,
+ *  - u = ((r >> 9) + 1/2) * 2^-23, r = word (m & 3) of Philox4x32-10(ctr = {i, sweep, replica,
  *    q << 16 | m >> 2}, key = {seed lo, seed hi}) for the m-th slice of class q.
  *  - world-line move after the local sweeps of each schedule step: classes in order
  *    0..M-1, per spin E = sum_k e_k (FP32, k ascending), ediff = -2E, u from word 0 of
@@ -73,7 +73,21 @@ float orc_expf(float x) {
     return p * fbits((uint32_t)(n + 127) << 23);
 }
 
-static inline float u01(uint32_t r) { return fbits((r >> 9) | 0x3f800000u) - 1.0f; }
+/* u = (2 (r >> 9) + 1) * 2^-24: (1 + (r >> 9) * 2^-23) - (1 - 2^-24), exact in FP32 */
+static inline float u01(uint32_t r) { return fbits((r >> 9) | 0x3f800000u) - 0.999999940395355224609375f; }
+
+float orc_u01(uint32_t r) { return u01(r); }
+
+/* Largest orc_expf(x) over the FP32 inputs with bit patterns in [lo_bits, hi_bits]
+ * (negative floats: a larger pattern is more negative). */
+float orc_expf_max(uint32_t lo_bits, uint32_t hi_bits) {
+    float worst = 0.0f;
+    for (uint64_t b = lo_bits; b <= hi_bits; ++b) {
+        const float v = orc_expf(fbits((uint32_t)b));
+        if (v > worst) worst = v;
+    }
+    return worst;
+}
 
 static inline float signed_by(float v, uint64_t w, int k) {
     return ((w >> k) & 1) ? fbits(bitsf(v) ^ 0x80000000u) : v;

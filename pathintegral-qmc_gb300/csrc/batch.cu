@@ -19,7 +19,8 @@ __device__ __forceinline__ void run_task_item(const pq_batch_item& bi, const pq_
                                               const pq_batch_run& run, const int32_t* nbr_pool,
                                               const float* cpl_pool, const float* field_pool,
                                               const int32_t* csize_pool, const float* jperp_pool,
-                                              unsigned char* words_pool, unsigned char* smem, const Group& g,
+                                              unsigned char* words_pool, unsigned char* smem, const SiteQueue& q,
+                                              const Group& g,
                                               int lanes_per_site, bool& bad, unsigned long long& nacc) {
     Item it;
     it.nbr = nbr_pool + in.tab_off;
@@ -37,7 +38,7 @@ __device__ __forceinline__ void run_task_item(const pq_batch_item& bi, const pq_
     it.sweep_base = run.sweep_base;
     it.nsched = run.nsched; it.mcsteps = run.mcsteps; it.global_moves = run.global_moves;
     it.beta = run.beta;
-    run_item_any(it, smem + bi.smem_off, g, bad, nacc, lanes_per_site);
+    run_item_any(it, smem + bi.smem_off, q, g, bad, nacc, lanes_per_site);
 }
 
 __global__ void __launch_bounds__(256, 2) batch_kernel(const pq_batch_task* __restrict__ tasks, int ntasks,
@@ -49,6 +50,8 @@ __global__ void __launch_bounds__(256, 2) batch_kernel(const pq_batch_task* __re
                                                     unsigned long long* accepts, int32_t* status) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_task;
+    __shared__ uint32_t queue_slots[kQueuePerThread * 256];   // unsettled sites of a phase, per group
+    __shared__ int queue_count[2 * 8];
     bool bad = false;
     unsigned long long nacc = 0;
     for (;;) {
@@ -64,7 +67,8 @@ __global__ void __launch_bounds__(256, 2) batch_kernel(const pq_batch_task* __re
             const int gthr = task.gwarps * 32;
             const Group g{(int)threadIdx.x - gi * gthr, gthr,
                           (task.nitems == 1 && gthr == (int)blockDim.x) ? 0 : 1 + gi};
-            run_task_item(bi, in, run, nbr_pool, cpl_pool, field_pool, csize_pool, jperp_pool, words_pool, smem, g,
+            run_task_item(bi, in, run, nbr_pool, cpl_pool, field_pool, csize_pool, jperp_pool, words_pool, smem,
+                          SiteQueue{queue_slots + kQueuePerThread * gi * gthr, queue_count + 2 * gi}, g,
                           task.lanes_per_site, bad, nacc);
         }
         __syncthreads();

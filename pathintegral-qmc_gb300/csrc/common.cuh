@@ -77,9 +77,12 @@ __device__ __forceinline__ pq_u32x4 pq_philox_ks(pq_u32x4 c, const KS& ks) {
     return c;
 }
 
-// Uniform in [0, 1) with 23 random bits: (1 + (r >> 9) * 2^-23) - 1 = (r >> 9) * 2^-23, exact.
+// Uniform on the midpoints of 2^23 equal cells of (0, 1): u = ((r >> 9) + 1/2) * 2^-23 =
+// (2 (r >> 9) + 1) * 2^-24, computed exactly as (1 + (r >> 9) * 2^-23) - (1 - 2^-24).
+// Its smallest value is 2^-24, so a Metropolis test u < p with p <= 2^-24 rejects
+// whatever r is: such decisions need no random number.
 __device__ __forceinline__ float pq_u01(uint32_t r) {
-    return __fsub_rn(__uint_as_float((r >> 9) | 0x3f800000u), 1.0f);
+    return __fsub_rn(__uint_as_float((r >> 9) | 0x3f800000u), 0.999999940395355224609375f);
 }
 
 // Hardware 2^x approximation (MUFU), used only inside a guard band that makes the

@@ -32,6 +32,8 @@ __global__ void __launch_bounds__(512) qa_fast_kernel(W* __restrict__ words, con
                                                       int32_t* __restrict__ status) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int csize[kMaxClasses];
+    __shared__ uint32_t queue_slots[kQueuePerThread * 512];   // unsettled sites of a phase
+    __shared__ int queue_count[2];
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int c = 0; c < kMaxClasses; ++c) csize[c] = a.class_size[c];
@@ -54,7 +56,7 @@ __global__ void __launch_bounds__(512) qa_fast_kernel(W* __restrict__ words, con
     bool bad = false;
     unsigned long long nacc = 0;
     stage_in<W>(it, sw, g);   // also publishes csize
-    run_item<W, MAXDEG, NQC>(it, a.keys, sw, order, parity, g, bad, nacc);
+    run_item<W, MAXDEG, NQC>(it, a.keys, sw, order, parity, SiteQueue{queue_slots, queue_count}, g, bad, nacc);
     stage_out<W>(it, sw, g);
     if (bad) pq_set_status(status, PQ_ERR_BAD_INDEX);
     if (accepts) {

@@ -24,7 +24,7 @@
 //   e = s_i h_i;  e += J_im s_i s_jm for m = 0..maxdeg-1 (table order);
 //   t = (J-perp s_i s_{k-1}) + (J-perp s_i s_{k+1})      (exact);
 //   ediff = -2 (e + t);  flip if ediff > 0 or u < expf_neg(ediff * beta),
-// u = (r >> 9) * 2^-23.  Uniforms: Philox4x32-10, key = seed.  Local update:
+// u = ((r >> 9) + 1/2) * 2^-23.  Uniforms: Philox4x32-10, key = seed.  Local update:
 // counter = (device slot i, sweep, replica, q << 16 | m >> 2), word m & 3 for
 // the m-th slice of class q.  World-line move: counter = (i, last sweep of the
 // step, replica, 1 << 24 | gm << 16 | class), word 0.  Class order of a sweep:
@@ -238,36 +238,184 @@ __device__ __forceinline__ uint64_t update_fixed_half64(uint64_t wi, const uint6
     return ((uint64_t)f << sh) << q;
 }
 
+// Settled decisions.  The smallest uniform is 2^-24 (pq_u01), and expf_neg(x) <=
+// 2^-24 for every FP32 x <= kSettledX = -16.63553237915039 (bit pattern 0xc1851592;
+// checked over every float in [-87, kSettledX]; below -87 expf_neg is 0).  So an
+// update with sum >= 0 and fl(sum * m2beta) <= kSettledX rejects whatever its
+// uniform, and one with sum < 0 flips whatever its uniform.
+__device__ __forceinline__ float settled_x() { return __uint_as_float(0xc1851592u); }
+
+// Slice-class masks of P = 2 * NQ slices: bits of class 0 (even k), and the same
+// without its top bit (the bits b whose class successor b + 2 is in the class).
+template <typename W, int NQ>
+struct ClassMasks {
+    static constexpr W class0() {
+        W m = 0;
+        for (int k = 0; k < NQ; ++k) m |= (W)1 << (2 * k);
+        return m;
+    }
+    static constexpr W CM0 = class0();
+    static constexpr W IN0 = CM0 & ~((W)1 << (2 * NQ - 2));
+    static constexpr W MASK = 2 * NQ >= (int)(8 * sizeof(W)) ? ~(W)0 : (((W)1 << (2 * NQ)) - 1);
+};
+
+// Stage A of the local update of one site (compile-time P = 2 * NQC): a slice class
+// all of whose slices see the same neighbourhood -- own bit, neighbour bits and both
+// Trotter partners equal across the class -- has one energy sum for all of them.
+// When that sum settles the class (flip all, or reject all, see settled_x) it is
+// applied here without random numbers, which is exactly what the per-slice update
+// would do.  Classes are taken in the replica's parity order; returns the index qq
+// of the first class left unsettled (2 = the site is done).  A flip of a whole
+// class keeps every word straight on the other class, so the test of the second
+// class uses the neighbour words loaded once.
+template <typename W, int MAXDEG, int NQC, bool SPLIT>
+__device__ __forceinline__ int site_settle(const Item& it, W* rw, int i, uint32_t first, float jp, float m2beta,
+                                           int half, bool& bad, unsigned long long& nacc) {
+    using CMk = ClassMasks<W, NQC>;
+    constexpr int P = 2 * NQC;
+    W wi = rw[i];
+    W d[MAXDEG];
+    float J[MAXDEG];
+    load_site<W, MAXDEG>(rw, i, it.n, it.maxdeg, it.nbr, it.cpl, wi, d, J, bad);
+    const W w0 = wi;
+    if ((wi ^ (wi >> 2)) & (CMk::IN0 | (CMk::IN0 << 1))) return 0;
+    W nbx = 0;
+#pragma unroll
+    for (int m = 0; m < MAXDEG; ++m) nbx |= d[m] ^ (d[m] >> 2);
+    const float h = __ldg(it.field + i);
+    int qq = 0;
+    for (; qq < 2; ++qq) {
+        const int q = qq ^ (int)first;
+        if (nbx & (CMk::IN0 << q)) break;
+        const W up = ((wi << 1) | (wi >> (P - 1))) & CMk::MASK;   // bit k = s^{k-1}
+        const W dn = ((wi >> 1) | (wi << (P - 1))) & CMk::MASK;   // bit k = s^{k+1}
+        float e = flip_sign(h, bit_to_sign<W>(wi, q));
+#pragma unroll
+        for (int m = 0; m < MAXDEG; ++m) e = __fadd_rn(e, flip_sign(J[m], bit_to_sign<W>(d[m], q)));
+        const float t = __fadd_rn(flip_sign(jp, bit_to_sign<W>(wi ^ up, q)), flip_sign(jp, bit_to_sign<W>(wi ^ dn, q)));
+        const float sum = __fadd_rn(e, t);
+        W fl;
+        if (sum < 0.0f) fl = CMk::CM0 << q;
+        else if (__fmul_rn(sum, m2beta) <= settled_x()) fl = 0;
+        else break;
+        wi ^= fl;
+#pragma unroll
+        for (int m = 0; m < MAXDEG; ++m) d[m] ^= fl;
+        if (!SPLIT || half == 0)
+            nacc += sizeof(W) == 8 ? __popcll((unsigned long long)fl) : __popc((uint32_t)fl);
+    }
+    if (wi != w0 && (!SPLIT || half == 0)) rw[i] = wi;
+    return qq;
+}
+
+// The per-slice local update of one site from slice class qq0 on (all classes when
+// qq0 = 0): every slice draws its uniform and is decided on its own.
+template <typename W, int MAXDEG, int NQC, typename KS, bool SPLIT>
+__device__ __forceinline__ void site_update(const Item& it, const KS& ks, W* rw, int i, uint32_t rep, int qq0,
+                                            uint32_t first, int nclass_q, float jp, uint32_t sweep, float m2beta,
+                                            float m2blog2e, W mask, int half, unsigned pair_mask, bool& bad,
+                                            unsigned long long& nacc) {
+    const int P = it.P;
+    W wi = rw[i];
+    W d[MAXDEG];
+    float J[MAXDEG];
+    load_site<W, MAXDEG>(rw, i, it.n, it.maxdeg, it.nbr, it.cpl, wi, d, J, bad);
+    const float h = __ldg(it.field + i);
+    for (int qq = qq0; qq < nclass_q; ++qq) {
+        const int q = nclass_q == 2 ? (qq ^ (int)first) : qq;
+        W fl;
+        if constexpr (SPLIT) {
+            const W own = update_fixed_half64<MAXDEG, KS>(wi, d, J, h, jp, q, half, (uint32_t)i, sweep, rep, ks,
+                                                         m2beta, m2blog2e);
+            nacc += __popcll((unsigned long long)own);
+            fl = own | (W)__shfl_xor_sync(pair_mask, (unsigned long long)own, 1);
+        } else if constexpr (NQC > 0) {
+            fl = update_fixed<NQC, MAXDEG, W, KS>(wi, d, J, h, jp, q, (uint32_t)i, sweep, rep, ks, m2beta, m2blog2e);
+        } else {
+            W dl, dr;
+            trotter_diffs<W>(wi, P, mask, dl, dr);
+            fl = 0;
+            const int nq = slice_count(P, q);
+            for (int mb = 0; mb * 4 < nq; ++mb) {
+                const pq_u32x4 rnd = pq_philox_ks(pq_u32x4{(uint32_t)i, sweep, rep, (uint32_t)((q << 16) | mb)}, ks);
+                const uint32_t rw4[4] = {rnd.x, rnd.y, rnd.z, rnd.w};
+#pragma unroll
+                for (int jj = 0; jj < 4; ++jj) {
+                    const int mm = mb * 4 + jj;
+                    if (mm < nq) {
+                        const int k = slice_of(P, q, mm);
+                        float e = flip_sign(h, bit_to_sign<W>(wi, k));
+#pragma unroll
+                        for (int m = 0; m < MAXDEG; ++m)
+                            if (m < it.maxdeg) e = __fadd_rn(e, flip_sign(J[m], bit_to_sign<W>(d[m], k)));
+                        const float t = __fadd_rn(flip_sign(jp, bit_to_sign<W>(dl, k)),
+                                                  flip_sign(jp, bit_to_sign<W>(dr, k)));
+                        const bool acc = decide(__fadd_rn(e, t), pq_u01(rw4[jj]), m2beta, m2blog2e);
+                        fl |= (W)acc << k;
+                    }
+                }
+            }
+        }
+        // the neighbours are unchanged in this phase: only the spin's own bits move
+        wi ^= fl;
+#pragma unroll
+        for (int m = 0; m < MAXDEG; ++m) d[m] ^= fl;
+        if constexpr (!SPLIT) nacc += sizeof(W) == 8 ? __popcll((unsigned long long)fl) : __popc((uint32_t)fl);
+    }
+    if (half == 0) rw[i] = wi;
+}
+
+// Queue of unsettled sites of one group: kQueuePerThread entries per thread of the
+// group in shared memory, and two phase counters (used alternately).
+constexpr int kQueuePerThread = 2;
+
+struct SiteQueue {
+    uint32_t* slots;   // kQueuePerThread * group threads entries
+    int* count;        // [2]
+};
+
 // Anneal one item through its schedule.  sw: shared memory holding the item's
 // nrep x n words (staged by the caller); order: nrep x kMaxClasses bytes;
-// parity: nrep words.  Counts accepted local flips into nacc and out-of-range
-// indices into bad.
+// parity: nrep words; q: the group's queue.  Counts accepted local flips into
+// nacc and out-of-range indices into bad.
+//
+// Compile-time P (NQC > 0): each phase runs in two stages.  In stage A the
+// group walks the phase's sites and settles what site_settle can; the sites it
+// leaves are appended (warp-aggregated) to the group's queue as (slot, replica,
+// first unsettled slice class).  After a group barrier, stage B runs the
+// per-slice update on the queued sites, one per thread (lane pair), so the
+// per-slice work fills whole warps.  Sites of one phase share no coupling, so
+// which thread takes a site does not change any result; a site that finds the
+// queue full is updated at once by its own thread.
 //
 // SPLIT (64-bit words with P = 64 only): two adjacent lanes share each site, one
 // 32-bit half of the world-line each, and exchange their flips after every slice
 // class; the sweep's serial work per lane halves, its result is unchanged.
 template <typename W, int MAXDEG, int NQC, bool INLINE, typename KS, bool SPLIT = false>
 __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* sw, uint8_t* order, uint32_t* parity,
-                                              const Group& g, bool& bad, unsigned long long& nacc);
+                                              const SiteQueue& q, const Group& g, bool& bad,
+                                              unsigned long long& nacc);
 
 // The single-instance kernel inlines the item loop; the batched kernel calls one
 // out-of-line copy per variant, so each variant keeps its own register budget.
 template <typename W, int MAXDEG, int NQC>
 __device__ __forceinline__ void run_item(const Item& it, const PhiloxKeyTable& keys, W* sw, uint8_t* order,
-                                         uint32_t* parity, const Group& g, bool& bad, unsigned long long& nacc) {
-    run_item_body<W, MAXDEG, NQC, true, PhiloxKeysTab>(it, PhiloxKeysTab{keys}, sw, order, parity, g, bad, nacc);
+                                         uint32_t* parity, const SiteQueue& q, const Group& g, bool& bad,
+                                         unsigned long long& nacc) {
+    run_item_body<W, MAXDEG, NQC, true, PhiloxKeysTab>(it, PhiloxKeysTab{keys}, sw, order, parity, q, g, bad, nacc);
 }
 
 template <typename W, int MAXDEG, int NQC, bool SPLIT = false>
-__device__ __noinline__ void run_item_call(const Item& it, W* sw, uint8_t* order, uint32_t* parity, const Group& g,
-                                           bool& bad, unsigned long long& nacc) {
+__device__ __noinline__ void run_item_call(const Item& it, W* sw, uint8_t* order, uint32_t* parity,
+                                           const SiteQueue& q, const Group& g, bool& bad, unsigned long long& nacc) {
     run_item_body<W, MAXDEG, NQC, false, PhiloxKeysReg, SPLIT>(it, PhiloxKeysReg{it.key0, it.key1}, sw, order,
-                                                               parity, g, bad, nacc);
+                                                               parity, q, g, bad, nacc);
 }
 
 template <typename W, int MAXDEG, int NQC, bool INLINE, typename KS, bool SPLIT>
 __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* sw, uint8_t* order, uint32_t* parity,
-                                              const Group& g, bool& bad, unsigned long long& nacc) {
+                                              const SiteQueue& q, const Group& g, bool& bad,
+                                              unsigned long long& nacc) {
     const int n = it.n, P = it.P, S = it.stride, nrep = it.nrep;
     const W mask = full_mask<W>(P);
     const int nclass_q = P == 1 ? 1 : ((P & 1) ? 3 : 2);
@@ -277,6 +425,12 @@ __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* s
     const int site_nthr = SPLIT ? g.nthr >> 1 : g.nthr;
     const int half = SPLIT ? (g.tid & 1) : 0;
     const unsigned pair_mask = 3u << ((g.tid & 31) & ~1);
+    const uint32_t lane = (uint32_t)(g.tid & 31);
+    // queue rank below this site: lanes below this lane (below the pair's first lane for SPLIT)
+    const uint32_t lanes_below = (1u << (SPLIT ? (lane & ~1u) : lane)) - 1u;
+    const int qcap = kQueuePerThread * g.nthr;
+    uint32_t phase = 0;   // running phase count: picks the phase's queue counter
+    if (NQC > 0 && g.tid == 0) { q.count[0] = 0; q.count[1] = 0; }
     for (int gs = 0; gs < it.nsched; ++gs) {
         const float jp = P == 1 ? 0.0f : __ldg(it.jperp + gs);
         const float beta = it.betas ? __ldg(it.betas + gs) : it.beta;
@@ -303,69 +457,77 @@ __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* s
                     cls = order[rl * kMaxClasses + p];
                     cs = it.csize[cls];
                 }
-                for (; rl < nrep;) {
-                    {
-                        const int i = cls * S + s;
-                        W* rw = sw + rl * n;
-                        W wi = rw[i];
-                        W d[MAXDEG];
-                        float J[MAXDEG];
-                        load_site<W, MAXDEG>(rw, i, n, it.maxdeg, it.nbr, it.cpl, wi, d, J, bad);
-                        const float h = __ldg(it.field + i);
-                        const uint32_t rep = it.replica0 + rl;
-                        const uint32_t first = nclass_q == 2 ? (parity[rl] >> p) & 1u : 0u;
-                        for (int qq = 0; qq < nclass_q; ++qq) {
-                            const int q = nclass_q == 2 ? (qq ^ (int)first) : qq;
-                            W fl;
-                            if constexpr (SPLIT) {
-                                const W own = update_fixed_half64<MAXDEG, KS>(wi, d, J, h, jp, q, half, (uint32_t)i,
-                                                                             sweep, rep, ks, m2beta, m2blog2e);
-                                nacc += __popcll((unsigned long long)own);
-                                fl = own | (W)__shfl_xor_sync(pair_mask, (unsigned long long)own, 1);
-                            } else if constexpr (NQC > 0) {
-                                fl = update_fixed<NQC, MAXDEG, W, KS>(wi, d, J, h, jp, q, (uint32_t)i, sweep, rep, ks,
-                                                                      m2beta, m2blog2e);
-                            } else {
-                                W dl, dr;
-                                trotter_diffs<W>(wi, P, mask, dl, dr);
-                                fl = 0;
-                                const int nq = slice_count(P, q);
-                                for (int mb = 0; mb * 4 < nq; ++mb) {
-                                    const pq_u32x4 rnd = pq_philox_ks(
-                                        pq_u32x4{(uint32_t)i, sweep, rep, (uint32_t)((q << 16) | mb)}, ks);
-                                    const uint32_t rw4[4] = {rnd.x, rnd.y, rnd.z, rnd.w};
-#pragma unroll
-                                    for (int jj = 0; jj < 4; ++jj) {
-                                        const int mm = mb * 4 + jj;
-                                        if (mm < nq) {
-                                            const int k = slice_of(P, q, mm);
-                                            float e = flip_sign(h, bit_to_sign<W>(wi, k));
-#pragma unroll
-                                            for (int m = 0; m < MAXDEG; ++m)
-                                                if (m < it.maxdeg) e = __fadd_rn(e, flip_sign(J[m], bit_to_sign<W>(d[m], k)));
-                                            const float t = __fadd_rn(flip_sign(jp, bit_to_sign<W>(dl, k)),
-                                                                      flip_sign(jp, bit_to_sign<W>(dr, k)));
-                                            const bool acc = decide(__fadd_rn(e, t), pq_u01(rw4[jj]), m2beta, m2blog2e);
-                                            fl |= (W)acc << k;
-                                        }
-                                    }
+                if constexpr (NQC > 0) {
+                    int* cnt = q.count + (phase & 1u);
+                    // stage A: settle, queue the rest
+                    for (;;) {
+                        const bool active = rl < nrep;
+                        if (!__any_sync(0xffffffffu, active)) break;
+                        bool pend = false;
+                        uint32_t entry = 0;
+                        int site_i = 0, site_r = 0, site_qq = 2;
+                        if (active) {
+                            site_i = cls * S + s;
+                            site_r = rl;
+                            site_qq = site_settle<W, MAXDEG, NQC, SPLIT>(it, sw + rl * n, site_i,
+                                                                         (parity[rl] >> p) & 1u, jp, m2beta, half,
+                                                                         bad, nacc);
+                            pend = site_qq < 2;
+                            entry = (uint32_t)site_i | ((uint32_t)rl << 22) | ((uint32_t)site_qq << 30);
+                            s += site_nthr;
+                            while (s >= cs) {
+                                s -= cs;
+                                if (++rl == nrep) break;
+                                cls = order[rl * kMaxClasses + p];
+                                cs = it.csize[cls];
+                            }
+                        }
+                        const unsigned bal = __ballot_sync(0xffffffffu, pend && half == 0);
+                        if (bal) {
+                            const int leader = __ffs(bal) - 1;
+                            int base = 0;
+                            if ((int)lane == leader) base = atomicAdd(cnt, __popc(bal));
+                            base = __shfl_sync(0xffffffffu, base, leader);
+                            const int slot = base + __popc(bal & lanes_below);
+                            if (pend) {
+                                if (slot < qcap) {
+                                    if (half == 0) q.slots[slot] = entry;
+                                } else {   // queue full: update the site now
+                                    site_update<W, MAXDEG, NQC, KS, SPLIT>(it, ks, sw + site_r * n, site_i,
+                                                                           it.replica0 + site_r, site_qq,
+                                                                           (parity[site_r] >> p) & 1u, 2, jp, sweep,
+                                                                           m2beta, m2blog2e, mask, half, pair_mask,
+                                                                           bad, nacc);
                                 }
                             }
-                            // the neighbours are unchanged in this phase: only the spin's own bits move
-                            wi ^= fl;
-#pragma unroll
-                            for (int m = 0; m < MAXDEG; ++m) d[m] ^= fl;
-                            if constexpr (!SPLIT)
-                                nacc += sizeof(W) == 8 ? __popcll((unsigned long long)fl) : __popc((uint32_t)fl);
                         }
-                        if (half == 0) rw[i] = wi;
                     }
-                    s += site_nthr;
-                    while (s >= cs) {
-                        s -= cs;
-                        if (++rl == nrep) break;
-                        cls = order[rl * kMaxClasses + p];
-                        cs = it.csize[cls];
+                    // the other counter's last reader finished before this phase began
+                    if (g.tid == 0) q.count[(phase + 1u) & 1u] = 0;
+                    group_sync(g);
+                    // stage B: the per-slice update of the queued sites, one per thread (lane pair)
+                    const int nq = min(*cnt, qcap);
+                    for (int e = site_tid; e < nq; e += site_nthr) {
+                        const uint32_t en = q.slots[e];
+                        const int i = (int)(en & 0x3FFFFFu), r = (int)((en >> 22) & 0xFFu), qq0 = (int)(en >> 30);
+                        site_update<W, MAXDEG, NQC, KS, SPLIT>(it, ks, sw + r * n, i, it.replica0 + r, qq0,
+                                                               (parity[r] >> p) & 1u, 2, jp, sweep, m2beta,
+                                                               m2blog2e, mask, half, pair_mask, bad, nacc);
+                    }
+                    ++phase;
+                } else {
+                    for (; rl < nrep;) {
+                        const uint32_t first = nclass_q == 2 ? (parity[rl] >> p) & 1u : 0u;
+                        site_update<W, MAXDEG, NQC, KS, SPLIT>(it, ks, sw + rl * n, cls * S + s, it.replica0 + rl, 0,
+                                                               first, nclass_q, jp, sweep, m2beta, m2blog2e, mask,
+                                                               half, pair_mask, bad, nacc);
+                        s += site_nthr;
+                        while (s >= cs) {
+                            s -= cs;
+                            if (++rl == nrep) break;
+                            cls = order[rl * kMaxClasses + p];
+                            cs = it.csize[cls];
+                        }
                     }
                 }
                 group_sync(g);
@@ -427,7 +589,7 @@ __device__ __forceinline__ void stage_out(const Item& it, const W* sw, const Gro
 }
 
 // Word type / degree / compile-time P dispatch of one item.
-__device__ inline void run_item_any(const Item& it, unsigned char* smem, const Group& g, bool& bad,
+__device__ inline void run_item_any(const Item& it, unsigned char* smem, const SiteQueue& q, const Group& g, bool& bad,
                                     unsigned long long& nacc, int lanes_per_site = 1) {
     // layout of the item's shared memory: words, then order bytes, then parity words
     const size_t wbytes = it.P <= 32 ? 4 : 8;
@@ -437,20 +599,20 @@ __device__ inline void run_item_any(const Item& it, unsigned char* smem, const G
     if (it.P <= 32) {
         uint32_t* sw = reinterpret_cast<uint32_t*>(smem);
         stage_in<uint32_t>(it, sw, g);
-        if (it.maxdeg == 4 && it.P == 20) run_item_call<uint32_t, 4, 10>(it, sw, order, parity, g, bad, nacc);
-        else if (it.maxdeg == 4 && it.P == 16) run_item_call<uint32_t, 4, 8>(it, sw, order, parity, g, bad, nacc);
-        else if (it.maxdeg == 4 && it.P == 32) run_item_call<uint32_t, 4, 16>(it, sw, order, parity, g, bad, nacc);
-        else if (it.maxdeg <= 4) run_item_call<uint32_t, 4, 0>(it, sw, order, parity, g, bad, nacc);
-        else run_item_call<uint32_t, 8, 0>(it, sw, order, parity, g, bad, nacc);
+        if (it.maxdeg == 4 && it.P == 20) run_item_call<uint32_t, 4, 10>(it, sw, order, parity, q, g, bad, nacc);
+        else if (it.maxdeg == 4 && it.P == 16) run_item_call<uint32_t, 4, 8>(it, sw, order, parity, q, g, bad, nacc);
+        else if (it.maxdeg == 4 && it.P == 32) run_item_call<uint32_t, 4, 16>(it, sw, order, parity, q, g, bad, nacc);
+        else if (it.maxdeg <= 4) run_item_call<uint32_t, 4, 0>(it, sw, order, parity, q, g, bad, nacc);
+        else run_item_call<uint32_t, 8, 0>(it, sw, order, parity, q, g, bad, nacc);
         stage_out<uint32_t>(it, sw, g);
     } else {
         uint64_t* sw = reinterpret_cast<uint64_t*>(smem);
         stage_in<uint64_t>(it, sw, g);
         if (it.maxdeg == 4 && it.P == 64 && lanes_per_site == 2)
-            run_item_call<uint64_t, 4, 32, true>(it, sw, order, parity, g, bad, nacc);
-        else if (it.maxdeg == 4 && it.P == 64) run_item_call<uint64_t, 4, 32>(it, sw, order, parity, g, bad, nacc);
-        else if (it.maxdeg <= 4) run_item_call<uint64_t, 4, 0>(it, sw, order, parity, g, bad, nacc);
-        else run_item_call<uint64_t, 8, 0>(it, sw, order, parity, g, bad, nacc);
+            run_item_call<uint64_t, 4, 32, true>(it, sw, order, parity, q, g, bad, nacc);
+        else if (it.maxdeg == 4 && it.P == 64) run_item_call<uint64_t, 4, 32>(it, sw, order, parity, q, g, bad, nacc);
+        else if (it.maxdeg <= 4) run_item_call<uint64_t, 4, 0>(it, sw, order, parity, q, g, bad, nacc);
+        else run_item_call<uint64_t, 8, 0>(it, sw, order, parity, q, g, bad, nacc);
         stage_out<uint64_t>(it, sw, g);
     }
 }
