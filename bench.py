@@ -35,6 +35,8 @@ for _p in (ROOT, os.path.join(ROOT, "pathintegral-qmc_gb300")):
 
 import numpy as np  # noqa: E402
 
+from piqmc import shard  # noqa: E402  (replica sharding over ranks)
+
 L_SIDE, P_SLICES, TEMP, NSCHED, REPLICAS = 80, 20, 0.05, 2000, 1024
 FLOP_PER_UPDATE = 14   # 2(z+2)+2 FP32 flop per update at z = 4 (z coupling adds, 2 Trotter, x 1/T, exp)
 METRIC = "spin-slice updates/s"
@@ -52,36 +54,13 @@ BENCH_SEED = 7
 
 
 def rank_plan(rank, world, R):
-    """Rank `rank` of `world` anneals the global replicas [rank R, (rank + 1) R) with the job's Philox key.
-
-    A replica's stream depends only on (key, global replica id, sweep), so the
-    union of the ranks' results equals one process annealing all world x R
-    replicas; the only collective is the max-over-ranks timing reduction."""
-    if not 0 <= rank < world or R <= 0:
-        raise ValueError("bad rank plan: rank %d of %d, %d replicas" % (rank, world, R))
-    return {"replica_base": rank * R, "replicas": R, "seed": BENCH_SEED, "total_replicas": world * R}
+    """Rank `rank` of `world` anneals the global replicas [rank R, (rank + 1) R) with the bench's key."""
+    return shard.rank_plan(rank, world, R, BENCH_SEED)
 
 
-def initial_spins(replica_base, R, n, seed=1234):
-    """+-1 start vectors of global replicas replica_base .. replica_base + R - 1 (the same on any rank layout)."""
-    out = np.empty((R, n), dtype=np.int8)
-    for j in range(R):
-        g = np.random.default_rng([seed, replica_base + j])
-        out[j] = np.where(g.random(n) < 0.5, -1, 1)
-    return out
-
-
-def max_over_ranks(x, dist, device):
-    """The largest of the ranks' values of x (the job's time is its slowest rank's)."""
-    import torch
-    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
-
-
-def whole_job_rate(units_per_rank_step, steps, world, total_s):
-    """Units all ranks processed / the slowest rank's time."""
-    return units_per_rank_step * steps * world / total_s
+initial_spins = shard.initial_spins
+max_over_ranks = shard.max_over_ranks
+whole_job_rate = shard.whole_job_rate
 
 
 def instance_arrays(seed=2026):
@@ -250,9 +229,12 @@ class ClockSampler:
 # GPU arm
 # ------------------------------------------------------------------------------------------
 
-def measured_fp32_peak(lib, torch):
-    """FP32 FMA throughput of this GPU in TFLOP/s (in-run probe kernel, best of 5)."""
+def measured_fp32_peak(torch):
+    """FP32 FMA throughput of this GPU in TFLOP/s (in-run probe kernel of tests/native, best of 5)."""
     from piqmc import _device
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from native import probes
+    lib = probes.lib()
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     blocks, threads, iters = sms * 8, 256, 4096
     out = torch.empty(blocks, device="cuda")
@@ -260,7 +242,7 @@ def measured_fp32_peak(lib, torch):
     for _ in range(6):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        lib.pq_fp32_fma_probe(_device.ptr(out), iters, blocks, threads, _device.stream_handle())
+        lib.pqt_fp32_fma_probe(_device.ptr(out), iters, blocks, threads, _device.stream_handle())
         e1.record()
         torch.cuda.synchronize()
         best = max(best, blocks * threads * iters * 8 * 2 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
@@ -368,7 +350,7 @@ def gpu_arm(args):
         learnedw = learned_vs_plain(args, torch, prob, R=args.learned_replicas)
         reforderw = reforder_workload(args, torch)
 
-    peak = measured_fp32_peak(lib, torch)
+    peak = measured_fp32_peak(torch)
     achieved_tflops = value / world * FLOP_PER_UPDATE / 1e12
     ms_per_step = total_s / args.steps * 1e3
     traffic, issue = None, None

@@ -280,14 +280,18 @@ int pq_batch_anneal(const pq_batch_task* tasks, int ntasks, const pq_batch_item*
                     const float* field_pool, const int32_t* csize_pool, const float* jperp_pool,
                     void* words_pool, int* queue_head, const pq_batch_run* run, int grid, int threads,
                     int smem_bytes, unsigned long long* accepts, int32_t* status, void* stream);
+/* (pq_batch_anneal rejects ntasks + grid > 2^31 - 1 with PQ_ERR_TOO_LARGE: its
+ * 32-bit task counter would wrap.) */
 /* No counterpart in the reference.  The same batched anneal for callers that
  * cannot allocate device memory -- for instance a host application that hands
  * this library only its own input and output buffers, or code running where
  * cudaMalloc is not allowed -- so it has no queue_head argument: the task counter
  * lives in a 256-byte static device array of this library (held on every GPU
  * that loads it until the process exits).  The first call on each device looks
- * that array's address up (cudaGetSymbolAddress), so make the first call on a
- * device before any stream capture.  Each call resets the counter; all calls
+ * that array's address up (cudaGetSymbolAddress), and so does the first call
+ * after the device's context was reset, so make those calls before any stream
+ * capture.  ntasks < 0 or grid <= 0 is PQ_ERR_INVALID_ARG, as for
+ * pq_batch_anneal.  Each call resets the counter; all calls
  * share it, so calls that overlap on the GPU (other streams, other threads) race
  * and must be serialised by the caller.  Limit: ntasks + grid <= 2^31 - 1 (the
  * counter is 32-bit), else PQ_ERR_TOO_LARGE.  Allocates nothing. */
@@ -330,6 +334,17 @@ int pq_dense_sweep(uint32_t* words, float* F, int ldf, const float* K, const int
                    const float* jperp, int N, int P, int R, int nsched, int mcsteps, float beta, uint64_t seed,
                    int64_t sweep_base, int replica_base, int per_slice_order, unsigned long long* accepts,
                    int32_t* status, void* stream);
+/* pq_dense_sweep with its wavefront waits under the caller's control: a warp
+ * polls a neighbour's progress at most poll_limit times (< 0: the default,
+ * 2^24 polls of ~64 ns) before it gives up, records PQ_ERR_TIMEOUT, releases
+ * the warps that wait on it and returns.  wait_skew (0 in use, at most 2^24) is
+ * added to every awaited progress count: a positive value is progress that no
+ * warp ever reports, so every wait runs to its limit -- how the timeout path is
+ * tested without faulting or hanging a GPU. */
+int pq_dense_sweep_ex(uint32_t* words, float* F, int ldf, const float* K, const int32_t* units, int nunits,
+                      const float* jperp, int N, int P, int R, int nsched, int mcsteps, float beta, uint64_t seed,
+                      int64_t sweep_base, int replica_base, int per_slice_order, int64_t poll_limit, int wait_skew,
+                      unsigned long long* accepts, int32_t* status, void* stream);
 /* words [R][N] -> the GEMM operand: BF16 +-1 rows c = r*P + k (Mpad rows, zero
  * padding), each row = [s over j < Npad, the same again] (2*Npad columns, so one
  * GEMM against [K_hi | K_lo] sums both halves of the split couplings). */
@@ -406,18 +421,6 @@ int pq_adam(float* p, const float* g, float* m, float* v, int n, float lr, float
 int pq_energy_packed(const void* words, int word_bits, int n, int P, int R,
                      const int64_t* row_ptr, const int32_t* col, const double* val,
                      double* out, void* stream);
-
-/* FP32 FMA throughput probe (diagnostic, used as the measured FP32 peak of
- * the sweep's roofline): blocks x threads threads run 8 x iters dependent-free
- * FMAs each (2 flop per FMA).  out: device float [blocks] (written only to keep
- * the work live). */
-int pq_fp32_fma_probe(float* out, int iters, int blocks, int threads, void* stream);
-
-/* Diagnostic for the packed sweep's exact fast path: atomically raises *out (a
- * non-negative double's bit pattern, device memory) to the largest
- * |2^fl(x log2 e) (hardware approximation) / expf_neg(x) - 1| over the FP32 x
- * with bit patterns first_bits .. first_bits+count-1 that lie in [-87, 0]. */
-int pq_guard_band_probe(uint32_t first_bits, int64_t count, unsigned long long* out, void* stream);
 
 /* int8 layout [R][n][P] -> packed words [R][word_stride] and back.  perm[i] is
  * the word slot of spin i (NULL = identity, then word_stride >= n); slots that no

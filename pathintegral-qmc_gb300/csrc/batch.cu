@@ -87,21 +87,25 @@ __global__ void __launch_bounds__(256, 2) batch_kernel(const pq_batch_task* __re
 constexpr int kNoAllocScratchInts = 64;
 static __device__ __align__(256) int g_noalloc_scratch[kNoAllocScratchInts];
 
-// Device address of the scratch, looked up once per device (host code cannot use
-// the symbol itself: on the host it names a stand-in, not device memory).
-constexpr int kNoAllocMaxDevices = 64;
-static int* g_noalloc_ptr[kNoAllocMaxDevices];
-
+// Device address of the scratch, looked up once per device context (host code
+// cannot use the symbol itself: on the host it names a stand-in, not device
+// memory).  The lookup is redone after the device's context changes (a reset).
 int noalloc_scratch(int** out) {
+    static std::mutex mu;
+    static unsigned long long ctx[kPqMaxDevices];
+    static int* addr[kPqMaxDevices];
     int dev = 0;
     PQ_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kNoAllocMaxDevices) return PQ_ERR_UNSUPPORTED;
-    if (!g_noalloc_ptr[dev]) {
+    if (dev < 0 || dev >= kPqMaxDevices) return PQ_ERR_UNSUPPORTED;
+    std::lock_guard<std::mutex> lock(mu);
+    const unsigned long long id = pq_context_id();
+    if (!id || ctx[dev] != id || !addr[dev]) {
         void* p = nullptr;
         PQ_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-        g_noalloc_ptr[dev] = static_cast<int*>(p);
+        addr[dev] = static_cast<int*>(p);
+        ctx[dev] = pq_context_id();
     }
-    *out = g_noalloc_ptr[dev];
+    *out = addr[dev];
     return PQ_OK;
 }
 
@@ -116,7 +120,8 @@ int pq_batch_anneal_noalloc(const pq_batch_task* tasks, int ntasks, const pq_bat
                             const float* field_pool, const int32_t* csize_pool, const float* jperp_pool,
                             void* words_pool, const pq_batch_run* run, int grid, int threads, int smem_bytes,
                             unsigned long long* accepts, int32_t* status, void* stream) {
-    if (ntasks < 0 || grid <= 0 || (int64_t)ntasks + grid > (int64_t)INT32_MAX) return PQ_ERR_TOO_LARGE;
+    if (ntasks < 0 || grid <= 0) return PQ_ERR_INVALID_ARG;
+    if ((int64_t)ntasks + grid > (int64_t)INT32_MAX) return PQ_ERR_TOO_LARGE;
     int* head = nullptr;
     const int st = noalloc_scratch(&head);  // first call on a device: symbol lookup
     if (st != PQ_OK) return st;
@@ -146,16 +151,16 @@ int pq_batch_anneal(const pq_batch_task* tasks, int ntasks, const pq_batch_item*
     if (!run || ntasks < 0 || grid <= 0 || threads <= 0 || threads > 256 || threads % 32 || smem_bytes < 0 ||
         smem_bytes > 220 * 1024)
         return PQ_ERR_INVALID_ARG;
+    // the task counter is 32-bit: every CTA adds one past the last task before it stops
+    if ((int64_t)ntasks + grid > (int64_t)INT32_MAX) return PQ_ERR_TOO_LARGE;
     if (ntasks == 0 || run->nsched == 0) return PQ_OK;
     if (!tasks || !items || !insts || !field_pool || !csize_pool || !jperp_pool || !words_pool || !queue_head)
         return PQ_ERR_INVALID_ARG;
     // instances are checked on the host (maxdeg <= 8: the batched kernel carries no wider variant)
     if (run->order_mode != 0 && run->order_mode != 1) return PQ_ERR_INVALID_ARG;
-    static bool attr = false;
-    if (!attr) {
-        PQ_CUDA_TRY(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
-        attr = true;
-    }
+    static PqSmemAttr attr;
+    const int rc = pq_set_smem_limit(attr, (const void*)batch_kernel, 220 * 1024);
+    if (rc != PQ_OK) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     PQ_CUDA_TRY(cudaMemsetAsync(queue_head, 0, sizeof(int), st));
     batch_kernel<<<grid, threads, smem_bytes, st>>>(tasks, ntasks, items, insts, nbr_pool, cpl_pool, field_pool,

@@ -1,7 +1,11 @@
 // Shared device helpers: status words, Philox4x32-10, the sweep's own exp.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <atomic>
+#include <mutex>
 
 #include "piqmc_gb300.h"
 
@@ -14,6 +18,60 @@
 static inline int pq_launch_status() {
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? PQ_OK : -(int)e;
+}
+
+// ----------------------------------------------------------------------------
+// Per-device state.  Kernel attributes, symbol addresses and occupancy belong to
+// one device context, so caches of them are keyed by the device ordinal and
+// checked against the identity of the context they were made in: a process that
+// drives a second GPU, or that resets a device (a new primary context), redoes
+// the set-up instead of using a stale value.
+// ----------------------------------------------------------------------------
+constexpr int kPqMaxDevices = 64;
+
+// Identity of the calling thread's current context, unique for the process's
+// lifetime (the driver's cuCtxGetId, looked up through the runtime so the
+// library needs no link-time driver dependency); 0 when there is none yet.
+inline unsigned long long pq_context_id() {
+    using GetCurrent = CUresult (*)(CUcontext*);
+    using GetId = CUresult (*)(CUcontext, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrent>(p);
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetId>(p);
+    });
+    if (!get_current || !get_id) return 0;
+    CUcontext c = nullptr;
+    if (get_current(&c) != CUDA_SUCCESS || !c) return 0;
+    unsigned long long id = 0;
+    if (get_id(c, &id) != CUDA_SUCCESS) return 0;
+    return id + 1;   // 0 stays "unknown"
+}
+
+// A kernel's dynamic shared-memory limit, set once per device context.
+struct PqSmemAttr {
+    std::atomic<unsigned long long> ctx[kPqMaxDevices] = {};
+};
+
+inline int pq_set_smem_limit(PqSmemAttr& cache, const void* kernel, int bytes) {
+    int dev = 0;
+    PQ_CUDA_TRY(cudaGetDevice(&dev));
+    const bool slot = dev >= 0 && dev < kPqMaxDevices;
+    const unsigned long long id = pq_context_id();
+    if (slot && id && cache.ctx[dev].load(std::memory_order_acquire) == id) return PQ_OK;
+    PQ_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    const unsigned long long now = pq_context_id();   // the call above made the context current
+    if (slot && now) cache.ctx[dev].store(now, std::memory_order_release);
+    return PQ_OK;
 }
 
 // First error wins; later ones are dropped.

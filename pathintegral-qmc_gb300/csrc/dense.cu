@@ -23,7 +23,7 @@
 //  * update of spin i in slice k (FP32, one rounding per op, in order):
 //    e = s_i f_i (f = h + sum_j K_ij s_j, the stored field), t = J-perp s_i s_{k-1}
 //    + J-perp s_i s_{k+1}, sum = e + t; flip when sum < 0, else when
-//    u < expf_neg(fl(sum * (-2 beta))), u = (r >> 9) 2^-23 with r = word t & 3 of
+//    u < expf_neg(fl(sum * (-2 beta))), u = ((r >> 9) + 1/2) 2^-23 with r = word t & 3 of
 //    Philox(ctr = {k, sweep, replica, 4 << 24 | t >> 2});
 //  * on a flip, f_j <- fma(2 s_i_new, K_ij, f_j) for every j (K_ii = 0).
 #include <cuda_bf16.h>
@@ -42,6 +42,8 @@ struct DenseArgs {
     uint32_t key0, key1;
     int64_t sweep_base;
     int replica_base;
+    long long poll_limit;   // polls of a neighbour's progress before a wait gives up
+    int wait_skew;          // added to every awaited progress count (0; > 0 only to test the timeout)
 };
 
 // One sweep of slice k of the replica whose fields sf and world-lines sw are in
@@ -131,19 +133,20 @@ __device__ __forceinline__ unsigned long long sweep_slice(int k, uint32_t sweep,
     return nacc;
 }
 
-constexpr long long kWaveWait = 1ll << 24;   // polls of a neighbour's progress before giving up
+constexpr long long kWaveWait = 1ll << 24;   // default polls of a neighbour's progress before giving up
 
 // Wait until *flag >= need for every lane (each lane reads the flag itself, then
 // fences, so the producer's shared-memory writes before its release are visible).
-__device__ __forceinline__ bool wait_progress(const volatile int* flag, int need) {
-    for (long long it = 0; it < kWaveWait; ++it) {
+// Gives up (false) after `limit` unsuccessful polls.
+__device__ __forceinline__ bool wait_progress(const volatile int* flag, int need, long long limit) {
+    for (long long it = 0;; ++it) {
         if (__all_sync(0xffffffffu, *flag >= need)) {
             __threadfence_block();
             return true;
         }
+        if (it >= limit) return false;
         __nanosleep(64);
     }
-    return false;
 }
 
 __global__ void __launch_bounds__(512, 2) dense_sweep_kernel(uint32_t* __restrict__ words, float* __restrict__ F,
@@ -184,12 +187,12 @@ __global__ void __launch_bounds__(512, 2) dense_sweep_kernel(uint32_t* __restric
             const float jp = jperp[g];
             for (int step = 0; step < a.mcsteps && ok; ++step, ++n) {
                 const uint32_t sweep = (uint32_t)(a.sweep_base + (int64_t)g * a.mcsteps + step);
-                if (!(ok = wait_progress(vprog + 32 + wl, n))) break;
+                if (!(ok = wait_progress(vprog + 32 + wl, n + a.wait_skew, a.poll_limit))) break;
                 nacc += sweep_slice(2 * w, sweep, jp, m2beta, m2blog2e, sf, sw, K, units, a, rep, lane);
                 __syncwarp();
                 __threadfence_block();
                 if (lane == 0) vprog[w] = n + 1;
-                if (!(ok = wait_progress(vprog + wr, n + 1))) break;
+                if (!(ok = wait_progress(vprog + wr, n + 1 + a.wait_skew, a.poll_limit))) break;
                 nacc += sweep_slice(2 * w + 1, sweep, jp, m2beta, m2blog2e, sf, sw, K, units, a, rep, lane);
                 __syncwarp();
                 __threadfence_block();
@@ -255,28 +258,36 @@ int pq_dense_unpack_bf16(const uint32_t* words, int N, int P, int R, int Npad, i
     return pq_launch_status();
 }
 
-int pq_dense_sweep(uint32_t* words, float* F, int ldf, const float* K, const int32_t* units, int nunits,
-                   const float* jperp, int N, int P, int R, int nsched, int mcsteps, float beta, uint64_t seed,
-                   int64_t sweep_base, int replica_base, int per_slice_order, unsigned long long* accepts,
-                   int32_t* status, void* stream) {
+int pq_dense_sweep_ex(uint32_t* words, float* F, int ldf, const float* K, const int32_t* units, int nunits,
+                      const float* jperp, int N, int P, int R, int nsched, int mcsteps, float beta, uint64_t seed,
+                      int64_t sweep_base, int replica_base, int per_slice_order, int64_t poll_limit, int wait_skew,
+                      unsigned long long* accepts, int32_t* status, void* stream) {
     if (!words || !F || !K || !units || !jperp || N <= 0 || P < 1 || P > 32 || R < 0 || nsched < 0 || mcsteps < 0 ||
-        nunits <= 0 || ldf < N)
+        nunits <= 0 || ldf < N || wait_skew < 0 || wait_skew > (1 << 24))
         return PQ_ERR_INVALID_ARG;
     if (R == 0 || nsched == 0) return PQ_OK;
     const size_t smem = (size_t)P * N * 4 + (size_t)N * 4;
     if (smem > 220 * 1024) return PQ_ERR_TOO_LARGE;
-    static bool attr = false;
-    if (!attr) {
-        PQ_CUDA_TRY(cudaFuncSetAttribute(dense_sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
-        attr = true;
-    }
+    static PqSmemAttr attr;
+    const int rc = pq_set_smem_limit(attr, (const void*)dense_sweep_kernel, 220 * 1024);
+    if (rc != PQ_OK) return rc;
     DenseArgs a;
     a.N = N; a.P = P; a.R = R; a.nunits = nunits; a.ldf = ldf; a.per_slice_order = per_slice_order ? 1 : 0; a.nsched = nsched; a.mcsteps = mcsteps; a.beta = beta;
     a.key0 = (uint32_t)seed; a.key1 = (uint32_t)(seed >> 32); a.sweep_base = sweep_base; a.replica_base = replica_base;
+    a.poll_limit = poll_limit < 0 ? kWaveWait : poll_limit;
+    a.wait_skew = wait_skew;
     const int maxq = P == 1 ? 1 : (P + 1) / 2;
     const int threads = 32 * maxq;
     dense_sweep_kernel<<<R, threads, smem, (cudaStream_t)stream>>>(words, F, K, units, jperp, a, accepts, status);
     return pq_launch_status();
+}
+
+int pq_dense_sweep(uint32_t* words, float* F, int ldf, const float* K, const int32_t* units, int nunits,
+                   const float* jperp, int N, int P, int R, int nsched, int mcsteps, float beta, uint64_t seed,
+                   int64_t sweep_base, int replica_base, int per_slice_order, unsigned long long* accepts,
+                   int32_t* status, void* stream) {
+    return pq_dense_sweep_ex(words, F, ldf, K, units, nunits, jperp, N, P, R, nsched, mcsteps, beta, seed, sweep_base,
+                             replica_base, per_slice_order, -1, 0, accepts, status, stream);
 }
 
 }  // extern "C"

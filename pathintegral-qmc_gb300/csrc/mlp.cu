@@ -607,11 +607,18 @@ __global__ void uniform_move_kernel(W* __restrict__ words, const int32_t* __rest
 // and TMEM (4 x 128 columns per SM) -- four CTAs per SM.
 template <typename W, int MAXD>
 int move_grid(int64_t ntiles) {
-    static int occ = 0, nsm = 0;
-    if (!occ) {
+    // per device: (context identity, SMs, resident CTAs per SM)
+    static std::mutex mu;
+    static unsigned long long ctx[kPqMaxDevices];
+    static int nsm_dev[kPqMaxDevices], occ_dev[kPqMaxDevices];
+    int dev = 0;
+    PQ_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kPqMaxDevices) return -(int)cudaErrorInvalidDevice;   // callers read <= 0 as an error
+    std::lock_guard<std::mutex> lock(mu);
+    const unsigned long long id = pq_context_id();
+    if (!id || ctx[dev] != id) {
         auto kernel = learned_move_kernel<W, MAXD>;
-        int dev = 0, smem_sm = 0, regs_sm = 0, reserved = 0;
-        PQ_CUDA_TRY(cudaGetDevice(&dev));
+        int nsm = 0, smem_sm = 0, regs_sm = 0, reserved = 0;
         PQ_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
         PQ_CUDA_TRY(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
         PQ_CUDA_TRY(cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev));
@@ -625,11 +632,13 @@ int move_grid(int64_t ntiles) {
         const int warp_regs = (fa.numRegs * 32 + 255) / 256 * 256;    // allocated per warp in units of 256
         const int by_regs = regs_sm / (warp_regs * 4);
         const int by_tmem = 512 / (2 * kLd);
-        occ = by_smem < by_regs ? by_smem : by_regs;
+        int occ = by_smem < by_regs ? by_smem : by_regs;
         occ = occ < by_tmem ? occ : by_tmem;
-        occ = occ < 1 ? 1 : occ;
+        nsm_dev[dev] = nsm;
+        occ_dev[dev] = occ < 1 ? 1 : occ;
+        ctx[dev] = pq_context_id();
     }
-    const int64_t g = (int64_t)nsm * occ;
+    const int64_t g = (int64_t)nsm_dev[dev] * occ_dev[dev];
     return (int)(ntiles < g ? ntiles : g);
 }
 

@@ -211,11 +211,9 @@ int launch_gemm(const void* A, int lda, const void* B, int ldb, float* D, int ld
     CUtensorMap td;
     rc = encode_map(&td, D, M, N, ldd, BM, 4);
     if (rc != PQ_OK) return rc;
-    static bool attr = false;
-    if (!attr) {
-        PQ_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::kSmem));
-        attr = true;
-    }
+    static PqSmemAttr attr;
+    rc = pq_set_smem_limit(attr, (const void*)tc_gemm_kernel<BN>, C::kSmem);
+    if (rc != PQ_OK) return rc;
     dim3 grid(M / BM, N / BN);
     tc_gemm_kernel<BN><<<grid, 128, C::kSmem, stream>>>(ta, tb, td, K, alpha, bias, status);
     return pq_launch_status();

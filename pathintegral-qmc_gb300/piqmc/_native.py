@@ -89,8 +89,6 @@ SIGNATURES = {
     "pq_color_graph": (_I32, [_I32, _I32, _V, _V, _V]),
     "pq_qa_fast": (_I32, [_V, _V, _V, _V, _V, ctypes.POINTER(FastParams), _V, _V, _V]),
     "pq_qa_fast_ex": (_I32, [_V, _V, _V, _V, _V, _V, ctypes.POINTER(FastParams), _V, _V, _V]),
-    "pq_guard_band_probe": (_I32, [_U32, _I64, _V, _V]),
-    "pq_fp32_fma_probe": (_I32, [_V, _I32, _I32, _I32, _V]),
     "pq_batch_anneal": (_I32, [_V, _I32, _V, _V, _V, _V, _V, _V, _V, _V, _V, _V, _I32, _I32, _I32, _V, _V, _V]),
     "pq_batch_anneal_noalloc": (_I32, [_V, _I32, _V, _V, _V, _V, _V, _V, _V, _V, _V, _I32, _I32, _I32, _V, _V,
                                        _V]),
@@ -99,6 +97,8 @@ SIGNATURES = {
     "pq_tc_gemm_bf16": (_I32, [_V, _I32, _V, _I32, _V, _I32, _I32, _I32, _I32, _F32, _V, _V, _V]),
     "pq_dense_sweep": (_I32, [_V, _V, _I32, _V, _V, _I32, _V, _I32, _I32, _I32, _I32, _I32, _F32, _U64, _I64, _I32,
                               _I32, _V, _V, _V]),
+    "pq_dense_sweep_ex": (_I32, [_V, _V, _I32, _V, _V, _I32, _V, _I32, _I32, _I32, _I32, _I32, _F32, _U64, _I64,
+                                 _I32, _I32, _I64, _I32, _V, _V, _V]),
     "pq_dense_unpack_bf16": (_I32, [_V, _I32, _I32, _I32, _I32, _I32, _V, _V]),
     "pq_mlp_features": (_I32, [_V, _I32, _I32, _I32, _I32, _I32, _V, _V, _V, _I32, _I32, _I32, _F32, _F32, _V, _V,
                                _I64, _V]),

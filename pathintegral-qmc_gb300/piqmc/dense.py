@@ -109,19 +109,21 @@ class DenseProblem:
         return out
 
     def sweep(self, words, F, P, jperp, beta, seed, mcsteps=1, sweep_base=0, replica_base=0, accepts=None,
-              per_slice_order=False, status=None):
+              per_slice_order=False, status=None, poll_limit=-1, wait_skew=0):
         """Dense sweeps of every replica through len(jperp) field steps starting from fields F (updated in place).
 
         The spin order of a sweep is shared by every slice (as in the reference) unless
         ``per_slice_order`` -- which anneals faster but with different dynamics.
+        ``poll_limit`` bounds each wavefront wait (< 0: the kernel's default);
+        ``wait_skew`` > 0 makes every wait run to that bound (to test the timeout path).
         """
         R = words.shape[0]
-        _native.check(_native.lib().pq_dense_sweep(
+        _native.check(_native.lib().pq_dense_sweep_ex(
             _device.ptr(words), _device.ptr(F), F.stride(0), _device.ptr(self.K), _device.ptr(self.units),
             self.units.numel(), _device.ptr(jperp), self.N, int(P), R, int(jperp.numel()), int(mcsteps),
             float(np.float32(beta)), int(seed) & 0xFFFFFFFFFFFFFFFF, int(sweep_base), int(replica_base),
-            int(bool(per_slice_order)), _device.ptr(accepts), (status or self._status).ptr, _device.stream_handle()),
-            "pq_dense_sweep")
+            int(bool(per_slice_order)), int(poll_limit), int(wait_skew), _device.ptr(accepts),
+            (status or self._status).ptr, _device.stream_handle()), "pq_dense_sweep")
 
     def anneal(self, words, sched, P, temp, seed=0, mcsteps=1, recompute_every=50, accepts=None,
                per_slice_order=False, check=True):

@@ -76,3 +76,46 @@ def test_dense_anneal_reaches_low_energy_and_energies_match():
             ref = oracle.classical_energy(fin[r, :, k].astype(np.float64), J)
             assert abs(E[r, k] - ref) <= 1e-10 * max(1.0, abs(ref))
     assert E.mean() < E0.mean() - 0.3 * N ** 0.5
+
+
+def test_wavefront_wait_runs_to_its_limit_and_the_kernel_returns():
+    """A wait for progress that no warp reports gives up after its poll limit: the kernel
+    records PQ_ERR_TIMEOUT, returns, and the context stays usable (the same sweep then runs
+    normally and matches the oracle).  No GPU is hung: every wait is bounded."""
+    from piqmc import _device, _native, dense
+    N, P, R = 64, 8, 2
+    J, g = _instance(N, 11)
+    prob = dense.DenseProblem(J)
+    spins = np.where(g.random((R, N, P)) < 0.5, -1, 1).astype(np.int8)
+    words0 = prob.pack(torch.from_numpy(spins))
+    F0, _ = prob.fields(words0, P)
+    sched = np.linspace(3.0, 1e-8, 4)
+    jp = oracle.jperp(sched, P, 0.05)
+    beta = np.float32(1) / np.float32(0.05)
+    status = _device.Status()
+    words, F = words0.clone(), F0.clone()
+    prob.sweep(words, F, P, torch.from_numpy(jp).cuda(), beta, 5, status=status, poll_limit=1000, wait_skew=1 << 20)
+    torch.cuda.synchronize()
+    assert int(status.t.item()) == _native.PQ_ERR_TIMEOUT
+    # the same call with the waits in use completes and is exact
+    words, F = words0.clone(), F0.clone()
+    status.reset()
+    prob.sweep(words, F, P, torch.from_numpy(jp).cuda(), beta, 5, status=status, poll_limit=1000)
+    torch.cuda.synchronize()
+    assert int(status.t.item()) == 0
+    got = words.cpu().numpy().view(np.uint32)
+    for r in range(R):
+        w = words0[r].cpu().numpy().view(np.uint32).copy()
+        f = F0[r * P:(r + 1) * P, :N].cpu().numpy().copy()
+        oracle.dense_sweep(f, prob.K.cpu().numpy(), prob.units.cpu().numpy(), w, P, jp, 1, beta, 5, replica=r)
+        np.testing.assert_array_equal(got[r], w)
+
+
+def test_wait_skew_is_bounded():
+    from piqmc import _native, dense
+    J, g = _instance(16, 12)
+    prob = dense.DenseProblem(J)
+    words = prob.pack(torch.from_numpy(np.ones((1, 16, 4), np.int8)))
+    F, _ = prob.fields(words, 4)
+    with pytest.raises(_native.PiqmcError):
+        prob.sweep(words, F, 4, torch.zeros(1, device="cuda"), 1.0, 0, wait_skew=-1)

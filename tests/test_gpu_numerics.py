@@ -9,7 +9,8 @@ pytestmark = pytest.mark.gpu
 def test_guard_band_covers_hardware_exp2():
     """Every FP32 argument in [-87, 0]: the hardware 2^x stays far inside the 1e-4 guard band."""
     from piqmc import _device, _native
-    L = _native.lib()
+    from native import probes
+    L = probes.lib()
     out = torch.zeros(1, dtype=torch.int64, device="cuda")
     lo = 0x80000000  # -0.0; more negative floats have larger patterns
     hi = int(np.array([-87.0], np.float32).view(np.uint32)[0])
@@ -17,7 +18,7 @@ def test_guard_band_covers_hardware_exp2():
     b = lo
     while b <= hi:
         cnt = min(step, hi - b + 1)
-        _native.check(L.pq_guard_band_probe(b, cnt, _device.ptr(out), _device.stream_handle()), "probe")
+        _native.check(L.pqt_guard_band_probe(b, cnt, _device.ptr(out), _device.stream_handle()), "probe")
         b += cnt
     torch.cuda.synchronize()
     worst = float(np.array([out.item()], dtype=np.int64).view(np.float64)[0])

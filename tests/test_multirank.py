@@ -1,7 +1,7 @@
 """The N-rank path on CPU: two gloo ranks shard replicas with no data-path collective.
 
 Each rank anneals its replicas of a small lattice through the packed sweep's CPU
-oracle with the job's key and its own global replica ids (``bench.rank_plan``);
+oracle with the job's key and its own global replica ids (``piqmc.shard.rank_plan``);
 the gathered results must equal one process annealing all replicas, and the
 timing reduction must return the slowest rank's time.
 """
@@ -22,14 +22,14 @@ def _free_port():
         return s.getsockname()[1]
 
 
+SEED = 7
+
+
 def _setup():
-    import sys
-    sys.path.insert(0, ROOT)
-    import bench
-    from piqmc import fast, tools
+    from piqmc import fast, shard, tools
     J = lattice(6, True, np.random.default_rng(3), dist=lambda r: r.normal())
     nbs = tools.GenerateNeighbors(36, J, 4)
-    return bench, fast.Problem(nbs, on_device=False)
+    return shard, fast.Problem(nbs, on_device=False)
 
 
 def _anneal(prob, spins, replica_base, P, seed):
@@ -52,13 +52,13 @@ def _rank(rank, world, port, R, P, q):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     dist.init_process_group("gloo", rank=rank, world_size=world)
     try:
-        bench, prob = _setup()
-        plan = bench.rank_plan(rank, world, R)
-        spins = bench.initial_spins(plan["replica_base"], R, prob.n)
-        w = torch.from_numpy(_anneal(prob, spins, plan["replica_base"], P, plan["seed"]).view(np.int64))
+        shard, prob = _setup()
+        plan = shard.rank_plan(rank, world, R, SEED)
+        spins = shard.initial_spins(plan.replica_base, R, prob.n)
+        w = torch.from_numpy(_anneal(prob, spins, plan.replica_base, P, plan.seed).view(np.int64))
         parts = [torch.empty_like(w) for _ in range(world)]
         dist.all_gather(parts, w)                # gathered here only to check; the bench never gathers
-        slow = bench.max_over_ranks(0.5 + rank, dist, "cpu")
+        slow = shard.max_over_ranks(0.5 + rank, dist, "cpu")
         if rank == 0:
             q.put((np.concatenate([p.numpy() for p in parts]).view(np.uint64), slow))
     finally:
@@ -66,17 +66,32 @@ def _rank(rank, world, port, R, P, q):
 
 
 def test_rank_plan_is_a_partition():
+    from piqmc import shard
+    plans = [shard.rank_plan(r, 4, 8, SEED) for r in range(4)]
+    ids = np.concatenate([np.arange(p.replica_base, p.replica_base + p.replicas) for p in plans])
+    np.testing.assert_array_equal(ids, np.arange(32))
+    assert len({p.seed for p in plans}) == 1 and plans[0].total_replicas == 32
+    np.testing.assert_array_equal(shard.initial_spins(8, 8, 36), shard.initial_spins(0, 16, 36)[8:])
+    assert shard.whole_job_rate(100.0, 3, 4, 2.0) == 600.0
+    with pytest.raises(ValueError):
+        shard.rank_plan(4, 4, 8)
+
+
+def test_plan_from_env(monkeypatch):
+    from piqmc import shard
+    monkeypatch.setenv("RANK", "3")
+    monkeypatch.setenv("WORLD_SIZE", "4")
+    p = shard.plan_from_env(16, seed=5)
+    assert (p.rank, p.world, p.replica_base, p.replicas, p.seed) == (3, 4, 48, 16, 5)
+
+
+def test_bench_uses_the_package_plan():
     import sys
     sys.path.insert(0, ROOT)
     import bench
-    plans = [bench.rank_plan(r, 4, 8) for r in range(4)]
-    ids = np.concatenate([np.arange(p["replica_base"], p["replica_base"] + p["replicas"]) for p in plans])
-    np.testing.assert_array_equal(ids, np.arange(32))
-    assert len({p["seed"] for p in plans}) == 1
-    np.testing.assert_array_equal(bench.initial_spins(8, 8, 36), bench.initial_spins(0, 16, 36)[8:])
-    assert bench.whole_job_rate(100.0, 3, 4, 2.0) == 600.0
-    with pytest.raises(ValueError):
-        bench.rank_plan(4, 4, 8)
+    from piqmc import shard
+    assert bench.rank_plan(1, 2, 8) == shard.rank_plan(1, 2, 8, bench.BENCH_SEED)
+    assert bench.initial_spins is shard.initial_spins
 
 
 def test_two_gloo_ranks_equal_one_process():
@@ -91,7 +106,7 @@ def test_two_gloo_ranks_equal_one_process():
         p.join(120)
         assert p.exitcode == 0
     gathered, slow = q.get()
-    bench, prob = _setup()
-    single = _anneal(prob, bench.initial_spins(0, world * R, prob.n), 0, P, bench.BENCH_SEED)
+    shard, prob = _setup()
+    single = _anneal(prob, shard.initial_spins(0, world * R, prob.n), 0, P, SEED)
     np.testing.assert_array_equal(gathered, single)
     assert slow == 1.5

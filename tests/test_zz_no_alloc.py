@@ -35,11 +35,12 @@ def _batch():
     return B
 
 
-def _call(B, words, noalloc):
+def _call(B, words, noalloc, status=None):
     from piqmc import _device, _native
     lib = _native.lib()
     run = B._runs(6, 0.05, 1, 0, 1, None)[0]
-    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    if status is None:
+        status = torch.zeros(1, dtype=torch.int32, device="cuda")
     args_head = [_device.ptr(B.d_tasks), len(B.tasks), _device.ptr(B.d_items), _device.ptr(B.d_inst),
                  _device.ptr(B.d_nbr), _device.ptr(B.d_cpl), _device.ptr(B.d_field), _device.ptr(B.d_csize),
                  _device.ptr(B.d_jperp), _device.ptr(words)]
@@ -64,10 +65,35 @@ def test_noalloc_matches_regular_entry_point_twice():
     assert not torch.equal(regular, B.words)   # the anneal did change the state
 
 
-def test_noalloc_rejects_counter_overflow():
+def test_noalloc_call_allocates_nothing():
+    """After a first call (which loads the kernel and looks up the scratch's address),
+    a call changes neither torch's allocated bytes nor the device's free memory."""
+    B = _batch()
+    words = B.words.clone()
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    _call(B, words, noalloc=True, status=status)
+    torch.cuda.synchronize()
+    allocated, (free, _) = torch.cuda.memory_allocated(), torch.cuda.mem_get_info()
+    _call(B, words, noalloc=True, status=status)
+    torch.cuda.synchronize()
+    assert torch.cuda.memory_allocated() == allocated
+    assert torch.cuda.mem_get_info()[0] == free
+
+
+def test_noalloc_rejects_bad_arguments_like_the_regular_entry_point():
     from piqmc import _native
+    lib = _native.lib()
     B = _batch()
     run = B._runs(6, 0.05, 1, 0, 1, None)[0]
-    rc = _native.lib().pq_batch_anneal_noalloc(None, 2 ** 31 - 10, None, None, None, None, None, None, None, None,
-                                              ctypes.byref(run), 64, 256, 0, None, None, None)
-    assert rc == _native.PQ_ERR_TOO_LARGE
+    nulls = [None] * 8   # items .. words_pool
+    # the 32-bit task counter: ntasks + grid must fit
+    assert lib.pq_batch_anneal_noalloc(None, 2 ** 31 - 10, *nulls, ctypes.byref(run), 64, 256, 0, None, None,
+                                       None) == _native.PQ_ERR_TOO_LARGE
+    assert lib.pq_batch_anneal(None, 2 ** 31 - 10, *nulls, None, ctypes.byref(run), 64, 256, 0, None, None,
+                               None) == _native.PQ_ERR_TOO_LARGE
+    # a negative task count or an empty grid is an argument error on both entry points
+    for ntasks, grid in [(-1, 64), (4, 0)]:
+        assert lib.pq_batch_anneal_noalloc(None, ntasks, *nulls, ctypes.byref(run), grid, 256, 0, None, None,
+                                           None) == _native.PQ_ERR_INVALID_ARG
+        assert lib.pq_batch_anneal(None, ntasks, *nulls, None, ctypes.byref(run), grid, 256, 0, None, None,
+                                   None) == _native.PQ_ERR_INVALID_ARG
