@@ -343,12 +343,13 @@ def gpu_arm(args):
         e2e_s = max_over_ranks(e2e_s, dist, "cuda")
     e2e_value = whole_job_rate(updates, len(e2e_ms), world, e2e_s)
 
-    batched = densew = learnedw = reforderw = None
+    batched = densew = learnedw = reforderw = dropinw = None
     if not args.no_batched and rank == 0:
         batched = batched_workload(args, torch)
         densew = dense_workload(args, torch)
         learnedw = learned_vs_plain(args, torch, prob, R=args.learned_replicas)
         reforderw = reforder_workload(args, torch)
+        dropinw = dropin_workload(args, torch)
 
     peak = measured_fp32_peak(torch)
     achieved_tflops = value / world * FLOP_PER_UPDATE / 1e12
@@ -397,6 +398,14 @@ def gpu_arm(args):
     }
     if cpu_base is not None:
         line["cpu_baseline"] = cpu_base
+    extras = compact_extras(batched, densew, learnedw, reforderw, dropinw)
+    if extras:
+        # the compact figures go right after the config, the detailed objects at the end of the line
+        keys = list(line)
+        at = keys.index("config") + 1
+        line = {k: line[k] for k in keys[:at]} | {"extras": extras} | {k: line[k] for k in keys[at:]}
+    if dropinw is not None:
+        line["dropin"] = dropinw
     if batched is not None:
         line["batched_uneven"] = batched
     if densew is not None:
@@ -409,6 +418,28 @@ def gpu_arm(args):
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def compact_extras(batched, densew, learnedw, reforderw, dropinw):
+    """Headline figure of every extra workload, in a few keys (the detailed objects follow at the end)."""
+    ex = {}
+    if batched is not None:
+        ex["batched_uneven_updates_per_s"] = batched["value"]
+    if densew is not None:
+        ex["dense_N512_P32_updates_per_s"] = densew["value"]
+        if "cpu_baseline" in densew:
+            ex["dense_reference_all_cores_updates_per_s"] = densew["cpu_baseline"]["value"]
+    if learnedw is not None:
+        ex["learned_time_to_plain_residual_over_plain"] = learnedw.get("learned_time_to_plain_residual_over_plain")
+        ex["uniform_pair_time_to_plain_residual_over_plain"] = learnedw.get(
+            "uniform_pair_time_to_plain_residual_over_plain")
+    if reforderw is not None:
+        ex["reference_order_1_replica_updates_per_s"] = reforderw["replicas_1"]["value"]
+        ex["reference_order_8_replicas_updates_per_s"] = reforderw["replicas_8"]["value"]
+    if dropinw is not None:
+        ex["dropin_speedup_vs_one_core"] = {r["call"].split(" ")[0]: r.get("speedup_vs_one_core")
+                                            for r in dropinw["calls"]}
+    return ex
 
 
 def batched_workload(args, torch):
@@ -517,14 +548,19 @@ def dense_workload(args, torch):
 
 
 def learned_vs_plain(args, torch, prob_big, R=1024, every=20):
-    """80x80 P=20 anneal with a world-line move pass every `every` steps: uniform (plain) vs learned.
+    """Residual energy at equal GPU time on the 80x80 P=20 workload: plain vs pair forms.
 
-    The network is first trained on moves recorded from plain 32x32 P=20 runs (J ~ U[-2, 2]).  Both forms
-    run the same local sweeps; the learned one replaces the uniform pass (every spin tried) with the
-    network's MH-corrected proposals.  Residual energy per spin = best-slice energy minus the best
-    energy found by either form, divided by n."""
+    Forms (the same local sweeps; a move pass every `every` field steps):
+      plain         uniform single world-line moves (every spin tried) -- the method the others are judged by;
+      uniform_pair  plain + a pair world-line pass that tries every bond (piqmc.pairs.pair_pass);
+      learned_pair  plain + pair moves proposed by the MLP (8 -> 64 -> 64 -> 1, BF16 on the tensor cores)
+                    with the exact Metropolis-Hastings correction (piqmc.pairs.learned_pair_pass), trained
+                    on pair moves recorded from uniform-pair runs of a 32x32 P=20 instance (J ~ U[-2, 2]).
+    Residual energy per spin = best-slice energy minus the best energy any run found, over n.  The target
+    is the plain form's median at the full 2000-step schedule; a form's time to it is the GPU time of its
+    shortest schedule whose median reaches it."""
     import scipy.sparse as sps
-    from piqmc import fast, learned, tools
+    from piqmc import fast, learned, pairs, tools
     P = P_SLICES
     g = np.random.default_rng(11)
     L = 32
@@ -545,9 +581,10 @@ def learned_vs_plain(args, torch, prob_big, R=1024, every=20):
     for g0 in range(0, len(sched_s), 20):
         fast.anneal(small, ws, sched_s[g0:g0 + 20], P, TEMP, seed=21, sweep_base=g0,
                     jperp=torch.from_numpy(jp_s[g0:g0 + 20]).cuda())
-        X, y = learned.record_moves(small, ws, P, 1.0 / TEMP, float(jp_s[g0 + 19]))
+        X, y = pairs.record_pair_moves(small, ws, P, 1.0 / TEMP, float(jp_s[g0 + 19]))
         Xs.append(X)
         ys.append(y)
+        pairs.pair_pass(small, ws, P, 1.0 / TEMP, seed=22, move=g0)
     X, y = torch.cat(Xs), torch.cat(ys)
     mlp = learned.ProposalMLP(seed=0)
     hist = mlp.train(X, y, epochs=2, batch=16384, lr=3e-3)
@@ -556,6 +593,7 @@ def learned_vs_plain(args, torch, prob_big, R=1024, every=20):
     n = prob_big.n
     spins = np.repeat(np.where(np.random.default_rng(12).random((R, n)) < 0.5, -1, 1).astype(np.int8)[:, :, None], P,
                       axis=2)
+    pairs.bond_classes(prob_big)
 
     def run(kind, steps):
         sched = schedule(steps)
@@ -563,6 +601,8 @@ def learned_vs_plain(args, torch, prob_big, R=1024, every=20):
         jp = torch.from_numpy(jp_host).cuda()
         w = prob_big.pack(torch.from_numpy(spins))
         cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
+        pcnt = torch.zeros(2, dtype=torch.int64, device="cuda")
+        status = torch.zeros(1, dtype=torch.int32, device="cuda")
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         marks = []
@@ -572,35 +612,52 @@ def learned_vs_plain(args, torch, prob_big, R=1024, every=20):
             fast.anneal(prob_big, w, sched[g0:g1], P, TEMP, seed=31, sweep_base=g0, jperp=jp[g0:g1], check=False)
             pa, pb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             pa.record()
-            learned.learned_pass(prob_big, w, P, mlp, 1.0 / TEMP, float(jp_host[g1 - 1]), seed=32, move=g0,
-                                 counters=cnt, uniform=(kind == "uniform"), check=False)
+            learned.learned_pass(prob_big, w, P, None, 1.0 / TEMP, float(jp_host[g1 - 1]), seed=32, move=g0,
+                                 counters=cnt, uniform=True, check=False)
+            if kind == "uniform_pair":
+                pairs.pair_pass(prob_big, w, P, 1.0 / TEMP, seed=33, move=g0, counters=pcnt, status=status,
+                                check=False)
+            elif kind == "learned_pair":
+                pairs.learned_pair_pass(prob_big, w, P, mlp, 1.0 / TEMP, float(jp_host[g1 - 1]), seed=33, move=g0,
+                                        counters=pcnt, status=status, check=False)
             pb.record()
             marks.append((pa, pb))
         e1.record()
         torch.cuda.synchronize()
-        learned.check_status()
+        if int(status.item()):
+            raise RuntimeError("pair pass status %d" % int(status.item()))
         E = prob_big.energies(w, P).cpu().numpy().min(axis=1)
-        c = cnt.cpu().numpy()
-        return {"gpu_s": e0.elapsed_time(e1) * 1e-3, "best": E, "proposed": int(c[0]), "accepted": int(c[1]),
+        c, pc = cnt.cpu().numpy(), pcnt.cpu().numpy()
+        return {"gpu_s": e0.elapsed_time(e1) * 1e-3, "best": E, "wl_tried": int(c[0]), "wl_accepted": int(c[1]),
+                "pair_tried": int(pc[0]), "pair_accepted": int(pc[1]),
                 "pass_ms": sum(a.elapsed_time(b) for a, b in marks) / len(marks)}
 
-    lengths = (2000, 1400, 1000, 700)
-    res = {(kind, st): run(kind, st) for kind in ("uniform", "learned") for st in lengths}
+    plan = {"plain": (2000, 1400, 1000, 700), "uniform_pair": (400, 200, 100, 50), "learned_pair": (400, 200, 100, 50)}
+    res = {(kind, st): run(kind, st) for kind, lens in plan.items() for st in lens}
     e_ref = min(r["best"].min() for r in res.values())
-    plain = res[("uniform", 2000)]
+    plain = res[("plain", 2000)]
     target = float(np.median(plain["best"] - e_ref) / n)
-    out = {"workload": "80x80 P=20, %d replicas, world-line pass every %d steps, schedules of %s steps; MLP 8-64-64-1 "
-                       "trained on moves recorded from plain 32x32 P=20 runs" % (R, every, "/".join(map(str, lengths))),
-           "train_s": train_s, "train_loss_first_last": [hist[0], hist[-1]],
+    out = {"workload": "80x80 P=20, %d replicas, a move pass every %d steps; plain (single world-line moves) at %s "
+                       "steps, uniform and learned pair world-line moves at %s steps; MLP 8-64-64-1 trained on pair "
+                       "moves recorded from uniform-pair 32x32 P=20 runs"
+                       % (R, every, "/".join(map(str, plan["plain"])), "/".join(map(str, plan["learned_pair"]))),
+           "train_s": train_s, "train_rows": int(X.shape[0]), "train_loss_first_last": [hist[0], hist[-1]],
            "plain_median_residual_energy_per_spin": target, "runs": []}
     for (kind, st), r in res.items():
         out["runs"].append({"form": kind, "steps": st, "gpu_s": r["gpu_s"],
                             "median_residual_energy_per_spin": float(np.median(r["best"] - e_ref) / n),
-                            "proposed": r["proposed"], "accepted": r["accepted"], "ms_per_pass": r["pass_ms"]})
-    hits = [r for r in out["runs"] if r["form"] == "learned" and r["median_residual_energy_per_spin"] <= target]
-    best = min(hits, key=lambda r: r["gpu_s"]) if hits else None
-    out["learned_time_to_plain_residual_over_plain"] = best["gpu_s"] / plain["gpu_s"] if best else None
-    out["learned_time_over_uniform_same_steps"] = res[("learned", 2000)]["gpu_s"] / plain["gpu_s"]
+                            "worldline_tried": r["wl_tried"], "worldline_accepted": r["wl_accepted"],
+                            "pair_tried": r["pair_tried"], "pair_accepted": r["pair_accepted"],
+                            "ms_per_move_pass": r["pass_ms"]})
+
+    def time_to_target(kind):
+        hits = [r for r in out["runs"] if r["form"] == kind and r["median_residual_energy_per_spin"] <= target]
+        return min(r["gpu_s"] for r in hits) if hits else None
+
+    tl, tu = time_to_target("learned_pair"), time_to_target("uniform_pair")
+    out["learned_time_to_plain_residual_over_plain"] = tl / plain["gpu_s"] if tl else None
+    out["uniform_pair_time_to_plain_residual_over_plain"] = tu / plain["gpu_s"] if tu else None
+    out["learned_over_uniform_pair_time_to_target"] = tl / tu if tl and tu else None
     return out
 
 
@@ -817,6 +874,77 @@ def gemm_workload(args, torch):
     return out
 
 
+def dropin_workload(args, torch):
+    """The default drop-in calls end to end, as an existing script makes them: reference order, one replica per
+    call, host buffers in and out, the permutations drawn from the caller's rng and the uniforms from this
+    process's libc rand() inside the timed call.  Each beside the compiled reference's own call on one host
+    core (oracle/_ref), same inputs; updates/s = spins x slices x field steps x mcsteps / wall time."""
+    from piqmc import qmc as d_qmc, sa as d_sa, tools
+    import scipy.sparse as sps
+    ref = None
+    if ref_available():
+        sys.path.insert(0, os.path.join(ROOT, "oracle", "_ref"))
+        from piqmc_ref import qmc as r_qmc, sa as r_sa
+        ref = (r_qmc, r_sa)
+    g = np.random.default_rng(31)
+
+    def timed(fn, *a):
+        t0 = time.perf_counter()
+        fn(*a)
+        return time.perf_counter() - t0
+
+    out = {"note": "wall time of one synchronous call (host streams, copies and the kernel); reference: the "
+                   "compiled reference's same call on one host core"}
+    # QuantumAnneal: the headline 80x80 P=20 instance, 20 field values of its schedule
+    n, P = L_SIDE * L_SIDE, P_SLICES
+    rows, cols, vals = instance_arrays()
+    J = sps.dok_matrix((n, n))
+    for a_, b_, v in zip(rows, cols, vals):
+        J[int(a_), int(b_)] = v
+    nbs = tools.GenerateNeighbors(n, J, 4)
+    conf0 = np.tile(np.where(g.random(n) < 0.5, -1.0, 1.0), (P, 1)).T
+    sched = schedule()[::100]
+    cases = [("QuantumAnneal 80x80 P=20, %d field steps" % len(sched), n * P * len(sched),
+              lambda m: (lambda: m.QuantumAnneal(sched, 1, P, TEMP, n, conf0.copy(order="F"), nbs,
+                                                 np.random.RandomState(1))))]
+    # QuantumAnneal_dense: N=512, P=32, FP64-valued couplings (a user's np.random matrix), 4 field steps
+    N, Pd = 512, 32
+    Jd = np.triu(g.normal(0.0, 1.0 / np.sqrt(N), (N, N)), 1) + np.diag(g.normal(0.0, np.sqrt(0.1), N))
+    confd = np.tile(np.where(g.random(N) < 0.5, -1.0, 1.0), (Pd, 1)).T
+    schedd = schedule(1000)[::250]
+    cases.append(("QuantumAnneal_dense N=512 P=32 FP64-valued J, %d field steps" % len(schedd), N * Pd * len(schedd),
+                  lambda m: (lambda: m.QuantumAnneal_dense(schedd, 1, Pd, TEMP, N, confd.copy(order="F"), Jd,
+                                                           np.random.RandomState(2)))))
+    # sa.Anneal: the 80x80 instance, classical, 50 temperatures
+    temps = np.linspace(3.0, 0.05, 50)
+    sv0 = np.where(g.random(n) < 0.5, -1.0, 1.0)
+    cases.append(("sa.Anneal 80x80, %d temperatures" % len(temps), n * len(temps),
+                  lambda m: (lambda: m.Anneal(temps, 1, sv0.copy(), nbs, np.random.RandomState(3)))))
+    # sa.Anneal_bipartite: 256 + 256 spins, FP64-valued couplings and biases, 20 temperatures
+    nl = nr = 256
+    Jb = g.normal(0.0, 1.0 / np.sqrt(nl), (nl, nr))
+    lb, rb = g.normal(0.0, 0.3, nl), g.normal(0.0, 0.3, nr)
+    lv0, rv0 = np.where(g.random(nl) < 0.5, -1.0, 1.0), np.where(g.random(nr) < 0.5, -1.0, 1.0)
+    tb = np.linspace(3.0, 0.05, 20)
+    cases.append(("sa.Anneal_bipartite 256+256 FP64-valued J, %d temperatures" % len(tb), (nl + nr) * len(tb),
+                  lambda m: (lambda: m.Anneal_bipartite(tb, 1, lv0.copy(), rv0.copy(), Jb, lb, rb,
+                                                        np.random.RandomState(4)))))
+    rows_out = []
+    for name, updates, make in cases:
+        mod_ours = d_sa if name.startswith("sa.") else d_qmc
+        call = make(mod_ours)
+        call()                                     # warm-up: kernel load, first-call set-up
+        ours = min(timed(call) for _ in range(2))
+        row = {"call": name, "updates": updates, "ours_s": ours, "ours_updates_per_s": updates / ours}
+        if ref is not None:
+            rcall = make(ref[1] if name.startswith("sa.") else ref[0])
+            rs = timed(rcall)
+            row.update(reference_s=rs, reference_updates_per_s=updates / rs, speedup_vs_one_core=rs / ours)
+        rows_out.append(row)
+    out["calls"] = rows_out
+    return out
+
+
 def only_arm(args):
     """One extra workload on its own (profiling entry point)."""
     import torch
@@ -830,6 +958,8 @@ def only_arm(args):
         out = reforder_workload(args, torch)
     elif args.only == "gemm":
         out = gemm_workload(args, torch)
+    elif args.only == "dropin":
+        out = dropin_workload(args, torch)
     else:
         from piqmc import fast, tools
         import scipy.sparse as sps
@@ -851,8 +981,10 @@ def reference_arm(args):
     line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": "updates/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp32/fp64", "data": "synthetic",
-            "config": {"workload": "80x80 periodic lattice, J~N(0,1) fp32, P=20, T=0.05, G linear 3.0->1e-8 "
-                                   "(every 20th of 2000 steps), one replica per host core",
+            "config": {"workload": "80x80 periodic lattice, J~N(0,1) fp32, P=20, T=0.05, G linear 3.0->1e-8; "
+                                   "each step a bounded sample of the 2000-step schedule: every 20th field value "
+                                   "(100 steps, 1.28e7 updates per process), one replica per host core",
+                       "sample": base["sample"],
                        "parallelism": "%d host processes" % base["cores"]},
             "cpu_baseline": base,
             "e2e": {"value": base["value"], "unit": "updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -871,7 +1003,7 @@ def main():
     ap.add_argument("--rpc", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched, dense and learned extras")
-    ap.add_argument("--only", choices=["batched", "dense", "learned", "reforder", "gemm"], default=None,
+    ap.add_argument("--only", choices=["batched", "dense", "learned", "reforder", "gemm", "dropin"], default=None,
                     help="run one extra workload alone (for profiling) and print its JSON")
     ap.add_argument("--batched-count", type=int, default=256)
     ap.add_argument("--batched-steps", type=int, default=500)

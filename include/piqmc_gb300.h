@@ -401,6 +401,32 @@ int pq_worldline_pass(void* words, int word_bits, int n, int P, int R, int maxde
                       const float* cpl, const float* field, int nclass, int stride, const int32_t* class_size,
                       float beta, uint32_t move, uint64_t seed, int replica_base, unsigned long long* counters,
                       void* stream);
+/* Pair world-line moves (new; no reference counterpart): the world-lines of the
+ * two spins of a bond flip together in every slice.  Bonds (device slots
+ * bond_i[b] < bond_j[b], total coupling bond_J[b], FP32) are grouped in classes
+ * [class_start[c], class_start[c + 1]) whose bonds are at graph distance >= 2
+ * (piqmc.pairs builds them), so a class's moves commute.  Cost, decision rule,
+ * uniforms and features are specified in csrc/mlp.cu.  pq_pair_pass: the
+ * uniform move (every bond tried, Metropolis), all classes in order.
+ * pq_pair_features: rows [0, M) the 8 features of the current pairs of bonds
+ * [first, first + count) of every replica (row r * count + b; BF16, ld 64), rows
+ * [Mpad, Mpad + M) of the flipped pairs, dE the move's classical cost.
+ * pq_pair_propose: the learned move of those bonds from the network's logits of
+ * both row sets: proposed with q = clamp(sigmoid(logit), qmin, 1), accepted with
+ * min(1, exp(-beta dE) q'/q).  counters (nullable): [tried/proposed, accepted].
+ * A slot outside [0, n) sets *status (nullable) to PQ_ERR_BAD_INDEX. */
+int pq_pair_pass(void* words, int word_bits, int n, int P, int R, int maxdeg, const int32_t* nbr, const float* cpl,
+                 const float* field, const int32_t* bond_i, const int32_t* bond_j, const float* bond_J,
+                 const int32_t* class_start, int nclass, float beta, uint32_t move, uint64_t seed, int replica_base,
+                 unsigned long long* counters, int32_t* status, void* stream);
+int pq_pair_features(const void* words, int word_bits, int n, int P, int R, int maxdeg, const int32_t* nbr,
+                     const float* cpl, const float* field, const int32_t* bond_i, const int32_t* bond_j,
+                     const float* bond_J, int first, int count, float beta, float jp, void* X, float* dE,
+                     int64_t Mpad, int32_t* status, void* stream);
+int pq_pair_propose(void* words, int word_bits, int n, int P, int R, const int32_t* bond_i, const int32_t* bond_j,
+                    int first, int count, int cls, const float* logit, const float* dE, int64_t Mpad, float qmin,
+                    float beta, uint32_t move, uint64_t seed, int replica_base, unsigned long long* counters,
+                    int32_t* status, void* stream);
 /* Training (BCE with soft targets y, mean over the batch B): head backward
  * (dH2 row-major and transposed, grads of w3, b3, loss), hidden backward
  * (mask by relu'(H1), transposed BF16 dH1, grad of b1), column sums, BF16

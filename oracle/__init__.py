@@ -22,7 +22,8 @@ Pinned to the reference itself: the golden vectors in tests/golden/ were recorde
 its compiled Cython code, and where that code is built here (oracle/build_ref.py)
 tests/test_oracle_vs_reference.py compares the two on random cases.
 
-``fast_oracle.c`` (``fast_anneal``, ``dense_sweep``, ``philox4x32_10``, ``expf_neg``)
+``fast_oracle.c`` (``fast_anneal``, ``dense_sweep``, ``pair_class``, ``pair_features``,
+``philox4x32_10``, ``expf_neg``)
 restates this library's own packed algorithms, which have no reference counterpart:
 it is the bit-exact check of those kernels, pinned by Philox's published known-answer
 vectors and, statistically, by the reference (tests/test_statistics.py).
@@ -103,6 +104,14 @@ def _setup_fast(L):
     L.orc_fast_anneal.argtypes = [i32, i32, i32, P, P, P, i32, i32, P, i32, P, i32, i32, f32, u64,
                                   i64, i32, i32, P, P]
     L.orc_fast_anneal.restype = i64
+    if hasattr(L, "orc_pair_class"):
+        L.orc_pair_features.argtypes = [P, i32, i32, i32, P, P, P, i32, i32, f32, f32, f32, i32, P]
+        L.orc_pair_features.restype = f32
+        L.orc_pair_class.argtypes = [P, i32, i32, i32, P, P, P, P, P, P, i32, i32, i32, f32, f32, P, P,
+                                     ctypes.c_uint32, u64, ctypes.c_uint32]
+        L.orc_pair_class.restype = i64
+        L.orc_pair_sigmoid.argtypes = [f32]
+        L.orc_pair_sigmoid.restype = f32
     if hasattr(L, "orc_dense_sweep"):
         L.orc_dense_sweep.argtypes = [i32, i32, P, P, P, i32, P, i32, i32, f32, u64, i64, i32, P, i32]
         L.orc_dense_sweep.restype = i64
@@ -320,3 +329,49 @@ def generate_neighbors(nspins, J, maxnb):
                 nbs[ispin, ipair] = (pair[0], J[pair])
                 ipair += 1
     return nbs
+
+
+# ----------------------------------------------------------------------------------------
+# pair world-line moves (this library's own move; restated in fast_oracle.c)
+# ----------------------------------------------------------------------------------------
+
+def _tables(nbr, cpl, field):
+    nbr = np.ascontiguousarray(nbr, dtype=np.int32)
+    cpl = np.ascontiguousarray(cpl, dtype=np.float32)
+    field = np.ascontiguousarray(field, dtype=np.float32)
+    maxdeg = nbr.shape[0] if nbr.ndim == 2 else 0
+    return nbr, cpl, field, maxdeg
+
+
+def pair_features(words, nbr, cpl, field, P, si, sj, Jb, beta, jp, flipped=False):
+    """(features[8] FP32, cost dE) of the pair (si, sj) of one replica (words uint64 per slot)."""
+    nbr, cpl, field, maxdeg = _tables(nbr, cpl, field)
+    w = np.ascontiguousarray(words, dtype=np.uint64)
+    x = np.zeros(8, np.float32)
+    dE = lib().orc_pair_features(_p(w), len(w), int(P), maxdeg, _p(nbr), _p(cpl), _p(field), int(si), int(sj),
+                                 float(np.float32(Jb)), float(np.float32(beta)), float(np.float32(jp)),
+                                 int(bool(flipped)), _p(x))
+    return x, np.float32(dE)
+
+
+def pair_class(words, nbr, cpl, field, P, bond_i, bond_j, bond_J, first, count, cls, beta, seed, move, replica,
+               qmin=0.05, logit=None, logit_f=None):
+    """The pair moves of bonds [first, first + count) of one replica, in place on ``words`` (uint64 per slot).
+
+    Uniform (every bond tried) when ``logit`` is None, else the learned move with the
+    network's logits of the current (``logit``) and flipped (``logit_f``) pairs."""
+    nbr, cpl, field, maxdeg = _tables(nbr, cpl, field)
+    bi = np.ascontiguousarray(bond_i, dtype=np.int32)
+    bj = np.ascontiguousarray(bond_j, dtype=np.int32)
+    bJ = np.ascontiguousarray(bond_J, dtype=np.float32)
+    lg = None if logit is None else np.ascontiguousarray(logit, dtype=np.float32)
+    lf = None if logit_f is None else np.ascontiguousarray(logit_f, dtype=np.float32)
+    return int(lib().orc_pair_class(_p(words), len(words), int(P), maxdeg, _p(nbr), _p(cpl), _p(field), _p(bi),
+                                    _p(bj), _p(bJ), int(first), int(count), int(cls), float(np.float32(beta)),
+                                    float(np.float32(qmin)), None if lg is None else _p(lg),
+                                    None if lf is None else _p(lf), int(move) & 0xFFFFFFFF,
+                                    int(seed) & 0xFFFFFFFFFFFFFFFF, int(replica) & 0xFFFFFFFF))
+
+
+def pair_sigmoid(z):
+    return np.float32(lib().orc_pair_sigmoid(float(np.float32(z))))

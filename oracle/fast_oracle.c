@@ -266,3 +266,107 @@ int64_t orc_dense_sweep(int N, int P, float* F, const float* K, const int32_t* u
     }
     return nacc;
 }
+
+/* ---------------------------------------------------------------------------
+ * Pair world-line moves (this library's own move; no reference counterpart),
+ * restated from the specification in csrc/mlp.cu: the world-lines of the two
+ * spins of a bond flip together.  One replica; w holds device slot i's
+ * world-line (bit k set = -1).  FP32, one rounding per operation, in order.
+ * ------------------------------------------------------------------------- */
+static inline int popc64(uint64_t x) { return __builtin_popcountll(x); }
+
+/* sum_k s^k f^k of slot s: h (P - 2 popc(w_s)), then + J_m (P - 2 popc(w_s ^ w_m)), m in table order */
+static float wl_align(const uint64_t* w, int s, uint64_t ws, int n, int P, int maxdeg, const int32_t* nbr,
+                      const float* cpl, const float* field, int si, int sj, uint64_t fi, uint64_t fj, int flipped) {
+    const uint64_t mask = P >= 64 ? ~(uint64_t)0 : (((uint64_t)1 << P) - 1);
+    float sa = field[s] * (float)(P - 2 * popc64(ws & mask));
+    for (int m = 0; m < maxdeg; ++m) {
+        const int j = nbr[(int64_t)m * n + s];
+        uint64_t wm = w[j];
+        if (flipped) wm = j == sj ? fj : (j == si ? fi : wm);
+        sa = sa + cpl[(int64_t)m * n + s] * (float)(P - 2 * popc64((ws ^ wm) & mask));
+    }
+    return sa;
+}
+
+static float clip8f(float v) { return v < -8.0f ? -8.0f : (v > 8.0f ? 8.0f : v); }
+
+/* Features x[8] and cost of the pair (si, sj) in the current state (flipped = 0) or
+ * with both world-lines flipped (flipped = 1).  Returns the cost dE. */
+float orc_pair_features(const uint64_t* w, int n, int P, int maxdeg, const int32_t* nbr, const float* cpl,
+                        const float* field, int si, int sj, float Jb, float beta, float jp, int flipped, float* x) {
+    const uint64_t mask = P >= 64 ? ~(uint64_t)0 : (((uint64_t)1 << P) - 1);
+    const uint64_t fi = w[si] ^ mask, fj = w[sj] ^ mask;
+    const uint64_t wi = flipped ? fi : w[si], wj = flipped ? fj : w[sj];
+    const float dEi = 2.0f * wl_align(w, si, wi, n, P, maxdeg, nbr, cpl, field, si, sj, fi, fj, flipped);
+    const float dEj = 2.0f * wl_align(w, sj, wj, n, P, maxdeg, nbr, cpl, field, si, sj, fi, fj, flipped);
+    const int c = P - 2 * popc64((wi ^ wj) & mask);
+    const float dE = (dEi + dEj) - 4.0f * (Jb * (float)c);
+    if (x) {
+        const float inv = 1.0f / (float)P;
+        const uint64_t mi = wi & mask, mj = wj & mask;
+        const uint64_t roti = ((mi >> 1) | (mi << (P - 1))) & mask, rotj = ((mj >> 1) | (mj << (P - 1))) & mask;
+        x[0] = clip8f((beta * dE) * inv);
+        x[1] = clip8f((beta * dEi) * inv);
+        x[2] = clip8f((beta * dEj) * inv);
+        x[3] = ((Jb * (float)c) * inv) / (1.0f + fabsf(Jb));
+        x[4] = (float)(popc64(mi ^ roti) + popc64(mj ^ rotj)) / (float)(2 * P);
+        x[5] = ((float)(P - 2 * popc64(mi)) * inv) * ((float)(P - 2 * popc64(mj)) * inv);
+        {
+            float v = (jp * beta) * inv;
+            x[6] = v < 0.0f ? 0.0f : (v > 8.0f ? 8.0f : v);
+        }
+        x[7] = 1.0f;
+    }
+    return dE;
+}
+
+float orc_pair_sigmoid(float z) {
+    if (z >= 0.0f) return 1.0f / (1.0f + orc_expf(-z));
+    const float e = orc_expf(z);
+    return e / (1.0f + e);
+}
+
+int orc_pair_accept(float dE, float beta, float q, float qf, float u) {
+    const float x = -(beta * dE);
+    const float uq = u * q;
+    if (x <= 0.0f) return uq < qf * orc_expf(x);
+    return (uq * orc_expf(-x)) < qf;
+}
+
+/* The pair moves of bonds [first, first + count) of class cls for one replica.
+ * logit == NULL: the uniform move (q = q' = 1); else logit[b - first] scores the
+ * current pair and logit_f[b - first] the flipped one.  Returns accepted moves. */
+int64_t orc_pair_class(uint64_t* w, int n, int P, int maxdeg, const int32_t* nbr, const float* cpl,
+                       const float* field, const int32_t* bi, const int32_t* bj, const float* bJ, int first,
+                       int count, int cls, float beta, float qmin, const float* logit, const float* logit_f,
+                       uint32_t move, uint64_t seed, uint32_t replica) {
+    const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    const uint64_t mask = P >= 64 ? ~(uint64_t)0 : (((uint64_t)1 << P) - 1);
+    int64_t nacc = 0;
+    /* the moves of a class commute: decide all from the state at the start of the class */
+    uint8_t* flip = (uint8_t*)__builtin_alloca(count > 0 ? count : 1);
+    for (int t = 0; t < count; ++t) {
+        const int b = first + t;
+        uint32_t u[4];
+        const uint32_t ctr[4] = {(uint32_t)b, move, replica, (5u << 24) | (uint32_t)cls};
+        orc_philox4x32_10(ctr, key, u);
+        const float dE = orc_pair_features(w, n, P, maxdeg, nbr, cpl, field, bi[b], bj[b], bJ[b], beta, 0.0f, 0, NULL);
+        float q = 1.0f, qf = 1.0f;
+        if (logit) {
+            q = orc_pair_sigmoid(logit[t]);
+            q = q < qmin ? qmin : (q > 1.0f ? 1.0f : q);
+            qf = orc_pair_sigmoid(logit_f[t]);
+            qf = qf < qmin ? qmin : (qf > 1.0f ? 1.0f : qf);
+        }
+        const int proposed = u01(u[0]) < q;
+        flip[t] = (uint8_t)(proposed && orc_pair_accept(dE, beta, q, qf, u01(u[1])));
+    }
+    for (int t = 0; t < count; ++t)
+        if (flip[t]) {
+            w[bi[first + t]] ^= mask;
+            w[bj[first + t]] ^= mask;
+            ++nacc;
+        }
+    return nacc;
+}

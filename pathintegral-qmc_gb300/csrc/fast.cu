@@ -90,13 +90,39 @@ __global__ void energy_packed_kernel(const W* __restrict__ words, int n, int P, 
     if (lane == 0) out[warp] = -acc;
 }
 
+// Configuration streaming between the int8 layout [R][n][P] and packed words.
+// A block of kStreamThreads threads owns kStreamThreads consecutive (replica, spin)
+// items t = r n + i, whose spins are one contiguous run of kStreamThreads * P bytes;
+// the run moves between global and shared memory as 16-byte vectors when its start
+// is 16-byte aligned (byte by byte otherwise), and each thread packs or unpacks its
+// own P bytes in shared memory.
+constexpr int kStreamThreads = 256;
+
+__device__ __forceinline__ bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
 template <typename W>
-__global__ void pack_kernel(const int8_t* __restrict__ spins, int n, int P, int R, const int32_t* __restrict__ perm,
-                            W* __restrict__ words, int stride) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (int64_t)R * n) return;
+__global__ void __launch_bounds__(kStreamThreads) pack_kernel(const int8_t* __restrict__ spins, int n, int P, int R,
+                                                            const int32_t* __restrict__ perm, W* __restrict__ words,
+                                                            int stride) {
+    extern __shared__ __align__(16) int8_t run[];
+    const int64_t total = (int64_t)R * n;
+    const int64_t t0 = (int64_t)blockIdx.x * kStreamThreads;
+    const int items = (int)min((int64_t)kStreamThreads, total - t0);
+    const int nbytes = items * P;
+    const int8_t* src = spins + t0 * P;
+    if (aligned16(src)) {
+        const int nvec = nbytes >> 4;
+        for (int v = threadIdx.x; v < nvec; v += kStreamThreads)
+            reinterpret_cast<int4*>(run)[v] = __ldg(reinterpret_cast<const int4*>(src) + v);
+        for (int b = (nvec << 4) + threadIdx.x; b < nbytes; b += kStreamThreads) run[b] = src[b];
+    } else {
+        for (int b = threadIdx.x; b < nbytes; b += kStreamThreads) run[b] = src[b];
+    }
+    __syncthreads();
+    if ((int)threadIdx.x >= items) return;
+    const int64_t t = t0 + threadIdx.x;
     const int r = (int)(t / n), i = (int)(t % n);
-    const int8_t* s = spins + t * P;
+    const int8_t* s = run + threadIdx.x * P;
     W w = 0;
     for (int k = 0; k < P; ++k) w |= (W)(s[k] < 0) << k;
     const int di = perm ? perm[i] : i;
@@ -104,15 +130,32 @@ __global__ void pack_kernel(const int8_t* __restrict__ spins, int n, int P, int 
 }
 
 template <typename W>
-__global__ void unpack_kernel(const W* __restrict__ words, int n, int P, int R, const int32_t* __restrict__ perm,
-                              int stride, int8_t* __restrict__ spins) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (int64_t)R * n) return;
-    const int r = (int)(t / n), i = (int)(t % n);
-    const int di = perm ? perm[i] : i;
-    const W w = (unsigned)di < (unsigned)stride ? words[(int64_t)r * stride + di] : (W)0;
-    int8_t* s = spins + t * P;
-    for (int k = 0; k < P; ++k) s[k] = ((w >> k) & 1) ? -1 : 1;
+__global__ void __launch_bounds__(kStreamThreads) unpack_kernel(const W* __restrict__ words, int n, int P, int R,
+                                                              const int32_t* __restrict__ perm, int stride,
+                                                              int8_t* __restrict__ spins) {
+    extern __shared__ __align__(16) int8_t run[];
+    const int64_t total = (int64_t)R * n;
+    const int64_t t0 = (int64_t)blockIdx.x * kStreamThreads;
+    const int items = (int)min((int64_t)kStreamThreads, total - t0);
+    if ((int)threadIdx.x < items) {
+        const int64_t t = t0 + threadIdx.x;
+        const int r = (int)(t / n), i = (int)(t % n);
+        const int di = perm ? perm[i] : i;
+        const W w = (unsigned)di < (unsigned)stride ? words[(int64_t)r * stride + di] : (W)0;
+        int8_t* s = run + threadIdx.x * P;
+        for (int k = 0; k < P; ++k) s[k] = ((w >> k) & 1) ? -1 : 1;
+    }
+    __syncthreads();
+    const int nbytes = items * P;
+    int8_t* dst = spins + t0 * P;
+    if (aligned16(dst)) {
+        const int nvec = nbytes >> 4;
+        for (int v = threadIdx.x; v < nvec; v += kStreamThreads)
+            reinterpret_cast<int4*>(dst)[v] = reinterpret_cast<const int4*>(run)[v];
+        for (int b = (nvec << 4) + threadIdx.x; b < nbytes; b += kStreamThreads) dst[b] = run[b];
+    } else {
+        for (int b = threadIdx.x; b < nbytes; b += kStreamThreads) dst[b] = run[b];
+    }
 }
 
 template <typename W, int MAXDEG, int NQC>
@@ -239,10 +282,13 @@ int pq_pack_spins(const int8_t* spins, int n, int P, int R, const int32_t* perm,
     if (!((word_bits == 32 && P <= 32) || (word_bits == 64 && P <= 64))) return PQ_ERR_INVALID_ARG;
     if (R == 0) return PQ_OK;
     const int64_t tot = (int64_t)R * n;
-    const unsigned blocks = (unsigned)((tot + 255) / 256);
+    const unsigned blocks = (unsigned)((tot + kStreamThreads - 1) / kStreamThreads);
+    const size_t smem = (size_t)kStreamThreads * P;   // at most 16 KB (P <= 64)
     cudaStream_t st = (cudaStream_t)stream;
-    if (word_bits == 32) pack_kernel<uint32_t><<<blocks, 256, 0, st>>>(spins, n, P, R, perm, (uint32_t*)words, word_stride);
-    else pack_kernel<uint64_t><<<blocks, 256, 0, st>>>(spins, n, P, R, perm, (uint64_t*)words, word_stride);
+    if (word_bits == 32)
+        pack_kernel<uint32_t><<<blocks, kStreamThreads, smem, st>>>(spins, n, P, R, perm, (uint32_t*)words, word_stride);
+    else
+        pack_kernel<uint64_t><<<blocks, kStreamThreads, smem, st>>>(spins, n, P, R, perm, (uint64_t*)words, word_stride);
     return pq_launch_status();
 }
 
@@ -252,10 +298,15 @@ int pq_unpack_spins(const void* words, int word_bits, int n, int P, int R, const
     if (!((word_bits == 32 && P <= 32) || (word_bits == 64 && P <= 64))) return PQ_ERR_INVALID_ARG;
     if (R == 0) return PQ_OK;
     const int64_t tot = (int64_t)R * n;
-    const unsigned blocks = (unsigned)((tot + 255) / 256);
+    const unsigned blocks = (unsigned)((tot + kStreamThreads - 1) / kStreamThreads);
+    const size_t smem = (size_t)kStreamThreads * P;
     cudaStream_t st = (cudaStream_t)stream;
-    if (word_bits == 32) unpack_kernel<uint32_t><<<blocks, 256, 0, st>>>((const uint32_t*)words, n, P, R, perm, word_stride, spins);
-    else unpack_kernel<uint64_t><<<blocks, 256, 0, st>>>((const uint64_t*)words, n, P, R, perm, word_stride, spins);
+    if (word_bits == 32)
+        unpack_kernel<uint32_t><<<blocks, kStreamThreads, smem, st>>>((const uint32_t*)words, n, P, R, perm,
+                                                                      word_stride, spins);
+    else
+        unpack_kernel<uint64_t><<<blocks, kStreamThreads, smem, st>>>((const uint64_t*)words, n, P, R, perm,
+                                                                      word_stride, spins);
     return pq_launch_status();
 }
 

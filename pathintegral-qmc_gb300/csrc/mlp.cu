@@ -225,6 +225,240 @@ __global__ void propose_kernel(W* __restrict__ words, int n, int P, int R, int c
 }
 
 // ---------------------------------------------------------------------------
+// Pair world-line moves (no reference counterpart): the world-lines of the two
+// spins i, j of a bond (total coupling J_b between them) flip together, in every
+// slice.  Local sweeps and single world-line flips leave the anneal in states
+// that are stable against single flips but not against flipping two coupled
+// spins; this move reaches them.
+//  * cost: dE = fl(fl(2 sa_i) + fl(2 sa_j)) - fl(4 fl(J_b c)), c = P - 2 popc(w_i ^ w_j),
+//    sa = worldline_align (the bond's own term is unchanged by the move);
+//  * bonds are visited class by class: no endpoint of a bond of a class is an
+//    endpoint of, or a neighbour of an endpoint of, another bond of the class, so a
+//    pair flip changes neither the cost nor the features of another bond of its class;
+//  * decision with proposal probabilities q (current pair) and q' (flipped pair),
+//    x = -fl(beta dE), u uniform: x <= 0 accepts iff fl(u q) < fl(q' expf_neg(x)),
+//    x > 0 accepts iff fl(fl(u q) expf_neg(-x)) < q' -- the Metropolis-Hastings test
+//    u < exp(x) q'/q; the uniform pass has q = q' = 1 (every bond tried);
+//  * proposal: q = clamp(sigmoid(logit), qmin, 1), sigmoid(z) = 1 / (1 + expf_neg(-z))
+//    for z >= 0 and e / (1 + e) with e = expf_neg(z) for z < 0;
+//  * uniforms: Philox(ctr = {bond id, move, replica, 5 << 24 | class}), word 0 proposes,
+//    word 1 accepts;
+//  * features of a pair state (the reverse row is the same function of the flipped state):
+//    x0, x1, x2 = beta dE / P, beta dE_i / P, beta dE_j / P clipped to [-8, 8] (dE_i = 2 sa_i,
+//    the single world-line flip cost), x3 = (J_b c / P) / (1 + |J_b|),
+//    x4 = (kinks_i + kinks_j) / (2 P), x5 = m_i m_j (world-line magnetisations),
+//    x6 = clip(jp beta / P, 0, 8), x7 = 1.
+// ---------------------------------------------------------------------------
+template <typename W, int MAXD>
+struct PairIn {
+    int si, sj;                 // the bond's slots
+    W wi, wj;
+    W nbi[MAXD], nbj[MAXD];     // neighbour world-lines
+    int ii[MAXD], ij[MAXD];     // neighbour slots
+    float Ji[MAXD], Jj[MAXD];
+    float hi, hj, Jb;
+};
+
+template <typename W, int MAXD>
+__device__ __forceinline__ void load_side(const W* __restrict__ words_r, int s, int n, int maxdeg,
+                                          const int32_t* __restrict__ nbr, const float* __restrict__ cpl,
+                                          W (&nb)[MAXD], int (&ix)[MAXD], float (&J)[MAXD], bool& bad) {
+#pragma unroll
+    for (int m = 0; m < MAXD; ++m) {
+        J[m] = 0.0f;
+        ix[m] = s;
+        nb[m] = words_r[s];
+        if (m < maxdeg) {
+            int j = __ldg(nbr + (int64_t)m * n + s);
+            if ((unsigned)j >= (unsigned)n) { bad = true; j = s; }
+            ix[m] = j;
+            J[m] = __ldg(cpl + (int64_t)m * n + s);
+            nb[m] = words_r[j];
+        }
+    }
+}
+
+template <typename W, int MAXD>
+__device__ __forceinline__ void load_pair(const W* __restrict__ words_r, int si, int sj, float Jb, int n, int maxdeg,
+                                          const int32_t* __restrict__ nbr, const float* __restrict__ cpl,
+                                          const float* __restrict__ field, PairIn<W, MAXD>& p, bool& bad) {
+    p.si = si; p.sj = sj; p.Jb = Jb;
+    p.wi = words_r[si];
+    p.wj = words_r[sj];
+    p.hi = __ldg(field + si);
+    p.hj = __ldg(field + sj);
+    load_side<W, MAXD>(words_r, si, n, maxdeg, nbr, cpl, p.nbi, p.ii, p.Ji, bad);
+    load_side<W, MAXD>(words_r, sj, n, maxdeg, nbr, cpl, p.nbj, p.ij, p.Jj, bad);
+}
+
+// The pair state after the move: both world-lines flipped, wherever they appear.
+template <typename W, int MAXD>
+__device__ __forceinline__ void flip_pair(PairIn<W, MAXD>& p, W mask) {
+    const W fi = p.wi ^ mask, fj = p.wj ^ mask;
+#pragma unroll
+    for (int m = 0; m < MAXD; ++m) {
+        p.nbi[m] = p.ii[m] == p.sj ? fj : (p.ii[m] == p.si ? fi : p.nbi[m]);
+        p.nbj[m] = p.ij[m] == p.si ? fi : (p.ij[m] == p.sj ? fj : p.nbj[m]);
+    }
+    p.wi = fi;
+    p.wj = fj;
+}
+
+template <typename W, int MAXD>
+__device__ __forceinline__ float pair_cost(const PairIn<W, MAXD>& p, int P, int maxdeg, W mask, float& dEi,
+                                           float& dEj, int& c) {
+    dEi = __fmul_rn(2.0f, worldline_align<W, MAXD>(p.wi & mask, p.nbi, p.Ji, maxdeg, p.hi, P, mask));
+    dEj = __fmul_rn(2.0f, worldline_align<W, MAXD>(p.wj & mask, p.nbj, p.Jj, maxdeg, p.hj, P, mask));
+    c = P - 2 * popc_((p.wi ^ p.wj) & mask);
+    return __fsub_rn(__fadd_rn(dEi, dEj), __fmul_rn(4.0f, __fmul_rn(p.Jb, (float)c)));
+}
+
+__device__ __forceinline__ float clip8(float v) { return fminf(fmaxf(v, -8.0f), 8.0f); }
+
+template <typename W, int MAXD>
+__device__ __forceinline__ float pair_features(const PairIn<W, MAXD>& p, int P, int maxdeg, float beta, float jp,
+                                               float (&x)[kFeat]) {
+    const W mask = slice_mask<W>(P);
+    float dEi, dEj;
+    int c;
+    const float dE = pair_cost<W, MAXD>(p, P, maxdeg, mask, dEi, dEj, c);
+    const float inv = __fdiv_rn(1.0f, (float)P);
+    const W wi = p.wi & mask, wj = p.wj & mask;
+    const W roti = ((wi >> 1) | (wi << (P - 1))) & mask, rotj = ((wj >> 1) | (wj << (P - 1))) & mask;
+    x[0] = clip8(__fmul_rn(__fmul_rn(beta, dE), inv));
+    x[1] = clip8(__fmul_rn(__fmul_rn(beta, dEi), inv));
+    x[2] = clip8(__fmul_rn(__fmul_rn(beta, dEj), inv));
+    x[3] = __fdiv_rn(__fmul_rn(__fmul_rn(p.Jb, (float)c), inv), __fadd_rn(1.0f, fabsf(p.Jb)));
+    x[4] = __fdiv_rn((float)(popc_(wi ^ roti) + popc_(wj ^ rotj)), (float)(2 * P));
+    x[5] = __fmul_rn(__fmul_rn((float)(P - 2 * popc_(wi)), inv), __fmul_rn((float)(P - 2 * popc_(wj)), inv));
+    x[6] = fminf(fmaxf(__fmul_rn(__fmul_rn(jp, beta), inv), 0.0f), 8.0f);
+    x[7] = 1.0f;
+    return dE;
+}
+
+__device__ __forceinline__ float pair_sigmoid(float z) {
+    if (z >= 0.0f) return __fdiv_rn(1.0f, __fadd_rn(1.0f, pq_expf_neg(-z)));
+    const float e = pq_expf_neg(z);
+    return __fdiv_rn(e, __fadd_rn(1.0f, e));
+}
+
+__device__ __forceinline__ bool pair_accept(float dE, float beta, float q, float qf, float u) {
+    const float x = -__fmul_rn(beta, dE);
+    const float uq = __fmul_rn(u, q);
+    if (x <= 0.0f) return uq < __fmul_rn(qf, pq_expf_neg(x));
+    return __fmul_rn(uq, pq_expf_neg(-x)) < qf;
+}
+
+template <typename W>
+__device__ __forceinline__ void pair_apply(W* __restrict__ words_r, int si, int sj, int P) {
+    const W mask = slice_mask<W>(P);
+    words_r[si] ^= mask;
+    words_r[sj] ^= mask;
+}
+
+// Rows [0, M): features of the current pairs of bonds [first, first + count) (all
+// replicas, row = r * count + b); rows [Mpad, Mpad + M): of the flipped pairs;
+// dE[row] = cost of the move.
+template <typename W, int MAXD>
+__global__ void pair_features_kernel(const W* __restrict__ words, int n, int P, int R, int maxdeg,
+                                     const int32_t* __restrict__ nbr, const float* __restrict__ cpl,
+                                     const float* __restrict__ field, const int32_t* __restrict__ bi,
+                                     const int32_t* __restrict__ bj, const float* __restrict__ bJ, int first,
+                                     int count, float beta, float jp, __nv_bfloat16* __restrict__ X,
+                                     float* __restrict__ dE, int64_t Mpad, int32_t* __restrict__ status) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t M = (int64_t)R * count;
+    if (t >= M) return;
+    const int r = (int)(t / count), b = first + (int)(t % count);
+    const int si = bi[b], sj = bj[b];
+    if ((unsigned)si >= (unsigned)n || (unsigned)sj >= (unsigned)n) {
+        pq_set_status(status, PQ_ERR_BAD_INDEX);
+        return;
+    }
+    bool bad = false;
+    PairIn<W, MAXD> p;
+    load_pair<W, MAXD>(words + (int64_t)r * n, si, sj, bJ[b], n, maxdeg, nbr, cpl, field, p, bad);
+    float x[kFeat];
+    dE[t] = pair_features<W, MAXD>(p, P, maxdeg, beta, jp, x);
+    __nv_bfloat16* row = X + t * kLd;
+#pragma unroll
+    for (int k = 0; k < kFeat; ++k) row[k] = __float2bfloat16_rn(x[k]);
+    flip_pair<W, MAXD>(p, slice_mask<W>(P));
+    pair_features<W, MAXD>(p, P, maxdeg, beta, jp, x);
+    __nv_bfloat16* rowf = X + (Mpad + t) * kLd;
+#pragma unroll
+    for (int k = 0; k < kFeat; ++k) rowf[k] = __float2bfloat16_rn(x[k]);
+    if (bad) pq_set_status(status, PQ_ERR_BAD_INDEX);
+}
+
+// The learned pair move of bonds [first, first + count), from the logits of the
+// features rows (current at t, flipped at Mpad + t) and their costs.
+template <typename W>
+__global__ void pair_propose_kernel(W* __restrict__ words, int n, int P, int R, const int32_t* __restrict__ bi,
+                                    const int32_t* __restrict__ bj, int first, int count, int cls,
+                                    const float* __restrict__ logit, const float* __restrict__ dE, int64_t Mpad,
+                                    float qmin, float beta, uint32_t move, uint32_t key0, uint32_t key1,
+                                    uint32_t replica_base, unsigned long long* __restrict__ counters,
+                                    int32_t* __restrict__ status) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t M = (int64_t)R * count;
+    if (t >= M) return;
+    const int r = (int)(t / count), b = first + (int)(t % count);
+    const int si = bi[b], sj = bj[b];
+    if ((unsigned)si >= (unsigned)n || (unsigned)sj >= (unsigned)n) {
+        pq_set_status(status, PQ_ERR_BAD_INDEX);
+        return;
+    }
+    const pq_u32x4 u = pq_philox(pq_u32x4{(uint32_t)b, move, replica_base + (uint32_t)r, (5u << 24) | (uint32_t)cls},
+                                 key0, key1);
+    const float q = fminf(fmaxf(pair_sigmoid(logit[t]), qmin), 1.0f);
+    const float qf = fminf(fmaxf(pair_sigmoid(logit[Mpad + t]), qmin), 1.0f);
+    const bool proposed = pq_u01(u.x) < q;
+    const bool acc = proposed && pair_accept(dE[t], beta, q, qf, pq_u01(u.y));
+    if (acc) pair_apply<W>(words + (int64_t)r * n, si, sj, P);
+    if (counters) {
+        if (proposed) atomicAdd(counters, 1ull);
+        if (acc) atomicAdd(counters + 1, 1ull);
+    }
+}
+
+// The uniform pair move (q = q' = 1) of bonds [first, first + count): cost and decision only.
+template <typename W, int MAXD>
+__global__ void pair_uniform_kernel(W* __restrict__ words, int n, int P, int R, int maxdeg,
+                                    const int32_t* __restrict__ nbr, const float* __restrict__ cpl,
+                                    const float* __restrict__ field, const int32_t* __restrict__ bi,
+                                    const int32_t* __restrict__ bj, const float* __restrict__ bJ, int first,
+                                    int count, int cls, float beta, uint32_t move, uint32_t key0, uint32_t key1,
+                                    uint32_t replica_base, unsigned long long* __restrict__ counters,
+                                    int32_t* __restrict__ status) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t M = (int64_t)R * count;
+    if (t >= M) return;
+    const int r = (int)(t / count), b = first + (int)(t % count);
+    const int si = bi[b], sj = bj[b];
+    if ((unsigned)si >= (unsigned)n || (unsigned)sj >= (unsigned)n) {
+        pq_set_status(status, PQ_ERR_BAD_INDEX);
+        return;
+    }
+    bool bad = false;
+    PairIn<W, MAXD> p;
+    W* words_r = words + (int64_t)r * n;
+    load_pair<W, MAXD>(words_r, si, sj, bJ[b], n, maxdeg, nbr, cpl, field, p, bad);
+    float dEi, dEj;
+    int c;
+    const float dE = pair_cost<W, MAXD>(p, P, maxdeg, slice_mask<W>(P), dEi, dEj, c);
+    const pq_u32x4 u = pq_philox(pq_u32x4{(uint32_t)b, move, replica_base + (uint32_t)r, (5u << 24) | (uint32_t)cls},
+                                 key0, key1);
+    const bool acc = pair_accept(dE, beta, 1.0f, 1.0f, pq_u01(u.y));
+    if (acc) pair_apply<W>(words_r, si, sj, P);
+    if (counters) {
+        atomicAdd(counters, 1ull);
+        if (acc) atomicAdd(counters + 1, 1ull);
+    }
+    if (bad) pq_set_status(status, PQ_ERR_BAD_INDEX);
+}
+
+// ---------------------------------------------------------------------------
 // training: binary cross-entropy against soft targets y (the Metropolis
 // acceptance probability of the recorded move), mean over the batch.
 // ---------------------------------------------------------------------------
@@ -788,6 +1022,74 @@ int pq_worldline_pass(void* words, int word_bits, int n, int P, int R, int maxde
     for (int c = 0; c < nclass; ++c) {
         const int rc = pq_worldline_move(words, word_bits, n, P, R, maxdeg, nbr, cpl, field, c, stride, class_size[c],
                                          beta, move, seed, replica_base, counters, stream);
+        if (rc != PQ_OK) return rc;
+    }
+    return PQ_OK;
+}
+
+int pq_pair_features(const void* words, int word_bits, int n, int P, int R, int maxdeg, const int32_t* nbr,
+                     const float* cpl, const float* field, const int32_t* bond_i, const int32_t* bond_j,
+                     const float* bond_J, int first, int count, float beta, float jp, void* X, float* dE,
+                     int64_t Mpad, int32_t* status, void* stream) {
+    if (!words || !field || !bond_i || !bond_j || !bond_J || !X || !dE || n <= 0 || P < 1 || P > 64 || R <= 0 ||
+        first < 0 || count < 0 || maxdeg < 0 || maxdeg > 16 || (maxdeg > 0 && (!nbr || !cpl)) ||
+        Mpad < (int64_t)R * count || (P > 32 && word_bits != 64))
+        return PQ_ERR_INVALID_ARG;
+    const int64_t M = (int64_t)R * count;
+    if (M == 0) return PQ_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    PQ_WORD_DEG_DISPATCH(word_bits, maxdeg,
+                         (pair_features_kernel<W, D><<<blocks_for(M), 256, 0, st>>>(
+                             (const W*)words, n, P, R, maxdeg, nbr, cpl, field, bond_i, bond_j, bond_J, first, count,
+                             beta, jp, (__nv_bfloat16*)X, dE, Mpad, status)));
+    return pq_launch_status();
+}
+
+int pq_pair_propose(void* words, int word_bits, int n, int P, int R, const int32_t* bond_i, const int32_t* bond_j,
+                    int first, int count, int cls, const float* logit, const float* dE, int64_t Mpad, float qmin,
+                    float beta, uint32_t move, uint64_t seed, int replica_base, unsigned long long* counters,
+                    int32_t* status, void* stream) {
+    if (!words || !bond_i || !bond_j || !logit || !dE || n <= 0 || P < 1 || P > 64 || R <= 0 || first < 0 ||
+        count < 0 || Mpad < (int64_t)R * count || !(qmin > 0.0f) || qmin > 1.0f || (P > 32 && word_bits != 64))
+        return PQ_ERR_INVALID_ARG;
+    const int64_t M = (int64_t)R * count;
+    if (M == 0) return PQ_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    if (word_bits == 32)
+        pair_propose_kernel<uint32_t><<<blocks_for(M), 256, 0, st>>>((uint32_t*)words, n, P, R, bond_i, bond_j, first,
+                                                                     count, cls, logit, dE, Mpad, qmin, beta, move, k0,
+                                                                     k1, (uint32_t)replica_base, counters, status);
+    else if (word_bits == 64)
+        pair_propose_kernel<uint64_t><<<blocks_for(M), 256, 0, st>>>((uint64_t*)words, n, P, R, bond_i, bond_j, first,
+                                                                     count, cls, logit, dE, Mpad, qmin, beta, move, k0,
+                                                                     k1, (uint32_t)replica_base, counters, status);
+    else
+        return PQ_ERR_INVALID_ARG;
+    return pq_launch_status();
+}
+
+int pq_pair_pass(void* words, int word_bits, int n, int P, int R, int maxdeg, const int32_t* nbr, const float* cpl,
+                 const float* field, const int32_t* bond_i, const int32_t* bond_j, const float* bond_J,
+                 const int32_t* class_start, int nclass, float beta, uint32_t move, uint64_t seed, int replica_base,
+                 unsigned long long* counters, int32_t* status, void* stream) {
+    if (!words || !field || !bond_i || !bond_j || !bond_J || !class_start || nclass < 0 || n <= 0 || P < 1 ||
+        P > 64 || R <= 0 || maxdeg < 0 || maxdeg > 16 || (maxdeg > 0 && (!nbr || !cpl)) ||
+        (P > 32 && word_bits != 64))
+        return PQ_ERR_INVALID_ARG;
+    for (int c = 0; c < nclass; ++c)
+        if (class_start[c] < 0 || class_start[c + 1] < class_start[c]) return PQ_ERR_INVALID_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    for (int c = 0; c < nclass; ++c) {
+        const int first = class_start[c], count = class_start[c + 1] - class_start[c];
+        const int64_t M = (int64_t)R * count;
+        if (M == 0) continue;
+        PQ_WORD_DEG_DISPATCH(word_bits, maxdeg,
+                             (pair_uniform_kernel<W, D><<<blocks_for(M), 256, 0, st>>>(
+                                 (W*)words, n, P, R, maxdeg, nbr, cpl, field, bond_i, bond_j, bond_J, first, count, c,
+                                 beta, move, k0, k1, (uint32_t)replica_base, counters, status)));
+        const int rc = pq_launch_status();
         if (rc != PQ_OK) return rc;
     }
     return PQ_OK;

@@ -114,6 +114,12 @@ SIGNATURES = {
                                    _V, _V, _V, _V, _F32, _F32, _U32, _U64, _I32, _V, _V, _V]),
     "pq_worldline_pass": (_I32, [_V, _I32, _I32, _I32, _I32, _I32, _V, _V, _V, _I32, _I32, _V, _F32, _U32, _U64,
                                  _I32, _V, _V]),
+    "pq_pair_pass": (_I32, [_V, _I32, _I32, _I32, _I32, _I32, _V, _V, _V, _V, _V, _V, _V, _I32, _F32, _U32, _U64,
+                            _I32, _V, _V, _V]),
+    "pq_pair_features": (_I32, [_V, _I32, _I32, _I32, _I32, _I32, _V, _V, _V, _V, _V, _V, _I32, _I32, _F32, _F32,
+                                _V, _V, _I64, _V, _V]),
+    "pq_pair_propose": (_I32, [_V, _I32, _I32, _I32, _I32, _V, _V, _I32, _I32, _I32, _V, _V, _I64, _F32, _F32, _U32,
+                               _U64, _I32, _V, _V, _V]),
     "pq_mlp_head_backward": (_I32, [_V, _V, _V, _V, _I32, _V, _V, _V, _V, _V, _V]),
     "pq_mlp_hidden_backward": (_I32, [_V, _V, _I32, _V, _V, _V]),
     "pq_mlp_colsum_bf16": (_I32, [_V, _I32, _I32, _V, _V]),

@@ -1,4 +1,6 @@
 """Packed fast kernel: bit-exact against its CPU restatement, and the FP64 energy pass against FP64 NumPy."""
+import ctypes
+
 import numpy as np
 import pytest
 import torch
@@ -125,3 +127,31 @@ def test_classical_ising_energy_dropin():
     got = sa.ClassicalIsingEnergy(g["spins"].T, J)
     np.testing.assert_allclose(got, g["energies"], rtol=1e-13, atol=1e-12)
     assert sa.ClassicalIsingEnergy(g["spins"][0], J) == pytest.approx(g["energies"][0], rel=1e-13)
+
+
+@pytest.mark.parametrize("P", [1, 7, 20, 33, 64])
+@pytest.mark.parametrize("offset", [0, 1, 16])
+def test_pack_unpack_round_trip_any_alignment(P, offset):
+    """pq_pack_spins / pq_unpack_spins on buffers at any byte offset, with a partial last block."""
+    from piqmc import _device, _native
+    g = np.random.default_rng(P * 10 + offset)
+    R, n = 3, 301                                    # 903 items: not a multiple of the block size
+    spins = np.where(g.random((R, n, P)) < 0.5, -1, 1).astype(np.int8)
+    buf = torch.zeros(R * n * P + 32, dtype=torch.int8, device="cuda")
+    buf[offset:offset + R * n * P] = torch.from_numpy(spins.ravel()).cuda()
+    perm = torch.from_numpy(g.permutation(n).astype(np.int32)).cuda()
+    bits = 32 if P <= 32 else 64
+    words = torch.zeros((R, n), dtype=torch.int32 if bits == 32 else torch.int64, device="cuda")
+    lib = _native.lib()
+    base = buf.data_ptr()
+    _native.check(lib.pq_pack_spins(ctypes.c_void_p(base + offset), n, P, R, _device.ptr(perm), _device.ptr(words), bits,
+                                    n, _device.stream_handle()), "pack")
+    w = words.cpu().numpy().astype(np.uint64) & ((1 << bits) - 1) if bits == 32 else words.cpu().numpy().view(np.uint64)
+    expect = ((spins < 0).astype(np.uint64) << np.arange(P, dtype=np.uint64)).sum(axis=2, dtype=np.uint64)
+    np.testing.assert_array_equal(w[:, perm.cpu().numpy()], expect)
+    out = torch.full((R * n * P + 32,), 7, dtype=torch.int8, device="cuda")
+    _native.check(lib.pq_unpack_spins(_device.ptr(words), bits, n, P, R, _device.ptr(perm), n,
+                                      ctypes.c_void_p(out.data_ptr() + offset), _device.stream_handle()), "unpack")
+    o = out.cpu().numpy()
+    np.testing.assert_array_equal(o[offset:offset + R * n * P], spins.ravel())
+    assert (o[:offset] == 7).all() and (o[offset + R * n * P:] == 7).all()   # nothing written outside
