@@ -414,7 +414,12 @@ int pq_worldline_pass(void* words, int word_bits, int n, int P, int R, int maxde
  * pq_pair_propose: the learned move of those bonds from the network's logits of
  * both row sets: proposed with q = clamp(sigmoid(logit), qmin, 1), accepted with
  * min(1, exp(-beta dE) q'/q).  counters (nullable): [tried/proposed, accepted].
- * A slot outside [0, n) sets *status (nullable) to PQ_ERR_BAD_INDEX. */
+ * A slot outside [0, n) sets *status (nullable) to PQ_ERR_BAD_INDEX.
+ * pq_pair_learned_pass: the learned move of every class in order, fused (one
+ * persistent launch per class: features, both layers as tcgen05 MMAs with TMEM
+ * accumulators, head and decision on chip); the same moves as features + the
+ * network's GEMMs + pq_pair_propose.  Weights as for pq_mlp_learned_pass; a
+ * timed-out tensor-core wait sets *status to PQ_ERR_TIMEOUT. */
 int pq_pair_pass(void* words, int word_bits, int n, int P, int R, int maxdeg, const int32_t* nbr, const float* cpl,
                  const float* field, const int32_t* bond_i, const int32_t* bond_j, const float* bond_J,
                  const int32_t* class_start, int nclass, float beta, uint32_t move, uint64_t seed, int replica_base,
@@ -427,6 +432,12 @@ int pq_pair_propose(void* words, int word_bits, int n, int P, int R, const int32
                     int first, int count, int cls, const float* logit, const float* dE, int64_t Mpad, float qmin,
                     float beta, uint32_t move, uint64_t seed, int replica_base, unsigned long long* counters,
                     int32_t* status, void* stream);
+int pq_pair_learned_pass(void* words, int word_bits, int n, int P, int R, int maxdeg, const int32_t* nbr,
+                         const float* cpl, const float* field, const int32_t* bond_i, const int32_t* bond_j,
+                         const float* bond_J, const int32_t* class_start, int nclass, float beta, float jp,
+                         const void* W1, const void* W2, const float* b1, const float* b2, const float* w3, float b3,
+                         float qmin, uint32_t move, uint64_t seed, int replica_base, unsigned long long* counters,
+                         int32_t* status, void* stream);
 /* Training (BCE with soft targets y, mean over the batch B): head backward
  * (dH2 row-major and transposed, grads of w3, b3, loss), hidden backward
  * (mask by relu'(H1), transposed BF16 dH1, grad of b1), column sums, BF16

@@ -800,6 +800,219 @@ __global__ void __launch_bounds__(128) learned_move_kernel(W* __restrict__ words
     if (warp == 0) tc::tmem_dealloc(tmem, 2 * kLd);
 }
 
+// Fused learned pair move: the tile pipeline of learned_move_kernel with one
+// (replica, bond) row per thread -- features of the current and the flipped pair
+// (pair_features), both layers on the tensor cores, head, and the decision and
+// flips of pair_propose_kernel.  Rows t = r * count + b of bonds [first, first +
+// count) of class `cls`.  The inputs of the next tile are loaded while this
+// tile's moves land: the bonds of a class are independent, so no move of the
+// class changes them.
+struct PairMoveArgs {
+    int n, P, R, maxdeg, cls, first, count;
+    float beta, jp, qmin, b3;
+    uint32_t move, key0, key1, replica_base;
+    int64_t ntiles;
+};
+
+template <typename W, int MAXD>
+__global__ void __launch_bounds__(128) learned_pair_kernel(W* __restrict__ words, const int32_t* __restrict__ nbr,
+                                                          const float* __restrict__ cpl,
+                                                          const float* __restrict__ field,
+                                                          const int32_t* __restrict__ bi,
+                                                          const int32_t* __restrict__ bj,
+                                                          const float* __restrict__ bJ,
+                                                          const __nv_bfloat16* __restrict__ W1,
+                                                          const __nv_bfloat16* __restrict__ W2,
+                                                          const float* __restrict__ b1, const float* __restrict__ b2,
+                                                          const float* __restrict__ w3, PairMoveArgs a,
+                                                          unsigned long long* __restrict__ counters,
+                                                          int32_t* __restrict__ status) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    unsigned char* sX = smem + kOffX;
+    unsigned char* sXf = sX + kTile * kK1 * 2;
+    unsigned char* sH = smem + kOffH;
+    unsigned char* sHf = sH + kTile * kLd * 2;
+    unsigned char* sW1 = smem + kOffW1;
+    unsigned char* sW2 = smem + kOffW2;
+    float* sb1 = reinterpret_cast<float*>(smem + kOffB);
+    float* sb2 = sb1 + kLd;
+    float* sw3 = sb2 + kLd;
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + kOffBar);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + kOffBar + 8);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t M = (int64_t)a.R * a.count;
+
+    for (int c = tid; c < kLd * (kK1 / 8); c += 128) {
+        const int r = c / (kK1 / 8), kk = (c % (kK1 / 8)) * 8;
+        *reinterpret_cast<uint4*>(sW1 + tc::tile_off(r, kk, kK1)) =
+            *reinterpret_cast<const uint4*>(W1 + r * kLd + kk);
+    }
+    for (int c = tid; c < kLd * (kLd / 8); c += 128) {
+        const int r = c / (kLd / 8), kk = (c % (kLd / 8)) * 8;
+        *reinterpret_cast<uint4*>(sW2 + tc::tile_off(r, kk, kLd)) =
+            *reinterpret_cast<const uint4*>(W2 + r * kLd + kk);
+    }
+    for (int c = tid; c < 2 * kTile * kK1 * 2 / 16; c += 128) reinterpret_cast<uint4*>(sX)[c] = make_uint4(0, 0, 0, 0);
+    if (tid < kLd) { sb1[tid] = b1[tid]; sb2[tid] = b2[tid]; sw3[tid] = w3[tid]; }
+    if (tid == 0) {
+        tc::mbar_init(tc::smem_addr(mbar), 1);
+        tc::mbar_fence_init();
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(tc::smem_addr(tslot), 2 * kLd);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tslot;
+    const uint32_t tlane = tmem + ((uint32_t)(32 * warp) << 16);
+    constexpr uint32_t idesc = tc::idesc_bf16(kTile, kLd);
+    const W mask = slice_mask<W>(a.P);
+    uint32_t phase = 0;
+    bool ok = true, bad = false;
+
+    PairIn<W, MAXD> nxt;
+    bool nxt_ok = false;
+    auto prefetch = [&](int64_t tile) {
+        const int64_t t = tile * kTile + tid;
+        nxt_ok = false;
+        if (tile < a.ntiles && t < M) {
+            const int r = (int)(t / a.count);
+            const int b = a.first + (int)(t - (int64_t)r * a.count);
+            const int si = bi[b], sj = bj[b];
+            if ((unsigned)si < (unsigned)a.n && (unsigned)sj < (unsigned)a.n) {
+                load_pair<W, MAXD>(words + (int64_t)r * a.n, si, sj, bJ[b], a.n, a.maxdeg, nbr, cpl, field, nxt,
+                                   bad);
+                nxt_ok = true;
+            } else {
+                bad = true;
+            }
+        }
+    };
+    prefetch(blockIdx.x);
+    for (int64_t tile = blockIdx.x; tile < a.ntiles && ok; tile += gridDim.x) {
+        const int64_t t = tile * kTile + tid;
+        const bool valid = t < M && nxt_ok;
+        int r = 0, b = 0, si = 0, sj = 0;
+        float de = 0.0f;
+        {
+            float x[kFeat] = {0, 0, 0, 0, 0, 0, 0, 0}, xf[kFeat] = {0, 0, 0, 0, 0, 0, 0, 0};
+            if (valid) {
+                r = (int)(t / a.count);
+                b = a.first + (int)(t - (int64_t)r * a.count);
+                si = nxt.si;
+                sj = nxt.sj;
+                de = pair_features<W, MAXD>(nxt, a.P, a.maxdeg, a.beta, a.jp, x);
+                flip_pair<W, MAXD>(nxt, mask);
+                pair_features<W, MAXD>(nxt, a.P, a.maxdeg, a.beta, a.jp, xf);
+            }
+            uint32_t pc[4], pf[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                pc[e] = bf16x2_bits(x[2 * e], x[2 * e + 1]);
+                pf[e] = bf16x2_bits(xf[2 * e], xf[2 * e + 1]);
+            }
+            *reinterpret_cast<uint4*>(sX + tc::tile_off(tid, 0, kK1)) = make_uint4(pc[0], pc[1], pc[2], pc[3]);
+            *reinterpret_cast<uint4*>(sXf + tc::tile_off(tid, 0, kK1)) = make_uint4(pf[0], pf[1], pf[2], pf[3]);
+        }
+        tc::fence_async_shared();
+        tc::fence_before_sync();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after_sync();
+            const uint64_t bd = tc::smem_desc(tc::smem_addr(sW1), 128, kK1 * 16);
+            tc::mma_bf16(tmem, tc::smem_desc(tc::smem_addr(sX), 128, kK1 * 16), bd, idesc, 0u);
+            tc::mma_bf16(tmem + kLd, tc::smem_desc(tc::smem_addr(sXf), 128, kK1 * 16), bd, idesc, 0u);
+            tc::mma_commit(tc::smem_addr(mbar));
+        }
+        prefetch(tile + gridDim.x);
+        if (!tc::mbar_wait(tc::smem_addr(mbar), phase, kMmaWait)) { ok = false; break; }
+        phase ^= 1u;
+        tc::fence_after_sync();
+#pragma unroll 1
+        for (int half = 0; half < 2; ++half) {
+            uint32_t u0[32], u1[32];
+            tc::tmem_ld32_async(tlane + (uint32_t)(half * kLd), u0);
+            tc::tmem_ld32_async(tlane + (uint32_t)(half * kLd + 32), u1);
+            tc::tmem_wait_ld();
+            unsigned char* dst = half ? sHf : sH;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                uint32_t pk[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int j = 8 * q + 2 * e;
+                    const float v0 = __uint_as_float(j < 32 ? u0[j & 31] : u1[j & 31]);
+                    const float v1 = __uint_as_float(j + 1 < 32 ? u0[(j + 1) & 31] : u1[(j + 1) & 31]);
+                    pk[e] = bf16x2_bits(fmaxf(__fadd_rn(v0, sb1[j]), 0.0f), fmaxf(__fadd_rn(v1, sb1[j + 1]), 0.0f));
+                }
+                *reinterpret_cast<uint4*>(dst + tc::tile_off(tid, 8 * q, kLd)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            }
+        }
+        tc::fence_async_shared();
+        tc::fence_before_sync();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after_sync();
+#pragma unroll
+            for (int st = 0; st < kLd / 16; ++st) {
+                const uint64_t bd = tc::smem_desc(tc::smem_addr(sW2) + st * 256, 128, kLd * 16);
+                tc::mma_bf16(tmem, tc::smem_desc(tc::smem_addr(sH) + st * 256, 128, kLd * 16), bd, idesc,
+                             st > 0 ? 1u : 0u);
+                tc::mma_bf16(tmem + kLd, tc::smem_desc(tc::smem_addr(sHf) + st * 256, 128, kLd * 16), bd, idesc,
+                             st > 0 ? 1u : 0u);
+            }
+            tc::mma_commit(tc::smem_addr(mbar));
+        }
+        if (!tc::mbar_wait(tc::smem_addr(mbar), phase, kMmaWait)) { ok = false; break; }
+        phase ^= 1u;
+        tc::fence_after_sync();
+        float lg[2] = {a.b3, a.b3};
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            uint32_t u0[32], u1[32];
+            tc::tmem_ld32_async(tlane + (uint32_t)(half * kLd), u0);
+            tc::tmem_ld32_async(tlane + (uint32_t)(half * kLd + 32), u1);
+            tc::tmem_wait_ld();
+            float acc = a.b3;
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                acc = __fmaf_rn(fmaxf(__fadd_rn(__uint_as_float(u0[j]), sb2[j]), 0.0f), sw3[j], acc);
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                acc = __fmaf_rn(fmaxf(__fadd_rn(__uint_as_float(u1[j]), sb2[32 + j]), 0.0f), sw3[32 + j], acc);
+            lg[half] = acc;
+        }
+        bool proposed = false, accepted = false;
+        if (valid) {
+            const pq_u32x4 u = pq_philox(
+                pq_u32x4{(uint32_t)b, a.move, a.replica_base + (uint32_t)r, (5u << 24) | (uint32_t)a.cls}, a.key0,
+                a.key1);
+            const float q = fminf(fmaxf(pair_sigmoid(lg[0]), a.qmin), 1.0f);
+            const float qf = fminf(fmaxf(pair_sigmoid(lg[1]), a.qmin), 1.0f);
+            proposed = pq_u01(u.x) < q;
+            accepted = proposed && pair_accept(de, a.beta, q, qf, pq_u01(u.y));
+            if (accepted) pair_apply<W>(words + (int64_t)r * a.n, si, sj, a.P);
+        }
+        const unsigned bp = __ballot_sync(0xffffffffu, proposed), ba = __ballot_sync(0xffffffffu, accepted);
+        if (counters && lane == 0) {
+            if (bp) atomicAdd(counters, (unsigned long long)__popc(bp));
+            if (ba) atomicAdd(counters + 1, (unsigned long long)__popc(ba));
+        }
+        tc::fence_before_sync();
+    }
+    if (!ok) {
+        pq_set_status(status, PQ_ERR_TIMEOUT);
+        tc::mbar_wait(tc::smem_addr(mbar), phase, kMmaWait);
+    }
+    if (bad) pq_set_status(status, PQ_ERR_BAD_INDEX);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(tmem, 2 * kLd);
+}
+
 // Uniform world-line move of every spin of class `cls` (the plain form the
 // learned one is judged against): proposed always, accepted with
 // min(1, exp(-beta dE)), dE = 2 worldline_align; the same uniforms and the same
@@ -838,9 +1051,13 @@ __global__ void uniform_move_kernel(W* __restrict__ words, const int32_t* __rest
 // Persistent grid: SMs x resident CTAs per SM.  The runtime's occupancy query
 // reports one CTA per SM for this kernel (it cannot see the TMEM budget), so the
 // residency is computed from the kernel's own resources: shared memory, registers
-// and TMEM (4 x 128 columns per SM) -- four CTAs per SM.
-template <typename W, int MAXD>
-int move_grid(int64_t ntiles) {
+// and TMEM (4 x 128 columns per SM) -- four CTAs per SM.  One cache per kernel
+// instantiation (the Tag), per device.
+template <typename W, int MAXD, int KIND>
+struct GridTag {};
+
+template <typename Tag>
+int tile_grid(const void* kernel, int64_t ntiles) {
     // per device: (context identity, SMs, resident CTAs per SM)
     static std::mutex mu;
     static unsigned long long ctx[kPqMaxDevices];
@@ -851,7 +1068,6 @@ int move_grid(int64_t ntiles) {
     std::lock_guard<std::mutex> lock(mu);
     const unsigned long long id = pq_context_id();
     if (!id || ctx[dev] != id) {
-        auto kernel = learned_move_kernel<W, MAXD>;
         int nsm = 0, smem_sm = 0, regs_sm = 0, reserved = 0;
         PQ_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
         PQ_CUDA_TRY(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
@@ -874,6 +1090,16 @@ int move_grid(int64_t ntiles) {
     }
     const int64_t g = (int64_t)nsm_dev[dev] * occ_dev[dev];
     return (int)(ntiles < g ? ntiles : g);
+}
+
+template <typename W, int MAXD>
+int move_grid(int64_t ntiles) {
+    return tile_grid<GridTag<W, MAXD, 0>>((const void*)learned_move_kernel<W, MAXD>, ntiles);
+}
+
+template <typename W, int MAXD>
+int pair_grid(int64_t ntiles) {
+    return tile_grid<GridTag<W, MAXD, 1>>((const void*)learned_pair_kernel<W, MAXD>, ntiles);
 }
 
 inline unsigned blocks_for(int64_t n, int b = 256) { return (unsigned)((n + b - 1) / b); }
@@ -1089,6 +1315,42 @@ int pq_pair_pass(void* words, int word_bits, int n, int P, int R, int maxdeg, co
                              (pair_uniform_kernel<W, D><<<blocks_for(M), 256, 0, st>>>(
                                  (W*)words, n, P, R, maxdeg, nbr, cpl, field, bond_i, bond_j, bond_J, first, count, c,
                                  beta, move, k0, k1, (uint32_t)replica_base, counters, status)));
+        const int rc = pq_launch_status();
+        if (rc != PQ_OK) return rc;
+    }
+    return PQ_OK;
+}
+
+int pq_pair_learned_pass(void* words, int word_bits, int n, int P, int R, int maxdeg, const int32_t* nbr,
+                         const float* cpl, const float* field, const int32_t* bond_i, const int32_t* bond_j,
+                         const float* bond_J, const int32_t* class_start, int nclass, float beta, float jp,
+                         const void* W1, const void* W2, const float* b1, const float* b2, const float* w3, float b3,
+                         float qmin, uint32_t move, uint64_t seed, int replica_base, unsigned long long* counters,
+                         int32_t* status, void* stream) {
+    if (!words || !field || !bond_i || !bond_j || !bond_J || !class_start || nclass < 0 || !W1 || !W2 || !b1 ||
+        !b2 || !w3 || n <= 0 || P < 1 || P > 64 || R <= 0 || maxdeg < 0 || maxdeg > 16 ||
+        (maxdeg > 0 && (!nbr || !cpl)) || !(qmin > 0.0f) || qmin > 1.0f || (P > 32 && word_bits != 64))
+        return PQ_ERR_INVALID_ARG;
+    for (int c = 0; c < nclass; ++c)
+        if (class_start[c] < 0 || class_start[c + 1] < class_start[c]) return PQ_ERR_INVALID_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    for (int c = 0; c < nclass; ++c) {
+        PairMoveArgs a;
+        a.n = n; a.P = P; a.R = R; a.maxdeg = maxdeg; a.cls = c; a.first = class_start[c];
+        a.count = class_start[c + 1] - class_start[c];
+        a.beta = beta; a.jp = jp; a.qmin = qmin; a.b3 = b3;
+        a.move = move; a.key0 = (uint32_t)seed; a.key1 = (uint32_t)(seed >> 32); a.replica_base = (uint32_t)replica_base;
+        const int64_t M = (int64_t)R * a.count;
+        if (M == 0) continue;
+        a.ntiles = (M + kTile - 1) / kTile;
+        PQ_WORD_DEG_DISPATCH(word_bits, maxdeg, {
+            const int grid = pair_grid<W, D>(a.ntiles);
+            if (grid <= 0) return grid;
+            learned_pair_kernel<W, D><<<grid, 128, kSmemMove, st>>>((W*)words, nbr, cpl, field, bond_i, bond_j,
+                                                                    bond_J, (const __nv_bfloat16*)W1,
+                                                                    (const __nv_bfloat16*)W2, b1, b2, w3, a, counters,
+                                                                    status);
+        });
         const int rc = pq_launch_status();
         if (rc != PQ_OK) return rc;
     }

@@ -120,6 +120,8 @@ SIGNATURES = {
                                 _V, _V, _I64, _V, _V]),
     "pq_pair_propose": (_I32, [_V, _I32, _I32, _I32, _I32, _V, _V, _I32, _I32, _I32, _V, _V, _I64, _F32, _F32, _U32,
                                _U64, _I32, _V, _V, _V]),
+    "pq_pair_learned_pass": (_I32, [_V, _I32, _I32, _I32, _I32, _I32, _V, _V, _V, _V, _V, _V, _V, _I32, _F32, _F32,
+                                    _V, _V, _V, _V, _V, _F32, _F32, _U32, _U64, _I32, _V, _V, _V]),
     "pq_mlp_head_backward": (_I32, [_V, _V, _V, _V, _I32, _V, _V, _V, _V, _V, _V]),
     "pq_mlp_hidden_backward": (_I32, [_V, _V, _I32, _V, _V, _V]),
     "pq_mlp_colsum_bf16": (_I32, [_V, _I32, _I32, _V, _V]),

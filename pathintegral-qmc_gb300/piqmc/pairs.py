@@ -166,13 +166,29 @@ def pair_features(problem, words, P, beta, jp, cls, status=None):
 
 
 def learned_pair_pass(problem, words, P, mlp, beta, jp, seed, move, qmin=QMIN, counters=None, replica_base=0,
-                      status=None, check=True):
-    """One learned pair move per bond, class by class: the network chooses which bonds to try."""
+                      status=None, check=True, fused=True):
+    """One learned pair move per bond, class by class: the network chooses which bonds to try.
+
+    ``fused`` runs each class in one launch (features, network on the tensor cores,
+    decision); otherwise the feature kernel, the network's GEMMs and the propose
+    kernel run one after another -- the same moves."""
     bc = bond_classes(problem)
     R = words.shape[0]
     bits = 32 if P <= 32 else 64
     st = _status(status, words.device)
     lib = _native.lib()
+    if fused:
+        _native.check(lib.pq_pair_learned_pass(
+            _device.ptr(words), bits, problem.nslots, int(P), R, problem.maxdeg, _device.ptr(problem.nbr),
+            _device.ptr(problem.cpl), _device.ptr(problem.field), _device.ptr(bc.d_i), _device.ptr(bc.d_j),
+            _device.ptr(bc.d_J), _device.ptr(bc.class_start), bc.nclass, float(beta), float(jp), _device.ptr(mlp.W1b),
+            _device.ptr(mlp.W2b), _device.ptr(mlp.params["b1"]), _device.ptr(mlp.params["b2"]),
+            _device.ptr(mlp.params["w3"]), mlp.b3_host, float(qmin), int(move) & 0xFFFFFFFF,
+            int(seed) & 0xFFFFFFFFFFFFFFFF, int(replica_base), _device.ptr(counters), _device.ptr(st),
+            _device.stream_handle()), "pq_pair_learned_pass")
+        if check:
+            _raise(st, "learned pair pass")
+        return
     for cls in range(bc.nclass):
         X, dE, M, Mpad = pair_features(problem, words, P, beta, jp, cls, status=st)
         if M == 0:

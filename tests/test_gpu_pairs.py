@@ -149,3 +149,25 @@ def test_pair_passes_lower_the_final_energy():
         out.append(prob.energies(w, P).cpu().numpy().min(axis=1).mean() / 256)
     print("mean best-slice energy per spin: plain %.4f, with pair moves %.4f" % tuple(out))
     assert out[1] < out[0] - 0.02
+
+
+@pytest.mark.parametrize("P", [20, 64])
+def test_fused_learned_pair_pass_equals_unfused(P):
+    """One launch per class (features, tcgen05 layers in TMEM, head, decision) makes the unfused path's moves."""
+    from piqmc import learned, pairs
+    g = np.random.default_rng(40 + P)
+    J, prob = _problem("lattice", g)
+    R = 5
+    spins = np.where(g.random((R, prob.n, P)) < 0.5, -1, 1).astype(np.int8)
+    words = prob.pack(torch.from_numpy(spins))
+    mlp = learned.ProposalMLP(seed=8)
+    out = []
+    for fused in (True, False):
+        w = words.clone()
+        cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
+        for move in range(3):
+            pairs.learned_pair_pass(prob, w, P, mlp, 2.5, 0.4, seed=6, move=move, counters=cnt, fused=fused)
+        out.append((w, cnt.cpu().numpy()))
+    assert torch.equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    assert out[0][1][1] > 0
