@@ -21,7 +21,7 @@ struct FastArgs {
     PhiloxKeyTable keys;  // round keys of (key0, key1), read as constant operands
 };
 
-template <typename W, int MAXDEG, int NQC>
+template <typename W, int MAXDEG, int NQC, bool STAGED>
 __global__ void __launch_bounds__(512) qa_fast_kernel(W* __restrict__ words, const int32_t* __restrict__ nbr,
                                                       const float* __restrict__ cpl,
                                                       const float* __restrict__ field,
@@ -56,7 +56,8 @@ __global__ void __launch_bounds__(512) qa_fast_kernel(W* __restrict__ words, con
     bool bad = false;
     unsigned long long nacc = 0;
     stage_in<W>(it, sw, g);   // also publishes csize
-    run_item<W, MAXDEG, NQC>(it, a.keys, sw, order, parity, SiteQueue{queue_slots, queue_count}, g, bad, nacc);
+    run_item<W, MAXDEG, NQC, STAGED>(it, a.keys, sw, order, parity, SiteQueue{queue_slots, queue_count}, g, bad,
+                                     nacc);
     stage_out<W>(it, sw, g);
     if (bad) pq_set_status(status, PQ_ERR_BAD_INDEX);
     if (accepts) {
@@ -92,37 +93,24 @@ __global__ void energy_packed_kernel(const W* __restrict__ words, int n, int P, 
 
 // Configuration streaming between the int8 layout [R][n][P] and packed words.
 // A block of kStreamThreads threads owns kStreamThreads consecutive (replica, spin)
-// items t = r n + i, whose spins are one contiguous run of kStreamThreads * P bytes;
-// the run moves between global and shared memory as 16-byte vectors when its start
-// is 16-byte aligned (byte by byte otherwise), and each thread packs or unpacks its
-// own P bytes in shared memory.
+// items t = r n + i, whose spins are one contiguous run of kStreamThreads * P bytes.
+// Unpacking writes each thread's P bytes into shared memory and stores the run as
+// 16-byte vectors when its start is 16-byte aligned (byte by byte otherwise).
 constexpr int kStreamThreads = 256;
 
 __device__ __forceinline__ bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 
+// Packing reads each item's P spins directly: a warp's loads of one slice index
+// touch neighbouring sectors that the next indices reuse from L1 (measured faster
+// than staging the run for this direction).
 template <typename W>
 __global__ void __launch_bounds__(kStreamThreads) pack_kernel(const int8_t* __restrict__ spins, int n, int P, int R,
                                                             const int32_t* __restrict__ perm, W* __restrict__ words,
                                                             int stride) {
-    extern __shared__ __align__(16) int8_t run[];
-    const int64_t total = (int64_t)R * n;
-    const int64_t t0 = (int64_t)blockIdx.x * kStreamThreads;
-    const int items = (int)min((int64_t)kStreamThreads, total - t0);
-    const int nbytes = items * P;
-    const int8_t* src = spins + t0 * P;
-    if (aligned16(src)) {
-        const int nvec = nbytes >> 4;
-        for (int v = threadIdx.x; v < nvec; v += kStreamThreads)
-            reinterpret_cast<int4*>(run)[v] = __ldg(reinterpret_cast<const int4*>(src) + v);
-        for (int b = (nvec << 4) + threadIdx.x; b < nbytes; b += kStreamThreads) run[b] = src[b];
-    } else {
-        for (int b = threadIdx.x; b < nbytes; b += kStreamThreads) run[b] = src[b];
-    }
-    __syncthreads();
-    if ((int)threadIdx.x >= items) return;
-    const int64_t t = t0 + threadIdx.x;
+    const int64_t t = (int64_t)blockIdx.x * kStreamThreads + threadIdx.x;
+    if (t >= (int64_t)R * n) return;
     const int r = (int)(t / n), i = (int)(t % n);
-    const int8_t* s = run + threadIdx.x * P;
+    const int8_t* s = spins + t * P;
     W w = 0;
     for (int k = 0; k < P; ++k) w |= (W)(s[k] < 0) << k;
     const int di = perm ? perm[i] : i;
@@ -158,18 +146,32 @@ __global__ void __launch_bounds__(kStreamThreads) unpack_kernel(const W* __restr
     }
 }
 
+template <typename W, int MAXDEG, int NQC, bool STAGED>
+int launch_fast_t(void* words, const int32_t* nbr, const float* cpl, const float* field, const float* jperp,
+                  const float* betas, const FastArgs& a, int threads, unsigned long long* accepts, int32_t* status,
+                  cudaStream_t stream) {
+    const size_t smem = item_smem_bytes(a.rpc, a.n, a.P);
+    static PqSmemAttr attr;
+    const int rc = pq_set_smem_limit(attr, (const void*)qa_fast_kernel<W, MAXDEG, NQC, STAGED>, 220 * 1024);
+    if (rc != PQ_OK) return rc;
+    const int grid = (a.R + a.rpc - 1) / a.rpc;
+    qa_fast_kernel<W, MAXDEG, NQC, STAGED><<<grid, threads, smem, stream>>>((W*)words, nbr, cpl, field, jperp, betas,
+                                                                           a, accepts, status);
+    return pq_launch_status();
+}
+
+// Compile-time P: staged phases when a thread walks at least two sites per phase (staged_phase).
 template <typename W, int MAXDEG, int NQC>
 int launch_fast(void* words, const int32_t* nbr, const float* cpl, const float* field, const float* jperp,
                 const float* betas, const FastArgs& a, int threads, unsigned long long* accepts,
                 int32_t* status, cudaStream_t stream) {
-    const size_t smem = item_smem_bytes(a.rpc, a.n, a.P);
-    static PqSmemAttr attr;
-    const int rc = pq_set_smem_limit(attr, (const void*)qa_fast_kernel<W, MAXDEG, NQC>, 220 * 1024);
-    if (rc != PQ_OK) return rc;
-    const int grid = (a.R + a.rpc - 1) / a.rpc;
-    qa_fast_kernel<W, MAXDEG, NQC><<<grid, threads, smem, stream>>>((W*)words, nbr, cpl, field, jperp, betas, a,
-                                                                    accepts, status);
-    return pq_launch_status();
+    if constexpr (NQC > 0) {
+        if (staged_phase(NQC, a.rpc, a.stride, threads))
+            return launch_fast_t<W, MAXDEG, NQC, true>(words, nbr, cpl, field, jperp, betas, a, threads, accepts,
+                                                       status, stream);
+    }
+    return launch_fast_t<W, MAXDEG, NQC, false>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status,
+                                                stream);
 }
 
 template <typename W>
@@ -283,12 +285,11 @@ int pq_pack_spins(const int8_t* spins, int n, int P, int R, const int32_t* perm,
     if (R == 0) return PQ_OK;
     const int64_t tot = (int64_t)R * n;
     const unsigned blocks = (unsigned)((tot + kStreamThreads - 1) / kStreamThreads);
-    const size_t smem = (size_t)kStreamThreads * P;   // at most 16 KB (P <= 64)
     cudaStream_t st = (cudaStream_t)stream;
     if (word_bits == 32)
-        pack_kernel<uint32_t><<<blocks, kStreamThreads, smem, st>>>(spins, n, P, R, perm, (uint32_t*)words, word_stride);
+        pack_kernel<uint32_t><<<blocks, kStreamThreads, 0, st>>>(spins, n, P, R, perm, (uint32_t*)words, word_stride);
     else
-        pack_kernel<uint64_t><<<blocks, kStreamThreads, smem, st>>>(spins, n, P, R, perm, (uint64_t*)words, word_stride);
+        pack_kernel<uint64_t><<<blocks, kStreamThreads, 0, st>>>(spins, n, P, R, perm, (uint64_t*)words, word_stride);
     return pq_launch_status();
 }
 
@@ -299,7 +300,7 @@ int pq_unpack_spins(const void* words, int word_bits, int n, int P, int R, const
     if (R == 0) return PQ_OK;
     const int64_t tot = (int64_t)R * n;
     const unsigned blocks = (unsigned)((tot + kStreamThreads - 1) / kStreamThreads);
-    const size_t smem = (size_t)kStreamThreads * P;
+    const size_t smem = (size_t)kStreamThreads * P;   // at most 16 KB (P <= 64)
     cudaStream_t st = (cudaStream_t)stream;
     if (word_bits == 32)
         unpack_kernel<uint32_t><<<blocks, kStreamThreads, smem, st>>>((const uint32_t*)words, n, P, R, perm,

@@ -255,7 +255,7 @@ struct ClassMasks {
         return m;
     }
     static constexpr W CM0 = class0();
-    static constexpr W IN0 = CM0 & ~((W)1 << (2 * NQ - 2));
+    static constexpr W IN0 = NQ > 0 ? (W)(CM0 & ~((W)1 << (NQ > 0 ? 2 * NQ - 2 : 0))) : (W)0;
     static constexpr W MASK = 2 * NQ >= (int)(8 * sizeof(W)) ? ~(W)0 : (((W)1 << (2 * NQ)) - 1);
 };
 
@@ -271,6 +271,9 @@ struct ClassMasks {
 template <typename W, int MAXDEG, int NQC, bool SPLIT>
 __device__ __forceinline__ int site_settle(const Item& it, W* rw, int i, uint32_t first, float jp, float m2beta,
                                            int half, bool& bad, unsigned long long& nacc) {
+  if constexpr (NQC == 0) {
+    return 0;   // run-time P: never staged
+  } else {
     using CMk = ClassMasks<W, NQC>;
     constexpr int P = 2 * NQC;
     W wi = rw[i];
@@ -306,6 +309,7 @@ __device__ __forceinline__ int site_settle(const Item& it, W* rw, int i, uint32_
     }
     if (wi != w0 && (!SPLIT || half == 0)) rw[i] = wi;
     return qq;
+  }
 }
 
 // The per-slice local update of one site from slice class qq0 on (all classes when
@@ -391,28 +395,36 @@ struct SiteQueue {
 // SPLIT (64-bit words with P = 64 only): two adjacent lanes share each site, one
 // 32-bit half of the world-line each, and exchange their flips after every slice
 // class; the sweep's serial work per lane halves, its result is unchanged.
-template <typename W, int MAXDEG, int NQC, bool INLINE, typename KS, bool SPLIT = false>
+template <typename W, int MAXDEG, int NQC, bool INLINE, typename KS, bool SPLIT = false, bool STAGED = true>
 __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* sw, uint8_t* order, uint32_t* parity,
                                               const SiteQueue& q, const Group& g, bool& bad,
                                               unsigned long long& nacc);
 
+// The staged phase pays when a lane walks at least two sites per phase (stage B
+// then runs on fewer, fuller warps than the sites' own lanes); with fewer, every
+// lane updates its own site slice by slice.  Compile-time P only.
+__host__ __device__ inline bool staged_phase(int nqc, int nrep, int stride, int site_threads) {
+    return nqc > 0 && (int64_t)nrep * stride >= 2 * (int64_t)site_threads;
+}
+
 // The single-instance kernel inlines the item loop; the batched kernel calls one
 // out-of-line copy per variant, so each variant keeps its own register budget.
-template <typename W, int MAXDEG, int NQC>
+template <typename W, int MAXDEG, int NQC, bool STAGED>
 __device__ __forceinline__ void run_item(const Item& it, const PhiloxKeyTable& keys, W* sw, uint8_t* order,
                                          uint32_t* parity, const SiteQueue& q, const Group& g, bool& bad,
                                          unsigned long long& nacc) {
-    run_item_body<W, MAXDEG, NQC, true, PhiloxKeysTab>(it, PhiloxKeysTab{keys}, sw, order, parity, q, g, bad, nacc);
+    run_item_body<W, MAXDEG, NQC, true, PhiloxKeysTab, false, STAGED>(it, PhiloxKeysTab{keys}, sw, order, parity, q,
+                                                                      g, bad, nacc);
 }
 
-template <typename W, int MAXDEG, int NQC, bool SPLIT = false>
+template <typename W, int MAXDEG, int NQC, bool SPLIT = false, bool STAGED = true>
 __device__ __noinline__ void run_item_call(const Item& it, W* sw, uint8_t* order, uint32_t* parity,
                                            const SiteQueue& q, const Group& g, bool& bad, unsigned long long& nacc) {
-    run_item_body<W, MAXDEG, NQC, false, PhiloxKeysReg, SPLIT>(it, PhiloxKeysReg{it.key0, it.key1}, sw, order,
-                                                               parity, q, g, bad, nacc);
+    run_item_body<W, MAXDEG, NQC, false, PhiloxKeysReg, SPLIT, STAGED>(it, PhiloxKeysReg{it.key0, it.key1}, sw,
+                                                                       order, parity, q, g, bad, nacc);
 }
 
-template <typename W, int MAXDEG, int NQC, bool INLINE, typename KS, bool SPLIT>
+template <typename W, int MAXDEG, int NQC, bool INLINE, typename KS, bool SPLIT, bool STAGED>
 __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* sw, uint8_t* order, uint32_t* parity,
                                               const SiteQueue& q, const Group& g, bool& bad,
                                               unsigned long long& nacc) {
@@ -457,7 +469,7 @@ __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* s
                     cls = order[rl * kMaxClasses + p];
                     cs = it.csize[cls];
                 }
-                if constexpr (NQC > 0) {
+                if constexpr (NQC > 0 && STAGED) {
                     int* cnt = q.count + (phase & 1u);
                     // stage A: settle, queue the rest
                     for (;;) {
@@ -588,6 +600,17 @@ __device__ __forceinline__ void stage_out(const Item& it, const W* sw, const Gro
     for (int t = g.tid; t < it.nrep * it.n; t += g.nthr) dst[t] = sw[t];
 }
 
+// One item's compile-time variant, staged or per-site phases (staged_phase).
+template <typename W, int MAXDEG, int NQC, bool SPLIT = false>
+__device__ __forceinline__ void run_item_pick(const Item& it, W* sw, uint8_t* order, uint32_t* parity,
+                                              const SiteQueue& q, const Group& g, bool& bad,
+                                              unsigned long long& nacc) {
+    if (staged_phase(NQC, it.nrep, it.stride, SPLIT ? g.nthr / 2 : g.nthr))
+        run_item_call<W, MAXDEG, NQC, SPLIT, true>(it, sw, order, parity, q, g, bad, nacc);
+    else
+        run_item_call<W, MAXDEG, NQC, SPLIT, false>(it, sw, order, parity, q, g, bad, nacc);
+}
+
 // Word type / degree / compile-time P dispatch of one item.
 __device__ inline void run_item_any(const Item& it, unsigned char* smem, const SiteQueue& q, const Group& g, bool& bad,
                                     unsigned long long& nacc, int lanes_per_site = 1) {
@@ -599,9 +622,9 @@ __device__ inline void run_item_any(const Item& it, unsigned char* smem, const S
     if (it.P <= 32) {
         uint32_t* sw = reinterpret_cast<uint32_t*>(smem);
         stage_in<uint32_t>(it, sw, g);
-        if (it.maxdeg == 4 && it.P == 20) run_item_call<uint32_t, 4, 10>(it, sw, order, parity, q, g, bad, nacc);
-        else if (it.maxdeg == 4 && it.P == 16) run_item_call<uint32_t, 4, 8>(it, sw, order, parity, q, g, bad, nacc);
-        else if (it.maxdeg == 4 && it.P == 32) run_item_call<uint32_t, 4, 16>(it, sw, order, parity, q, g, bad, nacc);
+        if (it.maxdeg == 4 && it.P == 20) run_item_pick<uint32_t, 4, 10>(it, sw, order, parity, q, g, bad, nacc);
+        else if (it.maxdeg == 4 && it.P == 16) run_item_pick<uint32_t, 4, 8>(it, sw, order, parity, q, g, bad, nacc);
+        else if (it.maxdeg == 4 && it.P == 32) run_item_pick<uint32_t, 4, 16>(it, sw, order, parity, q, g, bad, nacc);
         else if (it.maxdeg <= 4) run_item_call<uint32_t, 4, 0>(it, sw, order, parity, q, g, bad, nacc);
         else run_item_call<uint32_t, 8, 0>(it, sw, order, parity, q, g, bad, nacc);
         stage_out<uint32_t>(it, sw, g);
@@ -609,8 +632,8 @@ __device__ inline void run_item_any(const Item& it, unsigned char* smem, const S
         uint64_t* sw = reinterpret_cast<uint64_t*>(smem);
         stage_in<uint64_t>(it, sw, g);
         if (it.maxdeg == 4 && it.P == 64 && lanes_per_site == 2)
-            run_item_call<uint64_t, 4, 32, true>(it, sw, order, parity, q, g, bad, nacc);
-        else if (it.maxdeg == 4 && it.P == 64) run_item_call<uint64_t, 4, 32>(it, sw, order, parity, q, g, bad, nacc);
+            run_item_pick<uint64_t, 4, 32, true>(it, sw, order, parity, q, g, bad, nacc);
+        else if (it.maxdeg == 4 && it.P == 64) run_item_pick<uint64_t, 4, 32>(it, sw, order, parity, q, g, bad, nacc);
         else if (it.maxdeg <= 4) run_item_call<uint64_t, 4, 0>(it, sw, order, parity, q, g, bad, nacc);
         else run_item_call<uint64_t, 8, 0>(it, sw, order, parity, q, g, bad, nacc);
         stage_out<uint64_t>(it, sw, g);
