@@ -343,13 +343,14 @@ def gpu_arm(args):
         e2e_s = max_over_ranks(e2e_s, dist, "cuda")
     e2e_value = whole_job_rate(updates, len(e2e_ms), world, e2e_s)
 
-    batched = densew = learnedw = reforderw = dropinw = None
+    batched = densew = learnedw = reforderw = dropinw = genw = None
     if not args.no_batched and rank == 0:
         batched = batched_workload(args, torch)
         densew = dense_workload(args, torch)
         learnedw = learned_vs_plain(args, torch, prob, R=args.learned_replicas)
         reforderw = reforder_workload(args, torch)
         dropinw = dropin_workload(args, torch)
+        genw = generators_workload(args, torch)
 
     peak = measured_fp32_peak(torch)
     achieved_tflops = value / world * FLOP_PER_UPDATE / 1e12
@@ -398,7 +399,7 @@ def gpu_arm(args):
     }
     if cpu_base is not None:
         line["cpu_baseline"] = cpu_base
-    extras = compact_extras(batched, densew, learnedw, reforderw, dropinw)
+    extras = compact_extras(batched, densew, learnedw, reforderw, dropinw, genw)
     if extras:
         # the compact figures go right after the config, the detailed objects at the end of the line
         keys = list(line)
@@ -406,6 +407,8 @@ def gpu_arm(args):
         line = {k: line[k] for k in keys[:at]} | {"extras": extras} | {k: line[k] for k in keys[at:]}
     if dropinw is not None:
         line["dropin"] = dropinw
+    if genw is not None:
+        line["generators"] = genw
     if batched is not None:
         line["batched_uneven"] = batched
     if densew is not None:
@@ -420,7 +423,7 @@ def gpu_arm(args):
         dist.destroy_process_group()
 
 
-def compact_extras(batched, densew, learnedw, reforderw, dropinw):
+def compact_extras(batched, densew, learnedw, reforderw, dropinw, genw=None):
     """Headline figure of every extra workload, in a few keys (the detailed objects follow at the end)."""
     ex = {}
     if batched is not None:
@@ -439,6 +442,8 @@ def compact_extras(batched, densew, learnedw, reforderw, dropinw):
     if dropinw is not None:
         ex["dropin_speedup_vs_one_core"] = {r["call"].split(" ")[0]: r.get("speedup_vs_one_core")
                                             for r in dropinw["calls"]}
+    if genw is not None:
+        ex["generator_gpu_ms"] = {r["instance"]: r["gpu_ms"] for r in genw["instances"]}
     return ex
 
 
@@ -945,6 +950,36 @@ def dropin_workload(args, torch):
     return out
 
 
+def generators_workload(args, torch):
+    """Instance generation: the GPU table generator against the host drop-in generator + GenerateNeighbors."""
+    from piqmc import tools
+    out = {"note": "GPU: tools.lattice_table (neighbour table written in device memory, CUDA events); host: the "
+                   "drop-in generator (the caller's MT19937 values, as the reference) + GenerateNeighbors, wall time"}
+    cases = [("ising2d 80x80 torus", "ising2d", 80, 80, 1, lambda: tools.Generate2DIsingInstance(
+                 80, np.random.RandomState(0)), 4),
+             ("kblock 64x64 k=2", "kblock", 64, 64, 2, lambda: tools.GenerateKblockLattice(
+                 64, 64, np.random.RandomState(0), k=2), 24)]
+    rows = []
+    for name, kind, r, c, k, host, maxnb in cases:
+        tools.lattice_table(kind, r, c, seed=1, k=k, maxnb=maxnb)            # warm-up
+        ms = []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            tools.lattice_table(kind, r, c, seed=1, k=k, maxnb=maxnb, check=False)
+            e1.record()
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        t0 = time.perf_counter()
+        J = host()
+        tools.GenerateNeighbors(r * c, J, maxnb)
+        host_ms = (time.perf_counter() - t0) * 1e3
+        rows.append({"instance": name, "gpu_ms": min(ms), "host_ms": host_ms, "speedup": host_ms / min(ms)})
+    out["instances"] = rows
+    return out
+
+
 def only_arm(args):
     """One extra workload on its own (profiling entry point)."""
     import torch
@@ -960,6 +995,8 @@ def only_arm(args):
         out = gemm_workload(args, torch)
     elif args.only == "dropin":
         out = dropin_workload(args, torch)
+    elif args.only == "generators":
+        out = generators_workload(args, torch)
     else:
         from piqmc import fast, tools
         import scipy.sparse as sps
@@ -1003,7 +1040,7 @@ def main():
     ap.add_argument("--rpc", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched, dense and learned extras")
-    ap.add_argument("--only", choices=["batched", "dense", "learned", "reforder", "gemm", "dropin"], default=None,
+    ap.add_argument("--only", choices=["batched", "dense", "learned", "reforder", "gemm", "dropin", "generators"], default=None,
                     help="run one extra workload alone (for profiling) and print its JSON")
     ap.add_argument("--batched-count", type=int, default=256)
     ap.add_argument("--batched-steps", type=int, default=500)

@@ -306,6 +306,24 @@ int pq_batch_smem_bytes(int nrep, int n, int P);
 int pq_batch_occupancy(int threads, int smem_bytes, int* blocks_per_sm, int* sm_count);
 
 /* ---------------------------------------------------------------------------
+ * Instance generators on the GPU (the bond sets of Generate2DIsingInstance,
+ * Generate2DLattice and GenerateKblockLattice, reference
+ * piqmc/tools.pyx:98-131, :133-175, :177-273).  Writes the neighbour table of
+ * tools.GenerateNeighbors (float64 [n][maxnb][2], rows in the reference's key
+ * order, zero padding) to device memory and row_len[n] (device int32) the
+ * entries of each row.  kind 0: nrows x nrows torus (ncols = nrows); kind 1:
+ * nrows x ncols lattice, periodic or not; kind 2: K-block lattice, 1 <= k <= 3.
+ * Coupling (a, b) = lo + (hi - lo) u with u the 53-bit uniform of
+ * Philox4x32-10(ctr = {a, b, 0, 6 << 24}, key = seed) -- not the caller's
+ * MT19937 stream, so the values differ from the host drop-ins' while the table's
+ * structure is the same.  A row longer than maxnb sets *status to
+ * PQ_ERR_TOO_LARGE (the reference's IndexError).
+ * ------------------------------------------------------------------------- */
+int pq_generate_lattice_table(int kind, int nrows, int ncols, int periodic, int k, double lo, double hi,
+                              uint64_t seed, int maxnb, double* nbs, int32_t* row_len, int32_t* status,
+                              void* stream);
+
+/* ---------------------------------------------------------------------------
  * Tensor-core GEMM (new): D[M][N] = alpha * A[M][K] B[N][K]^T (+ bias[n]),
  * BF16 row-major operands (K contiguous, leading dimensions lda/ldb elements,
  * multiples of 8, 16-byte aligned), FP32 D (ldd floats), FP32 accumulation in

@@ -122,6 +122,8 @@ SIGNATURES = {
                                _U64, _I32, _V, _V, _V]),
     "pq_pair_learned_pass": (_I32, [_V, _I32, _I32, _I32, _I32, _I32, _V, _V, _V, _V, _V, _V, _V, _I32, _F32, _F32,
                                     _V, _V, _V, _V, _V, _F32, _F32, _U32, _U64, _I32, _V, _V, _V]),
+    "pq_generate_lattice_table": (_I32, [_I32, _I32, _I32, _I32, _I32, ctypes.c_double, ctypes.c_double, _U64,
+                                         _I32, _V, _V, _V, _V]),
     "pq_mlp_head_backward": (_I32, [_V, _V, _V, _V, _I32, _V, _V, _V, _V, _V, _V]),
     "pq_mlp_hidden_backward": (_I32, [_V, _V, _I32, _V, _V, _V]),
     "pq_mlp_colsum_bf16": (_I32, [_V, _I32, _I32, _V, _V]),

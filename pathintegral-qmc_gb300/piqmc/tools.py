@@ -190,6 +190,68 @@ def GenerateKblockLattice(nrows, ncols, rng, k=1):
 
 
 # ------------------------------------------------------------------------------------------
+# the same instances generated on the GPU (neighbour table in device memory)
+# ------------------------------------------------------------------------------------------
+
+def lattice_table(kind, nrows, ncols=None, seed=0, periodic=0, k=1, maxnb=None, lo=None, hi=None, check=True):
+    """Neighbour table (GenerateNeighbors layout, float64 (n, maxnb, 2)) of a generated instance, on the GPU.
+
+    kind "ising2d" (Generate2DIsingInstance, nrows x nrows torus, U[-2, 2]), "lattice2d"
+    (Generate2DLattice, U[-1e-8, 1e-8]) or "kblock" (GenerateKblockLattice, U[-1e-8, 1e-8]).
+    The bonds and the order of every row are those GenerateNeighbors builds from the
+    host generators; the values come from a seeded counter-based stream (not the
+    caller's ``rng``), so use the host functions when the reference's values matter.
+    Returns the device tensor.
+    """
+    import torch
+    from . import _device
+    kinds = {"ising2d": 0, "lattice2d": 1, "kblock": 2}
+    if kind not in kinds:
+        raise ValueError("kind must be one of %s" % sorted(kinds))
+    kd = kinds[kind]
+    nrows = int(nrows)
+    ncols = nrows if ncols is None else int(ncols)
+    if kd == 0 and ncols != nrows:
+        raise ValueError("ising2d is square: ncols must equal nrows")
+    if maxnb is None:
+        maxnb = (2 * int(k) + 1) ** 2 - 1 if kd == 2 else 4
+    default = (-2.0, 2.0) if kd == 0 else (-1e-8, 1e-8)
+    lo = default[0] if lo is None else float(lo)
+    hi = default[1] if hi is None else float(hi)
+    n = nrows * ncols
+    dev = _device.device()
+    nbs = torch.empty((n, int(maxnb), 2), dtype=torch.float64, device=dev)
+    row_len = torch.empty(n, dtype=torch.int32, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    _native.check(_native.lib().pq_generate_lattice_table(
+        kd, nrows, ncols, int(bool(periodic)), int(k), lo, hi, int(seed) & 0xFFFFFFFFFFFFFFFF, int(maxnb),
+        _device.ptr(nbs), _device.ptr(row_len), _device.ptr(status), _device.stream_handle()),
+        "pq_generate_lattice_table")
+    if check:
+        code = int(status.item())
+        if code == _native.PQ_ERR_TOO_LARGE:
+            raise IndexError("a spin has more than maxnb=%d neighbours" % int(maxnb))
+        if code:
+            raise _native.PiqmcError(code, "pq_generate_lattice_table")
+    return nbs
+
+
+def Generate2DIsingInstanceTable(nRows, seed=0, maxnb=4):
+    """Generate2DIsingInstance's neighbour table, generated on the GPU (values from ``seed``)."""
+    return lattice_table("ising2d", nRows, seed=seed, maxnb=maxnb)
+
+
+def Generate2DLatticeTable(nrows, ncols, seed=0, periodic=0, maxnb=4):
+    """Generate2DLattice's neighbour table, generated on the GPU (values from ``seed``)."""
+    return lattice_table("lattice2d", nrows, ncols, seed=seed, periodic=periodic, maxnb=maxnb)
+
+
+def GenerateKblockLatticeTable(nrows, ncols, seed=0, k=1, maxnb=None):
+    """GenerateKblockLattice's neighbour table, generated on the GPU (values from ``seed``)."""
+    return lattice_table("kblock", nrows, ncols, seed=seed, k=k, maxnb=maxnb)
+
+
+# ------------------------------------------------------------------------------------------
 # instance and neighbour-table files
 # ------------------------------------------------------------------------------------------
 

@@ -382,7 +382,7 @@ def test_ctypes_signatures_match_the_header():
     decls = {m.group(2): (m.group(1).strip(), m.group(3))
              for m in re.finditer(r"([\w\s\*]+?)\b(pq_\w+)\s*\(([^)]*)\)\s*;", header)}
     kinds = {"int": ctypes.c_int, "int64_t": ctypes.c_int64, "uint32_t": ctypes.c_uint32,
-             "uint64_t": ctypes.c_uint64, "float": ctypes.c_float}
+             "uint64_t": ctypes.c_uint64, "float": ctypes.c_float, "double": ctypes.c_double}
     assert set(decls) == set(_native.SIGNATURES), set(decls) ^ set(_native.SIGNATURES)
     for name, (ret, plist) in decls.items():
         res, args = _native.SIGNATURES[name]
