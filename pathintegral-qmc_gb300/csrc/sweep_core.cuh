@@ -282,10 +282,38 @@ __device__ __forceinline__ int site_settle(const Item& it, W* rw, int i, uint32_
     load_site<W, MAXDEG>(rw, i, it.n, it.maxdeg, it.nbr, it.cpl, wi, d, J, bad);
     const W w0 = wi;
     if ((wi ^ (wi >> 2)) & (CMk::IN0 | (CMk::IN0 << 1))) return 0;
-    W nbx = 0;
+    W nbx = 0, full = wi ^ (wi >> 1);
 #pragma unroll
-    for (int m = 0; m < MAXDEG; ++m) nbx |= d[m] ^ (d[m] >> 2);
+    for (int m = 0; m < MAXDEG; ++m) {
+        nbx |= d[m] ^ (d[m] >> 2);
+        full |= d[m] ^ (d[m] >> 1);
+    }
     const float h = __ldg(it.field + i);
+    if ((full & (CMk::MASK >> 1)) == 0) {
+        // Every slice sees the same neighbourhood (own and neighbour world-lines
+        // straight): one sum e serves both classes -- the second class has the same
+        // own and neighbour bits, and Trotter partners that agree with it (t = jp + jp)
+        // unless the first class flipped (t = -jp + -jp).
+        float e = flip_sign(h, bit_to_sign<W>(wi, 0));
+#pragma unroll
+        for (int m = 0; m < MAXDEG; ++m) e = __fadd_rn(e, flip_sign(J[m], bit_to_sign<W>(d[m], 0)));
+        const float sum = __fadd_rn(e, __fadd_rn(jp, jp));
+        if (sum >= 0.0f) return __fmul_rn(sum, m2beta) <= settled_x() ? 2 : 0;   // both settled, or neither
+        const W fl = CMk::CM0 << first;
+        wi ^= fl;
+        const float mjp = flip_sign(jp, 0x80000000u);
+        const float sum2 = __fadd_rn(e, __fadd_rn(mjp, mjp));
+        W fl2 = 0;
+        int qq = 2;
+        if (sum2 < 0.0f) fl2 = CMk::CM0 << (first ^ 1u);
+        else if (!(__fmul_rn(sum2, m2beta) <= settled_x())) qq = 1;
+        wi ^= fl2;
+        if (!SPLIT || half == 0) {
+            nacc += sizeof(W) == 8 ? __popcll((unsigned long long)(fl | fl2)) : __popc((uint32_t)(fl | fl2));
+            rw[i] = wi;
+        }
+        return qq;
+    }
     int qq = 0;
     for (; qq < 2; ++qq) {
         const int q = qq ^ (int)first;
