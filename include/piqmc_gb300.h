@@ -219,7 +219,9 @@ typedef struct pq_fast_params {
 } pq_fast_params;
 
 /* words: packed layout in device order, 32-bit words when P <= 32 else 64-bit;
- * in/out.  jperp: device float [nsched] (ignored for P = 1).  accepts (optional,
+ * in/out.  field may be NULL when every field is zero (the same result as a table
+ * of zeros, one load per site less).  jperp: device float [nsched] (ignored for
+ * P = 1).  accepts (optional,
  * may be NULL): one device uint64 counter incremented by the accepted local flips. */
 int pq_qa_fast(void* words, const int32_t* nbr, const float* cpl, const float* field,
                const float* jperp, const pq_fast_params* prm, unsigned long long* accepts,

@@ -207,7 +207,7 @@ static const size_t kSmemBudget = 200 * 1024;
 int pq_qa_fast_ex(void* words, const int32_t* nbr, const float* cpl, const float* field, const float* jperp,
                   const float* betas, const pq_fast_params* prm, unsigned long long* accepts, int32_t* status,
                   void* stream) {
-    if (!prm || !words || !field || !jperp) return PQ_ERR_INVALID_ARG;
+    if (!prm || !words || !jperp) return PQ_ERR_INVALID_ARG;   // field may be NULL: no fields
     const pq_fast_params& p = *prm;
     if (p.n <= 0 || p.R < 0 || p.P < 1 || p.nsched < 0 || p.mcsteps < 0 || p.global_moves < 0 || p.maxdeg < 0)
         return PQ_ERR_INVALID_ARG;

@@ -43,7 +43,7 @@ constexpr int kMaxClasses = PQ_MAX_CLASSES;
 struct Item {
     const int32_t* nbr;       // [maxdeg][n] device slots
     const float* cpl;         // [maxdeg][n]
-    const float* field;       // [n]
+    const float* field;       // [n], or null when every field is zero
     const int32_t* csize;     // [nclass] class sizes (global or shared memory)
     const float* jperp;       // [nsched]
     const float* betas;       // [nsched] or null (then beta)
@@ -123,6 +123,10 @@ __device__ inline void class_order(int M, int order_mode, const KS& ks, uint32_t
         const uint8_t t = order[j]; order[j] = order[k]; order[k] = t;
     }
 }
+
+// A site's field; an instance without fields passes no table (+0, exactly what a
+// table of zeros would give).
+__device__ __forceinline__ float site_field(const Item& it, int i) { return it.field ? __ldg(it.field + i) : 0.0f; }
 
 template <typename W, int MAXDEG>
 __device__ __forceinline__ void load_site(const W* rw, int i, int n, int maxdeg, const int32_t* __restrict__ nbr,
@@ -277,18 +281,15 @@ __device__ __forceinline__ int site_settle(const Item& it, W* rw, int i, uint32_
     using CMk = ClassMasks<W, NQC>;
     constexpr int P = 2 * NQC;
     W wi = rw[i];
+    if ((wi ^ (wi >> 2)) & (CMk::IN0 | (CMk::IN0 << 1))) return 0;   // own world-line not straight per class
     W d[MAXDEG];
     float J[MAXDEG];
     load_site<W, MAXDEG>(rw, i, it.n, it.maxdeg, it.nbr, it.cpl, wi, d, J, bad);
     const W w0 = wi;
-    if ((wi ^ (wi >> 2)) & (CMk::IN0 | (CMk::IN0 << 1))) return 0;
-    W nbx = 0, full = wi ^ (wi >> 1);
+    W full = wi ^ (wi >> 1);
 #pragma unroll
-    for (int m = 0; m < MAXDEG; ++m) {
-        nbx |= d[m] ^ (d[m] >> 2);
-        full |= d[m] ^ (d[m] >> 1);
-    }
-    const float h = __ldg(it.field + i);
+    for (int m = 0; m < MAXDEG; ++m) full |= d[m] ^ (d[m] >> 1);
+    const float h = site_field(it, i);
     if ((full & (CMk::MASK >> 1)) == 0) {
         // Every slice sees the same neighbourhood (own and neighbour world-lines
         // straight): one sum e serves both classes -- the second class has the same
@@ -314,6 +315,9 @@ __device__ __forceinline__ int site_settle(const Item& it, W* rw, int i, uint32_
         }
         return qq;
     }
+    W nbx = 0;
+#pragma unroll
+    for (int m = 0; m < MAXDEG; ++m) nbx |= d[m] ^ (d[m] >> 2);
     int qq = 0;
     for (; qq < 2; ++qq) {
         const int q = qq ^ (int)first;
@@ -352,7 +356,7 @@ __device__ __forceinline__ void site_update(const Item& it, const KS& ks, W* rw,
     W d[MAXDEG];
     float J[MAXDEG];
     load_site<W, MAXDEG>(rw, i, it.n, it.maxdeg, it.nbr, it.cpl, wi, d, J, bad);
-    const float h = __ldg(it.field + i);
+    const float h = site_field(it, i);
     for (int qq = qq0; qq < nclass_q; ++qq) {
         const int q = nclass_q == 2 ? (qq ^ (int)first) : qq;
         W fl;
@@ -589,7 +593,7 @@ __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* s
                         W d[MAXDEG];
                         float J[MAXDEG];
                         load_site<W, MAXDEG>(rw, i, n, it.maxdeg, it.nbr, it.cpl, wi, d, J, bad);
-                        const float h = __ldg(it.field + i);
+                        const float h = site_field(it, i);
                         float E = 0.0f;
                         for (int k = 0; k < P; ++k) {
                             float e = flip_sign(h, bit_to_sign<W>(wi, k));

@@ -141,6 +141,7 @@ class Problem:
         cpl[slots, dev_rows] = jv[r_i, r_m]
         field[self.perm] = h64.astype(np.float32)
         self.nbr_host, self.cpl_host, self.field_host = nbr, cpl, field
+        self.no_field = not np.any(field)
         # FP64 CSR for energies, device order
         e_r, e_m = np.nonzero(self_mask | off_mask)
         vals = np.where(self_mask, jv64, 0.5 * jv64)
@@ -247,8 +248,9 @@ def anneal(problem, words, sched, P, temp, mcsteps=1, seed=0, global_moves=0, sw
     st = status if status is not None else _device.Status()
     prm = problem.params(P, R, nsched, mcsteps, temp, seed, global_moves, sweep_base, replica_base, threads,
                          replicas_per_cta, order_mode)
+    field = None if problem.no_field else problem.field     # no table when every field is zero
     code = _native.lib().pq_qa_fast_ex(
-        _device.ptr(words), _device.ptr(problem.nbr), _device.ptr(problem.cpl), _device.ptr(problem.field),
+        _device.ptr(words), _device.ptr(problem.nbr), _device.ptr(problem.cpl), _device.ptr(field),
         _device.ptr(jperp), _device.ptr(betas), ctypes.byref(prm), _device.ptr(accepts), st.ptr,
         _device.stream_handle(stream))
     _native.check(code, "pq_qa_fast")
