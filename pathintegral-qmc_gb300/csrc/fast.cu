@@ -32,8 +32,9 @@ __global__ void __launch_bounds__(512) qa_fast_kernel(W* __restrict__ words, con
                                                       int32_t* __restrict__ status) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int csize[kMaxClasses];
-    __shared__ uint32_t queue_slots[kQueuePerThread * 512];   // unsettled sites of a phase
-    __shared__ int queue_count[2];
+    // the unsettled sites of a phase: kQueuePerThread slots per thread and two counters, after the item
+    uint32_t* queue_slots = reinterpret_cast<uint32_t*>(smem_raw + item_smem_bytes(a.rpc, a.n, a.P));
+    int* queue_count = reinterpret_cast<int*>(queue_slots + kQueuePerThread * blockDim.x);
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int c = 0; c < kMaxClasses; ++c) csize[c] = a.class_size[c];
@@ -150,7 +151,7 @@ template <typename W, int MAXDEG, int NQC, bool STAGED>
 int launch_fast_t(void* words, const int32_t* nbr, const float* cpl, const float* field, const float* jperp,
                   const float* betas, const FastArgs& a, int threads, unsigned long long* accepts, int32_t* status,
                   cudaStream_t stream) {
-    const size_t smem = item_smem_bytes(a.rpc, a.n, a.P);
+    const size_t smem = item_smem_bytes(a.rpc, a.n, a.P) + (size_t)kQueuePerThread * threads * 4 + 16;
     static PqSmemAttr attr;
     const int rc = pq_set_smem_limit(attr, (const void*)qa_fast_kernel<W, MAXDEG, NQC, STAGED>, 220 * 1024);
     if (rc != PQ_OK) return rc;
@@ -160,11 +161,48 @@ int launch_fast_t(void* words, const int32_t* nbr, const float* cpl, const float
     return pq_launch_status();
 }
 
-// Compile-time P: staged phases when a thread walks at least two sites per phase (staged_phase).
+template <typename W, int MAXDEG, int NQC>
+const void* fast_kernel_for(const FastArgs& a, int threads) {
+    if constexpr (NQC > 0)
+        if (staged_phase(NQC, a.rpc, a.stride, threads)) return (const void*)qa_fast_kernel<W, MAXDEG, NQC, true>;
+    return (const void*)qa_fast_kernel<W, MAXDEG, NQC, false>;
+}
+
+// Waves of CTAs a launch of `threads`-thread CTAs takes on this device (resident
+// CTAs per SM from the runtime's occupancy of the variant that would run).
+template <typename W, int MAXDEG, int NQC>
+int fast_waves(const FastArgs& a, int threads, int64_t* waves) {
+    const void* k = fast_kernel_for<W, MAXDEG, NQC>(a, threads);
+    PQ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+    int dev = 0, nsm = 0, per_sm = 0;
+    PQ_CUDA_TRY(cudaGetDevice(&dev));
+    PQ_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const size_t smem = item_smem_bytes(a.rpc, a.n, a.P) + (size_t)kQueuePerThread * threads * 4 + 16;
+    PQ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem));
+    const int64_t slots = (int64_t)nsm * (per_sm > 0 ? per_sm : 1);
+    const int64_t grid = (a.R + a.rpc - 1) / a.rpc;
+    *waves = (grid + slots - 1) / slots;
+    return PQ_OK;
+}
+
+// Compile-time P: staged phases when a thread walks at least two sites per phase
+// (staged_phase).  With the thread count chosen automatically, CTAs of half the
+// size are taken when that runs the replicas in fewer waves (more CTAs resident
+// per SM): the last wave of a launch leaves SMs idle.
 template <typename W, int MAXDEG, int NQC>
 int launch_fast(void* words, const int32_t* nbr, const float* cpl, const float* field, const float* jperp,
-                const float* betas, const FastArgs& a, int threads, unsigned long long* accepts,
+                const float* betas, const FastArgs& a, int threads, bool auto_threads, unsigned long long* accepts,
                 int32_t* status, cudaStream_t stream) {
+    const int half = threads / 2;
+    if (auto_threads && half >= 64 && half % 32 == 0 && half >= a.rpc &&
+        ((int64_t)a.rpc * a.stride) % half == 0) {
+        int64_t w_full = 0, w_half = 0;
+        int rc = fast_waves<W, MAXDEG, NQC>(a, threads, &w_full);
+        if (rc != PQ_OK) return rc;
+        rc = fast_waves<W, MAXDEG, NQC>(a, half, &w_half);
+        if (rc != PQ_OK) return rc;
+        if (w_half < w_full) threads = half;
+    }
     if constexpr (NQC > 0) {
         if (staged_phase(NQC, a.rpc, a.stride, threads))
             return launch_fast_t<W, MAXDEG, NQC, true>(words, nbr, cpl, field, jperp, betas, a, threads, accepts,
@@ -176,24 +214,24 @@ int launch_fast(void* words, const int32_t* nbr, const float* cpl, const float* 
 
 template <typename W>
 int dispatch_deg(void* words, const int32_t* nbr, const float* cpl, const float* field, const float* jperp,
-                 const float* betas, const FastArgs& a, int threads, unsigned long long* accepts,
+                 const float* betas, const FastArgs& a, int threads, bool auto_threads, unsigned long long* accepts,
                  int32_t* status, cudaStream_t stream) {
     // compile-time slice counts for the common even P with exactly four couplings
     if (a.maxdeg == 4) {
         if constexpr (sizeof(W) == 4) {
-            if (a.P == 20) return launch_fast<W, 4, 10>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status, stream);
-            if (a.P == 16) return launch_fast<W, 4, 8>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status, stream);
-            if (a.P == 32) return launch_fast<W, 4, 16>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status, stream);
+            if (a.P == 20) return launch_fast<W, 4, 10>(words, nbr, cpl, field, jperp, betas, a, threads, auto_threads, accepts, status, stream);
+            if (a.P == 16) return launch_fast<W, 4, 8>(words, nbr, cpl, field, jperp, betas, a, threads, auto_threads, accepts, status, stream);
+            if (a.P == 32) return launch_fast<W, 4, 16>(words, nbr, cpl, field, jperp, betas, a, threads, auto_threads, accepts, status, stream);
         } else {
-            if (a.P == 64) return launch_fast<W, 4, 32>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status, stream);
+            if (a.P == 64) return launch_fast<W, 4, 32>(words, nbr, cpl, field, jperp, betas, a, threads, auto_threads, accepts, status, stream);
         }
     }
     if (a.maxdeg <= 4)
-        return launch_fast<W, 4, 0>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status, stream);
+        return launch_fast<W, 4, 0>(words, nbr, cpl, field, jperp, betas, a, threads, auto_threads, accepts, status, stream);
     if (a.maxdeg <= 8)
-        return launch_fast<W, 8, 0>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status, stream);
+        return launch_fast<W, 8, 0>(words, nbr, cpl, field, jperp, betas, a, threads, auto_threads, accepts, status, stream);
     if (a.maxdeg <= 16)
-        return launch_fast<W, 16, 0>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status, stream);
+        return launch_fast<W, 16, 0>(words, nbr, cpl, field, jperp, betas, a, threads, auto_threads, accepts, status, stream);
     return PQ_ERR_UNSUPPORTED;
 }
 
@@ -232,6 +270,7 @@ int pq_qa_fast_ex(void* words, const int32_t* nbr, const float* cpl, const float
     a.sweep_base = p.sweep_base;
     a.replica_base = p.replica_base;
     int threads = p.threads > 0 ? p.threads : 0;
+    const bool auto_threads = threads == 0;
     int rpc = p.replicas_per_cta;
     if (rpc <= 0) {
         // enough replicas per CTA for 128 items per phase, within the smem budget
@@ -251,11 +290,14 @@ int pq_qa_fast_ex(void* words, const int32_t* nbr, const float* cpl, const float
         if (!threads) threads = items >= 256 ? 256 : ((items + 31) / 32) * 32;
     }
     if (threads % 32 || threads > 512 || threads < rpc) return PQ_ERR_INVALID_ARG;
-    if (item_smem_bytes(rpc, p.n, p.P) > kSmemBudget) return PQ_ERR_TOO_LARGE;
+    if (item_smem_bytes(rpc, p.n, p.P) + (size_t)kQueuePerThread * threads * 4 + 16 > kSmemBudget)
+        return PQ_ERR_TOO_LARGE;
     a.rpc = rpc;
     cudaStream_t st = (cudaStream_t)stream;
-    if (wbytes == 4) return dispatch_deg<uint32_t>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status, st);
-    return dispatch_deg<uint64_t>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status, st);
+    if (wbytes == 4)
+        return dispatch_deg<uint32_t>(words, nbr, cpl, field, jperp, betas, a, threads, auto_threads, accepts, status,
+                                      st);
+    return dispatch_deg<uint64_t>(words, nbr, cpl, field, jperp, betas, a, threads, auto_threads, accepts, status, st);
 }
 
 int pq_qa_fast(void* words, const int32_t* nbr, const float* cpl, const float* field, const float* jperp,
