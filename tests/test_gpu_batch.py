@@ -76,3 +76,29 @@ def test_batch_chunks_and_graph_replay():
     EA, EB = A.energies(), B.energies()
     for a, b in zip(EA, EB):
         assert torch.equal(a, b)
+
+
+def test_batch_equals_the_oracle_directly():
+    """Every instance of a batch against the packed sweep's CPU restatement, bit for bit
+    (not only through the single-instance kernel): staged and per-site items, P = 1..64."""
+    import oracle
+    from piqmc import batch, fast
+    nbs, R, P, g = _instances(2)
+    spins = [np.where(g.random((r, nb.shape[0], p)) < 0.5, -1, 1).astype(np.int8) for nb, r, p in zip(nbs, R, P)]
+    B = batch.Batch(nbs, R, P)
+    B.set_spins(spins)
+    sched = np.linspace(3.0, 1e-8, 7)
+    T, seed = 0.05, 21
+    B.anneal(sched, T, seed=seed, global_moves=1)
+    got = [s.cpu().numpy() for s in B.spins()]
+    for i, (nb, r, p) in enumerate(zip(nbs, R, P)):
+        prob = fast.Problem(nb, on_device=False)
+        jp = oracle.jperp(sched, p, T) if p > 1 else np.zeros(len(sched), np.float32)
+        for rr in range(r):
+            w = np.zeros(prob.nslots, np.uint64)
+            bits = (spins[i][rr] < 0).astype(np.uint64)
+            w[prob.perm] = (bits << np.arange(p, dtype=np.uint64)).sum(axis=1, dtype=np.uint64)
+            oracle.fast_anneal(prob.nbr_host, prob.cpl_host, prob.field_host, prob.class_size, prob.class_stride, w,
+                               p, jp, 1, np.float32(1) / np.float32(T), seed + i, replica=rr, global_moves=1)
+            want = np.where((w[prob.perm][:, None] >> np.arange(p, dtype=np.uint64)) & np.uint64(1), -1, 1)
+            np.testing.assert_array_equal(got[i][rr], want.astype(np.int8), err_msg="instance %d replica %d" % (i, rr))
