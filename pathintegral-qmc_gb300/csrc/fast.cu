@@ -21,18 +21,16 @@ struct FastArgs {
     PhiloxKeyTable keys;  // round keys of (key0, key1), read as constant operands
 };
 
+// One CTA's replicas through the schedule (the body of both kernels below).
 template <typename W, int MAXDEG, int NQC, bool STAGED>
-__global__ void __launch_bounds__(512) qa_fast_kernel(W* __restrict__ words, const int32_t* __restrict__ nbr,
-                                                      const float* __restrict__ cpl,
-                                                      const float* __restrict__ field,
-                                                      const float* __restrict__ jperp,
-                                                      const float* __restrict__ betas,
-                                                      const __grid_constant__ FastArgs a,
-                                                      unsigned long long* __restrict__ accepts,
-                                                      int32_t* __restrict__ status) {
+__device__ __forceinline__ void fast_cta(W* __restrict__ words, const int32_t* __restrict__ nbr,
+                                         const float* __restrict__ cpl, const float* __restrict__ field,
+                                         const float* __restrict__ jperp, const float* __restrict__ betas,
+                                         const FastArgs& a, unsigned long long* __restrict__ accepts,
+                                         int32_t* __restrict__ status) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int csize[kMaxClasses];
-    // the unsettled sites of a phase: kQueuePerThread slots per thread and two counters, after the item
+    // the sites a phase visits: kQueuePerThread slots per thread and two counters, after the item
     uint32_t* queue_slots = reinterpret_cast<uint32_t*>(smem_raw + item_smem_bytes(a.rpc, a.n, a.P));
     int* queue_count = reinterpret_cast<int*>(queue_slots + kQueuePerThread * blockDim.x);
     if (threadIdx.x == 0) {
@@ -65,6 +63,41 @@ __global__ void __launch_bounds__(512) qa_fast_kernel(W* __restrict__ words, con
         for (int off = 16; off > 0; off >>= 1) nacc += __shfl_down_sync(0xffffffffu, nacc, off);
         if ((threadIdx.x & 31) == 0 && nacc) atomicAdd(accepts, nacc);
     }
+}
+
+template <typename W, int MAXDEG, int NQC, bool STAGED>
+__global__ void __launch_bounds__(512) qa_fast_kernel(W* __restrict__ words, const int32_t* __restrict__ nbr,
+                                                      const float* __restrict__ cpl,
+                                                      const float* __restrict__ field,
+                                                      const float* __restrict__ jperp,
+                                                      const float* __restrict__ betas,
+                                                      const __grid_constant__ FastArgs a,
+                                                      unsigned long long* __restrict__ accepts,
+                                                      int32_t* __restrict__ status) {
+    fast_cta<W, MAXDEG, NQC, STAGED>(words, nbr, cpl, field, jperp, betas, a, accepts, status);
+}
+
+// The staged 32-bit variants with a cap of 72 registers: seven 128-thread CTAs fit
+// an SM (the shared memory of an 80x80 replica allows seven); uncapped they take
+// over 90.
+template <int MAXDEG, int NQC>
+__global__ void __maxnreg__(72) qa_fast_kernel_staged32(uint32_t* __restrict__ words,
+                                                        const int32_t* __restrict__ nbr,
+                                                        const float* __restrict__ cpl,
+                                                        const float* __restrict__ field,
+                                                        const float* __restrict__ jperp,
+                                                        const float* __restrict__ betas,
+                                                        const __grid_constant__ FastArgs a,
+                                                        unsigned long long* __restrict__ accepts,
+                                                        int32_t* __restrict__ status) {
+    fast_cta<uint32_t, MAXDEG, NQC, true>(words, nbr, cpl, field, jperp, betas, a, accepts, status);
+}
+
+// The kernel of one variant.
+template <typename W, int MAXDEG, int NQC, bool STAGED>
+auto fast_kernel() {
+    if constexpr (STAGED && sizeof(W) == 4) return qa_fast_kernel_staged32<MAXDEG, NQC>;
+    else return qa_fast_kernel<W, MAXDEG, NQC, STAGED>;
 }
 
 // FP64 energy of one (replica, slice) per warp from the CSR of the coupling matrix.
@@ -153,19 +186,19 @@ int launch_fast_t(void* words, const int32_t* nbr, const float* cpl, const float
                   cudaStream_t stream) {
     const size_t smem = item_smem_bytes(a.rpc, a.n, a.P) + (size_t)kQueuePerThread * threads * 4 + 16;
     static PqSmemAttr attr;
-    const int rc = pq_set_smem_limit(attr, (const void*)qa_fast_kernel<W, MAXDEG, NQC, STAGED>, 220 * 1024);
+    const auto kernel = fast_kernel<W, MAXDEG, NQC, STAGED>();
+    const int rc = pq_set_smem_limit(attr, (const void*)kernel, 220 * 1024);
     if (rc != PQ_OK) return rc;
     const int grid = (a.R + a.rpc - 1) / a.rpc;
-    qa_fast_kernel<W, MAXDEG, NQC, STAGED><<<grid, threads, smem, stream>>>((W*)words, nbr, cpl, field, jperp, betas,
-                                                                           a, accepts, status);
+    kernel<<<grid, threads, smem, stream>>>((W*)words, nbr, cpl, field, jperp, betas, a, accepts, status);
     return pq_launch_status();
 }
 
 template <typename W, int MAXDEG, int NQC>
 const void* fast_kernel_for(const FastArgs& a, int threads) {
     if constexpr (NQC > 0)
-        if (staged_phase(NQC, a.rpc, a.stride, threads)) return (const void*)qa_fast_kernel<W, MAXDEG, NQC, true>;
-    return (const void*)qa_fast_kernel<W, MAXDEG, NQC, false>;
+        if (staged_phase(NQC, a.rpc, a.stride, threads)) return (const void*)fast_kernel<W, MAXDEG, NQC, true>();
+    return (const void*)fast_kernel<W, MAXDEG, NQC, false>();
 }
 
 // Waves of CTAs a launch of `threads`-thread CTAs takes on this device (resident

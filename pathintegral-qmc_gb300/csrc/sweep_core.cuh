@@ -164,11 +164,13 @@ __device__ __forceinline__ bool decide(float sum, float u, float m2beta, float m
 // Core of the compile-time path: NQH slices m = 0..NQH-1 whose bits sit at
 // positions 2m of the 32-bit (q-shifted) words wq, dq, dl, dr; the m-th uses
 // word m & 3 of Philox block blk0 + (m >> 2).  Returns the flips at bits 2m.
+//   calm: cleared unless every slice's sum is at least smin (a certain rejection,
+// settle_threshold).
 template <int NQH, int DEG, typename KS>
 __device__ __forceinline__ uint32_t update_half(uint32_t wq, const uint32_t (&dq)[DEG], uint32_t dl, uint32_t dr,
                                                 const float (&J)[DEG], float h, float jp, int q, int blk0, uint32_t i,
                                                 uint32_t sweep, uint32_t rep, const KS& ks, float m2beta,
-                                                float m2blog2e) {
+                                                float m2blog2e, float smin, bool& calm) {
     uint32_t flips = 0;
 #pragma unroll
     for (int blk = 0; blk < (NQH + 3) / 4; ++blk) {
@@ -184,6 +186,7 @@ __device__ __forceinline__ uint32_t update_half(uint32_t wq, const uint32_t (&dq
                 for (int m = 0; m < DEG; ++m) e = __fadd_rn(e, flip_sign(J[m], (dq[m] << sh) & 0x80000000u));
                 const float t = __fadd_rn(flip_sign(jp, (dl << sh) & 0x80000000u), flip_sign(jp, (dr << sh) & 0x80000000u));
                 const float sum = __fadd_rn(e, t);
+                calm = calm && sum >= smin;
                 if (decide(sum, pq_u01(rw4[jj]), m2beta, m2blog2e)) flips |= 1u << (2 * mm);
             }
         }
@@ -195,16 +198,23 @@ __device__ __forceinline__ uint32_t update_half(uint32_t wq, const uint32_t (&dq
 // fixed at compile time (NQ <= 16 with 32-bit words, NQ = 32 with 64-bit words
 // as two 32-bit halves), DEG couplings.  Same arithmetic and uniforms as the
 // generic path.
+// calm: cleared unless every slice of the class is a certain rejection (sum >= smin)
+// whose Trotter partners are not both opposite to it (t = -2 J-perp would fall as
+// J-perp grows; t = 2 J-perp or 0 does not).
 template <int NQ, int DEG, typename W, typename KS>
 __device__ __forceinline__ W update_fixed(W wi, const W (&d)[DEG], const float (&J)[DEG], float h, float jp, int q,
                                           uint32_t i, uint32_t sweep, uint32_t rep, const KS& ks, float m2beta,
-                                          float m2blog2e) {
+                                          float m2blog2e, float smin, bool& calm) {
     constexpr int P = 2 * NQ;
     constexpr int BITS = 8 * sizeof(W);
     constexpr W MASK = P >= BITS ? ~(W)0 : (((W)1 << P) - 1);
     const W up = ((wi << 1) | (wi >> (P - 1))) & MASK;
     const W dn = ((wi >> 1) | (wi << (P - 1))) & MASK;
     const W dlw = wi ^ up, drw = wi ^ dn;
+    W cm = 0;
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) cm |= (W)1 << (2 * k);
+    calm = calm && (dlw & drw & (cm << q)) == 0;
     W flips = 0;
 #pragma unroll
     for (int half = 0; half < (P + 31) / 32; ++half) {
@@ -215,7 +225,7 @@ __device__ __forceinline__ W update_fixed(W wi, const W (&d)[DEG], const float (
         const uint32_t f = update_half<NQH, DEG, KS>((uint32_t)(wi >> (32 * half)) >> q, dq,
                                                      (uint32_t)(dlw >> (32 * half)) >> q,
                                                      (uint32_t)(drw >> (32 * half)) >> q, J, h, jp, q, 4 * half, i,
-                                                     sweep, rep, ks, m2beta, m2blog2e);
+                                                     sweep, rep, ks, m2beta, m2blog2e, smin, calm);
         flips |= (W)f << (32 * half);
     }
     return flips << q;
@@ -228,17 +238,18 @@ template <int DEG, typename KS>
 __device__ __forceinline__ uint64_t update_fixed_half64(uint64_t wi, const uint64_t (&d)[DEG], const float (&J)[DEG],
                                                         float h, float jp, int q, int half, uint32_t i,
                                                         uint32_t sweep, uint32_t rep, const KS& ks, float m2beta,
-                                                        float m2blog2e) {
+                                                        float m2blog2e, float smin, bool& calm) {
     const uint64_t up = (wi << 1) | (wi >> 63);
     const uint64_t dn = (wi >> 1) | (wi << 63);
     const uint64_t dlw = wi ^ up, drw = wi ^ dn;
     const int sh = 32 * half;
+    calm = calm && ((uint32_t)((dlw & drw) >> sh) & (0x55555555u << q)) == 0;
     uint32_t dq[DEG];
 #pragma unroll
     for (int m = 0; m < DEG; ++m) dq[m] = (uint32_t)(d[m] >> sh) >> q;
     const uint32_t f = update_half<16, DEG, KS>((uint32_t)(wi >> sh) >> q, dq, (uint32_t)(dlw >> sh) >> q,
                                                 (uint32_t)(drw >> sh) >> q, J, h, jp, q, 4 * half, i, sweep, rep, ks,
-                                                m2beta, m2blog2e);
+                                                m2beta, m2blog2e, smin, calm);
     return ((uint64_t)f << sh) << q;
 }
 
@@ -263,85 +274,164 @@ struct ClassMasks {
     static constexpr W MASK = 2 * NQ >= (int)(8 * sizeof(W)) ? ~(W)0 : (((W)1 << (2 * NQ)) - 1);
 };
 
-// Stage A of the local update of one site (compile-time P = 2 * NQC): a slice class
-// all of whose slices see the same neighbourhood -- own bit, neighbour bits and both
-// Trotter partners equal across the class -- has one energy sum for all of them.
-// When that sum settles the class (flip all, or reject all, see settled_x) it is
-// applied here without random numbers, which is exactly what the per-slice update
-// would do.  Classes are taken in the replica's parity order; returns the index qq
-// of the first class left unsettled (2 = the site is done).  A flip of a whole
+// Outcome of one site's visit in a staged phase.
+enum SiteVisit { kVisitKept = 0, kVisitQuiet = 1, kVisitChanged = 2 };
+
+// The local update of one site in a staged phase (compile-time P = 2 * NQC), from
+// one load of its neighbourhood.  A slice class all of whose slices see the same
+// neighbourhood -- own bit, neighbour bits and both Trotter partners equal across
+// the class -- has one energy sum for all of them; when that sum settles the class
+// (flip all, or reject all, see settled_x) it is applied without random numbers,
+// which is exactly what the per-slice update would do.  Classes are taken in the
+// replica's parity order; from the first class left unsettled on, every slice
+// draws its uniform and is decided on its own (update_fixed).  A flip of a whole
 // class keeps every word straight on the other class, so the test of the second
 // class uses the neighbour words loaded once.
-template <typename W, int MAXDEG, int NQC, bool SPLIT>
-__device__ __forceinline__ int site_settle(const Item& it, W* rw, int i, uint32_t first, float jp, float m2beta,
-                                           int half, bool& bad, unsigned long long& nacc) {
-  if constexpr (NQC == 0) {
-    return 0;   // run-time P: never staged
-  } else {
+//
+// Returns kVisitQuiet when every slice of both classes is a rejection whatever its
+// uniform and its sum s = e + t cannot fall as J-perp grows (t = 2 J-perp or 0, not
+// -2 J-perp): either the site's own and neighbour world-lines are straight and the
+// common sum s = e + 2 J-perp rejects, or every slice, decided on its own, had
+// s >= smin and no slice had both Trotter partners opposite to it.  Such a site
+// rejects again at every later visit for which nothing in its neighbourhood has
+// changed, J-perp has not decreased and beta has not decreased (each s only grows
+// with J-perp, and fl(s * -2 beta) only falls as s and beta grow).  kVisitChanged
+// when the site's word changed.
+template <typename W, int MAXDEG, int NQC, typename KS, bool SPLIT>
+__device__ __forceinline__ int site_visit(const Item& it, const KS& ks, W* rw, int i, uint32_t rep, uint32_t first,
+                                          float jp, uint32_t sweep, float m2beta, float m2blog2e, float smin, int half,
+                                          unsigned pair_mask, bool& bad, unsigned long long& nacc) {
+    static_assert(NQC > 0, "staged phases need a compile-time slice count");
     using CMk = ClassMasks<W, NQC>;
     constexpr int P = 2 * NQC;
-    W wi = rw[i];
-    if ((wi ^ (wi >> 2)) & (CMk::IN0 | (CMk::IN0 << 1))) return 0;   // own world-line not straight per class
+    const W w0 = rw[i];
+    W wi = w0;
     W d[MAXDEG];
     float J[MAXDEG];
     load_site<W, MAXDEG>(rw, i, it.n, it.maxdeg, it.nbr, it.cpl, wi, d, J, bad);
-    const W w0 = wi;
-    W full = wi ^ (wi >> 1);
-#pragma unroll
-    for (int m = 0; m < MAXDEG; ++m) full |= d[m] ^ (d[m] >> 1);
     const float h = site_field(it, i);
-    if ((full & (CMk::MASK >> 1)) == 0) {
-        // Every slice sees the same neighbourhood (own and neighbour world-lines
-        // straight): one sum e serves both classes -- the second class has the same
-        // own and neighbour bits, and Trotter partners that agree with it (t = jp + jp)
-        // unless the first class flipped (t = -jp + -jp).
-        float e = flip_sign(h, bit_to_sign<W>(wi, 0));
-#pragma unroll
-        for (int m = 0; m < MAXDEG; ++m) e = __fadd_rn(e, flip_sign(J[m], bit_to_sign<W>(d[m], 0)));
-        const float sum = __fadd_rn(e, __fadd_rn(jp, jp));
-        if (sum >= 0.0f) return __fmul_rn(sum, m2beta) <= settled_x() ? 2 : 0;   // both settled, or neither
-        const W fl = CMk::CM0 << first;
-        wi ^= fl;
-        const float mjp = flip_sign(jp, 0x80000000u);
-        const float sum2 = __fadd_rn(e, __fadd_rn(mjp, mjp));
-        W fl2 = 0;
-        int qq = 2;
-        if (sum2 < 0.0f) fl2 = CMk::CM0 << (first ^ 1u);
-        else if (!(__fmul_rn(sum2, m2beta) <= settled_x())) qq = 1;
-        wi ^= fl2;
-        if (!SPLIT || half == 0) {
-            nacc += sizeof(W) == 8 ? __popcll((unsigned long long)(fl | fl2)) : __popc((uint32_t)(fl | fl2));
-            rw[i] = wi;
-        }
-        return qq;
-    }
-    W nbx = 0;
-#pragma unroll
-    for (int m = 0; m < MAXDEG; ++m) nbx |= d[m] ^ (d[m] >> 2);
     int qq = 0;
+    if (((wi ^ (wi >> 2)) & (CMk::IN0 | (CMk::IN0 << 1))) == 0) {   // own world-line straight per class
+        W full = wi ^ (wi >> 1);
+#pragma unroll
+        for (int m = 0; m < MAXDEG; ++m) full |= d[m] ^ (d[m] >> 1);
+        if ((full & (CMk::MASK >> 1)) == 0) {
+            // Every slice sees the same neighbourhood (own and neighbour world-lines
+            // straight): one sum e serves both classes -- the second class has the same
+            // own and neighbour bits, and Trotter partners that agree with it (t = jp + jp)
+            // unless the first class flipped (t = -jp + -jp).
+            float e = flip_sign(h, bit_to_sign<W>(wi, 0));
+#pragma unroll
+            for (int m = 0; m < MAXDEG; ++m) e = __fadd_rn(e, flip_sign(J[m], bit_to_sign<W>(d[m], 0)));
+            const float sum = __fadd_rn(e, __fadd_rn(jp, jp));
+            if (sum >= 0.0f) {
+                if (__fmul_rn(sum, m2beta) <= settled_x()) return kVisitQuiet;   // both classes reject
+                // neither class settled: every slice on its own
+            } else {
+                const W fl = CMk::CM0 << first;
+                const float mjp = flip_sign(jp, 0x80000000u);
+                const float sum2 = __fadd_rn(e, __fadd_rn(mjp, mjp));
+                W fl2 = 0;
+                qq = 2;
+                if (sum2 < 0.0f) fl2 = CMk::CM0 << (first ^ 1u);
+                else if (!(__fmul_rn(sum2, m2beta) <= settled_x())) qq = 1;
+                wi ^= fl | fl2;
+#pragma unroll
+                for (int m = 0; m < MAXDEG; ++m) d[m] ^= fl | fl2;
+                if (!SPLIT || half == 0)
+                    nacc += sizeof(W) == 8 ? __popcll((unsigned long long)(fl | fl2)) : __popc((uint32_t)(fl | fl2));
+            }
+        } else {
+            W nbx = 0;
+#pragma unroll
+            for (int m = 0; m < MAXDEG; ++m) nbx |= d[m] ^ (d[m] >> 2);
+            for (; qq < 2; ++qq) {
+                const int q = qq ^ (int)first;
+                if (nbx & (CMk::IN0 << q)) break;
+                const W up = ((wi << 1) | (wi >> (P - 1))) & CMk::MASK;   // bit k = s^{k-1}
+                const W dn = ((wi >> 1) | (wi << (P - 1))) & CMk::MASK;   // bit k = s^{k+1}
+                float e = flip_sign(h, bit_to_sign<W>(wi, q));
+#pragma unroll
+                for (int m = 0; m < MAXDEG; ++m) e = __fadd_rn(e, flip_sign(J[m], bit_to_sign<W>(d[m], q)));
+                const float t =
+                    __fadd_rn(flip_sign(jp, bit_to_sign<W>(wi ^ up, q)), flip_sign(jp, bit_to_sign<W>(wi ^ dn, q)));
+                const float sum = __fadd_rn(e, t);
+                W fl;
+                if (sum < 0.0f) fl = CMk::CM0 << q;
+                else if (__fmul_rn(sum, m2beta) <= settled_x()) fl = 0;
+                else break;
+                wi ^= fl;
+#pragma unroll
+                for (int m = 0; m < MAXDEG; ++m) d[m] ^= fl;
+                if (!SPLIT || half == 0)
+                    nacc += sizeof(W) == 8 ? __popcll((unsigned long long)fl) : __popc((uint32_t)fl);
+            }
+        }
+    }
+    bool calm = qq == 0;   // both classes decided slice by slice (none settled above)
+#pragma unroll 1
     for (; qq < 2; ++qq) {
         const int q = qq ^ (int)first;
-        if (nbx & (CMk::IN0 << q)) break;
-        const W up = ((wi << 1) | (wi >> (P - 1))) & CMk::MASK;   // bit k = s^{k-1}
-        const W dn = ((wi >> 1) | (wi << (P - 1))) & CMk::MASK;   // bit k = s^{k+1}
-        float e = flip_sign(h, bit_to_sign<W>(wi, q));
-#pragma unroll
-        for (int m = 0; m < MAXDEG; ++m) e = __fadd_rn(e, flip_sign(J[m], bit_to_sign<W>(d[m], q)));
-        const float t = __fadd_rn(flip_sign(jp, bit_to_sign<W>(wi ^ up, q)), flip_sign(jp, bit_to_sign<W>(wi ^ dn, q)));
-        const float sum = __fadd_rn(e, t);
         W fl;
-        if (sum < 0.0f) fl = CMk::CM0 << q;
-        else if (__fmul_rn(sum, m2beta) <= settled_x()) fl = 0;
-        else break;
+        if constexpr (SPLIT) {
+            const W own = update_fixed_half64<MAXDEG, KS>(wi, d, J, h, jp, q, half, (uint32_t)i, sweep, rep, ks,
+                                                         m2beta, m2blog2e, smin, calm);
+            nacc += __popcll((unsigned long long)own);
+            fl = own | (W)__shfl_xor_sync(pair_mask, (unsigned long long)own, 1);
+        } else {
+            fl = update_fixed<NQC, MAXDEG, W, KS>(wi, d, J, h, jp, q, (uint32_t)i, sweep, rep, ks, m2beta, m2blog2e,
+                                                  smin, calm);
+            nacc += sizeof(W) == 8 ? __popcll((unsigned long long)fl) : __popc((uint32_t)fl);
+        }
+        // the neighbours are unchanged in this phase: only the spin's own bits move
         wi ^= fl;
 #pragma unroll
         for (int m = 0; m < MAXDEG; ++m) d[m] ^= fl;
-        if (!SPLIT || half == 0)
-            nacc += sizeof(W) == 8 ? __popcll((unsigned long long)fl) : __popc((uint32_t)fl);
     }
-    if (wi != w0 && (!SPLIT || half == 0)) rw[i] = wi;
-    return qq;
-  }
+    if constexpr (SPLIT) calm = __shfl_xor_sync(pair_mask, (int)calm, 1) != 0 && calm;
+    if (wi == w0) return calm ? kVisitQuiet : kVisitKept;
+    if (!SPLIT || half == 0) rw[i] = wi;
+    return kVisitChanged;
+}
+
+// The smallest FP32 s >= 0 with fl(s * m2beta) <= settled_x() (m2beta = -2 beta < 0;
+// the product falls as s grows, so s >= the result is exactly that test); +inf when
+// m2beta >= 0.  Bisection over the bit patterns of the non-negative floats.
+__device__ __forceinline__ float settle_threshold(float m2beta) {
+    if (!(m2beta < 0.0f)) return __uint_as_float(0x7f800000u);
+    uint32_t lo = 0u, hi = 0x7f800000u;   // fails at lo (+0), holds at hi (+inf)
+#pragma unroll 1
+    while (hi - lo > 1u) {
+        const uint32_t mid = lo + ((hi - lo) >> 1);
+        if (__fmul_rn(__uint_as_float(mid), m2beta) <= settled_x()) hi = mid;
+        else lo = mid;
+    }
+    return __uint_as_float(hi);
+}
+
+// Quiet bits (one per device slot and replica, in shared memory after the parity
+// words): bit i set = site i was quiet at its last visit (site_visit) and nothing
+// in its neighbourhood has changed since.  A staged phase visits only the sites
+// whose bit is clear; any change of a word clears the bits of the site and of its
+// neighbours.
+__host__ __device__ inline int quiet_words(int n) { return (n + 31) >> 5; }
+
+__device__ __forceinline__ void quiet_set(uint32_t* quiet, int i) { atomicOr(quiet + (i >> 5), 1u << (i & 31)); }
+
+__device__ __forceinline__ void quiet_clear(uint32_t* quiet, int i) { atomicAnd(quiet + (i >> 5), ~(1u << (i & 31))); }
+
+// After site i of one replica changed: its neighbours are no longer known to be quiet
+// (its own bit is clear: only sites with a clear bit are visited, and a world-line
+// move clears it itself).
+template <int MAXDEG>
+__device__ __forceinline__ void quiet_clear_neighbours(const Item& it, uint32_t* quiet, int i) {
+#pragma unroll
+    for (int m = 0; m < MAXDEG; ++m) {
+        if (m < it.maxdeg) {
+            const int j = __ldg(it.nbr + (int64_t)m * it.n + i);
+            if ((unsigned)j < (unsigned)it.n) quiet_clear(quiet, j);
+        }
+    }
 }
 
 // The per-slice local update of one site from slice class qq0 on (all classes when
@@ -361,12 +451,15 @@ __device__ __forceinline__ void site_update(const Item& it, const KS& ks, W* rw,
         const int q = nclass_q == 2 ? (qq ^ (int)first) : qq;
         W fl;
         if constexpr (SPLIT) {
+            bool calm = false;   // not used here
             const W own = update_fixed_half64<MAXDEG, KS>(wi, d, J, h, jp, q, half, (uint32_t)i, sweep, rep, ks,
-                                                         m2beta, m2blog2e);
+                                                         m2beta, m2blog2e, 0.0f, calm);
             nacc += __popcll((unsigned long long)own);
             fl = own | (W)__shfl_xor_sync(pair_mask, (unsigned long long)own, 1);
         } else if constexpr (NQC > 0) {
-            fl = update_fixed<NQC, MAXDEG, W, KS>(wi, d, J, h, jp, q, (uint32_t)i, sweep, rep, ks, m2beta, m2blog2e);
+            bool calm = false;   // not used here
+            fl = update_fixed<NQC, MAXDEG, W, KS>(wi, d, J, h, jp, q, (uint32_t)i, sweep, rep, ks, m2beta, m2blog2e,
+                                                  0.0f, calm);
         } else {
             W dl, dr;
             trotter_diffs<W>(wi, P, mask, dl, dr);
@@ -401,8 +494,29 @@ __device__ __forceinline__ void site_update(const Item& it, const KS& ks, W* rw,
     if (half == 0) rw[i] = wi;
 }
 
-// Queue of unsettled sites of one group: kQueuePerThread entries per thread of the
-// group in shared memory, and two phase counters (used alternately).
+// One queued site of replica r in phase p: visit it, then record what the visit
+// showed in the quiet bits.  fresh: the sweep visits every site and rewrites its
+// bit (the bits read before it are not trusted); otherwise the site's bit is clear.
+template <typename W, int MAXDEG, int NQC, typename KS, bool SPLIT>
+__device__ __forceinline__ void visit_queued(const Item& it, const KS& ks, W* sw, uint32_t* quiet, int nwq,
+                                             const uint32_t* parity, int p, int i, int r, bool fresh, float jp,
+                                             uint32_t sweep, float m2beta, float m2blog2e, float smin, int half,
+                                             unsigned pair_mask, bool& bad, unsigned long long& nacc) {
+    const int v = site_visit<W, MAXDEG, NQC, KS, SPLIT>(it, ks, sw + r * it.n, i, it.replica0 + r,
+                                                        (parity[r] >> p) & 1u, jp, sweep, m2beta, m2blog2e, smin,
+                                                        half, pair_mask, bad, nacc);
+    if (SPLIT && half != 0) return;
+    uint32_t* qr = quiet + r * nwq;
+    if (v == kVisitQuiet) {
+        quiet_set(qr, i);
+    } else {
+        if (fresh) quiet_clear(qr, i);
+        if (v == kVisitChanged) quiet_clear_neighbours<MAXDEG>(it, qr, i);
+    }
+}
+
+// Queue of the sites a phase visits, per group: kQueuePerThread entries per thread
+// of the group in shared memory, and two phase counters (used alternately).
 constexpr int kQueuePerThread = 2;
 
 struct SiteQueue {
@@ -410,19 +524,26 @@ struct SiteQueue {
     int* count;        // [2]
 };
 
+// The quiet bits of an item: after its parity words (item_smem_bytes).
+__device__ __forceinline__ uint32_t* item_quiet(uint32_t* parity, int nrep) {
+    return parity + ((((size_t)nrep * 4 + 15) & ~(size_t)15) >> 2);
+}
+
 // Anneal one item through its schedule.  sw: shared memory holding the item's
 // nrep x n words (staged by the caller); order: nrep x kMaxClasses bytes;
-// parity: nrep words; q: the group's queue.  Counts accepted local flips into
-// nacc and out-of-range indices into bad.
+// parity: nrep words, followed by the quiet bits; q: the group's queue.  Counts
+// accepted local flips into nacc and out-of-range indices into bad.
 //
-// Compile-time P (NQC > 0): each phase runs in two stages.  In stage A the
-// group walks the phase's sites and settles what site_settle can; the sites it
-// leaves are appended (warp-aggregated) to the group's queue as (slot, replica,
-// first unsettled slice class).  After a group barrier, stage B runs the
-// per-slice update on the queued sites, one per thread (lane pair), so the
-// per-slice work fills whole warps.  Sites of one phase share no coupling, so
-// which thread takes a site does not change any result; a site that finds the
-// queue full is updated at once by its own thread.
+// Compile-time P (NQC > 0): each phase runs in two stages.  The scan walks the
+// phase's sites and appends (warp-aggregated) those whose quiet bit is clear to
+// the group's queue as (slot, replica); after a group barrier, the visit stage
+// runs site_visit on the queued sites, one per thread (lane pair), so the
+// per-slice work fills whole warps.  A quiet site is skipped: site_visit would
+// reject both of its classes without drawing a uniform, so skipping it changes no
+// result.  The first sweep of the item, and of a schedule step whose J-perp or beta
+// is below the previous step's, visits every site and rewrites its bit.  Sites of one
+// phase share no coupling, so which thread takes a site does not change any
+// result; a site that finds the queue full is visited at once by its own thread.
 //
 // SPLIT (64-bit words with P = 64 only): two adjacent lanes share each site, one
 // 32-bit half of the world-line each, and exchange their flips after every slice
@@ -474,13 +595,26 @@ __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* s
     const uint32_t lanes_below = (1u << (SPLIT ? (lane & ~1u) : lane)) - 1u;
     const int qcap = kQueuePerThread * g.nthr;
     uint32_t phase = 0;   // running phase count: picks the phase's queue counter
+    uint32_t* const quiet = item_quiet(parity, nrep);
+    const int nwq = quiet_words(n);
     if (NQC > 0 && g.tid == 0) { q.count[0] = 0; q.count[1] = 0; }
     for (int gs = 0; gs < it.nsched; ++gs) {
         const float jp = P == 1 ? 0.0f : __ldg(it.jperp + gs);
         const float beta = it.betas ? __ldg(it.betas + gs) : it.beta;
         const float m2beta = __fmul_rn(-2.0f, beta);                          // exact
         const float m2blog2e = __fmul_rn(m2beta, 1.44269502162933349609375f);  // guard-band argument scale
+        const float smin = NQC > 0 && STAGED ? settle_threshold(m2beta) : 0.0f;
+        // quiet bits hold while J-perp and beta do not decrease (site_visit): the first
+        // sweep of the item, or of a step where either decreased, visits every site
+        // and rewrites its bit
+        bool renew = true;
+        if (gs > 0) {
+            const float jp_prev = P == 1 ? 0.0f : __ldg(it.jperp + gs - 1);
+            const float beta_prev = it.betas ? __ldg(it.betas + gs - 1) : it.beta;
+            renew = !(jp >= jp_prev && beta >= beta_prev && beta_prev > 0.0f);
+        }
         for (int step = 0; step < it.mcsteps; ++step) {
+            const bool fresh = renew && step == 0;
             const uint32_t sweep = (uint32_t)(it.sweep_base + (int64_t)gs * it.mcsteps + step);
             if (g.tid < nrep)
                 class_order<KS>(it.nclass, it.order_mode, ks, sweep, it.replica0 + g.tid,
@@ -503,21 +637,18 @@ __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* s
                 }
                 if constexpr (NQC > 0 && STAGED) {
                     int* cnt = q.count + (phase & 1u);
-                    // stage A: settle, queue the rest
+                    // scan: queue the sites whose quiet bit is clear
                     for (;;) {
                         const bool active = rl < nrep;
                         if (!__any_sync(0xffffffffu, active)) break;
                         bool pend = false;
                         uint32_t entry = 0;
-                        int site_i = 0, site_r = 0, site_qq = 2;
+                        int site_i = 0, site_r = 0;
                         if (active) {
                             site_i = cls * S + s;
                             site_r = rl;
-                            site_qq = site_settle<W, MAXDEG, NQC, SPLIT>(it, sw + rl * n, site_i,
-                                                                         (parity[rl] >> p) & 1u, jp, m2beta, half,
-                                                                         bad, nacc);
-                            pend = site_qq < 2;
-                            entry = (uint32_t)site_i | ((uint32_t)rl << 22) | ((uint32_t)site_qq << 30);
+                            pend = fresh || ((quiet[rl * nwq + (site_i >> 5)] >> (site_i & 31)) & 1u) == 0u;
+                            entry = (uint32_t)site_i | ((uint32_t)rl << 22);
                             s += site_nthr;
                             while (s >= cs) {
                                 s -= cs;
@@ -536,12 +667,11 @@ __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* s
                             if (pend) {
                                 if (slot < qcap) {
                                     if (half == 0) q.slots[slot] = entry;
-                                } else {   // queue full: update the site now
-                                    site_update<W, MAXDEG, NQC, KS, SPLIT>(it, ks, sw + site_r * n, site_i,
-                                                                           it.replica0 + site_r, site_qq,
-                                                                           (parity[site_r] >> p) & 1u, 2, jp, sweep,
-                                                                           m2beta, m2blog2e, mask, half, pair_mask,
-                                                                           bad, nacc);
+                                } else {   // queue full: visit the site now
+                                    visit_queued<W, MAXDEG, NQC, KS, SPLIT>(it, ks, sw, quiet, nwq, parity, p,
+                                                                            site_i, site_r, fresh, jp, sweep, m2beta,
+                                                                            m2blog2e, smin, half, pair_mask, bad,
+                                                                            nacc);
                                 }
                             }
                         }
@@ -549,14 +679,14 @@ __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* s
                     // the other counter's last reader finished before this phase began
                     if (g.tid == 0) q.count[(phase + 1u) & 1u] = 0;
                     group_sync(g);
-                    // stage B: the per-slice update of the queued sites, one per thread (lane pair)
+                    // visits of the queued sites, one per thread (lane pair)
                     const int nq = min(*cnt, qcap);
                     for (int e = site_tid; e < nq; e += site_nthr) {
                         const uint32_t en = q.slots[e];
-                        const int i = (int)(en & 0x3FFFFFu), r = (int)((en >> 22) & 0xFFu), qq0 = (int)(en >> 30);
-                        site_update<W, MAXDEG, NQC, KS, SPLIT>(it, ks, sw + r * n, i, it.replica0 + r, qq0,
-                                                               (parity[r] >> p) & 1u, 2, jp, sweep, m2beta,
-                                                               m2blog2e, mask, half, pair_mask, bad, nacc);
+                        visit_queued<W, MAXDEG, NQC, KS, SPLIT>(it, ks, sw, quiet, nwq, parity, p,
+                                                                (int)(en & 0x3FFFFFu), (int)((en >> 22) & 0xFFu),
+                                                                fresh, jp, sweep, m2beta, m2blog2e, smin, half,
+                                                                pair_mask, bad, nacc);
                     }
                     ++phase;
                 } else {
@@ -606,7 +736,13 @@ __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* s
                             pq_u32x4{(uint32_t)i, sweep, it.replica0 + rl,
                                      (uint32_t)((1u << 24) | ((uint32_t)gm << 16) | (uint32_t)cls)},
                             ks);
-                        if (decide(E, pq_u01(rnd.x), m2beta, m2blog2e)) rw[i] = wi ^ mask;
+                        if (decide(E, pq_u01(rnd.x), m2beta, m2blog2e)) {
+                            rw[i] = wi ^ mask;
+                            if constexpr (NQC > 0 && STAGED) {
+                                quiet_clear(quiet + rl * nwq, i);
+                                quiet_clear_neighbours<MAXDEG>(it, quiet + rl * nwq, i);
+                            }
+                        }
                     }
                     s += g.nthr;
                     while (s >= csz) { s -= csz; ++rl; }
@@ -672,11 +808,11 @@ __device__ inline void run_item_any(const Item& it, unsigned char* smem, const S
     }
 }
 
-// Shared memory one item needs (words + order bytes + parity words), 16-byte aligned.
+// Shared memory one item needs (words + order bytes + parity words + quiet bits), 16-byte aligned.
 __host__ __device__ inline size_t item_smem_bytes(int nrep, int n, int P) {
     const size_t wbytes = P <= 32 ? 4 : 8;
     return (((size_t)nrep * n * wbytes + 15) & ~(size_t)15) + (((size_t)nrep * kMaxClasses + 15) & ~(size_t)15) +
-           (((size_t)nrep * 4 + 15) & ~(size_t)15);
+           (((size_t)nrep * 4 + 15) & ~(size_t)15) + (((size_t)nrep * quiet_words(n) * 4 + 15) & ~(size_t)15);
 }
 
 }  // namespace pq

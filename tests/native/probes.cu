@@ -6,7 +6,9 @@
 //  * pqt_guard_band_probe: the largest relative deviation of the hardware 2^x from
 //    the sweep's own expf_neg over a range of FP32 arguments, the bound the
 //    packed sweep's exact guard band relies on.
-#include "common.cuh"
+//  * pqt_settle_threshold: the per-step threshold of the quiet-site rule of the
+//    packed sweep (pq::settle_threshold), for checking against FP32 arithmetic.
+#include "sweep_core.cuh"
 
 namespace {
 
@@ -39,9 +41,22 @@ __global__ void guard_probe_kernel(uint32_t first_bits, int64_t count, unsigned 
     if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(worst));
 }
 
+__global__ void settle_threshold_kernel(const float* betas, int count, float* out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < count) out[t] = pq::settle_threshold(__fmul_rn(-2.0f, betas[t]));
+}
+
 }  // namespace
 
 extern "C" {
+
+// The quiet-site threshold of each beta: the smallest s >= 0 with fl(s * -2 beta) <= -16.63553237915039.
+int pqt_settle_threshold(const float* betas, int count, float* out, void* stream) {
+    if (!betas || !out || count < 0) return PQ_ERR_INVALID_ARG;
+    if (count == 0) return PQ_OK;
+    settle_threshold_kernel<<<(count + 127) / 128, 128, 0, (cudaStream_t)stream>>>(betas, count, out);
+    return pq_launch_status();
+}
 
 // Diagnostic: checks the accuracy the packed sweep's guard band relies on.
 int pqt_guard_band_probe(uint32_t first_bits, int64_t count, unsigned long long* out, void* stream) {

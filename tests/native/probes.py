@@ -2,7 +2,8 @@
 
 The probes are not part of the product library: ``pqt_fp32_fma_probe`` gives the
 FP32 peak that the bench's roofline divides by, ``pqt_guard_band_probe`` the bound
-the packed sweep's exact decision relies on.  ``build()`` compiles them for sm_103a
+the packed sweep's exact decision relies on, ``pqt_settle_threshold`` the per-step
+threshold of its quiet-site rule.  ``build()`` compiles them for sm_103a
 (called by ``__graft_entry__.build()``); ``lib()`` loads them.
 """
 import ctypes
@@ -18,7 +19,8 @@ INCLUDE = os.path.join(ROOT, "include")
 
 
 def build(force=False):
-    deps = [SRC, os.path.join(CSRC, "common.cuh"), os.path.join(INCLUDE, "piqmc_gb300.h")]
+    deps = [SRC, os.path.join(CSRC, "common.cuh"), os.path.join(CSRC, "sweep_core.cuh"),
+            os.path.join(INCLUDE, "piqmc_gb300.h")]
     if not force and os.path.exists(OUT) and all(os.path.getmtime(OUT) >= os.path.getmtime(d) for d in deps):
         return OUT
     os.makedirs(os.path.dirname(OUT), exist_ok=True)
@@ -44,5 +46,7 @@ def lib():
         L.pqt_fp32_fma_probe.restype = I32
         L.pqt_guard_band_probe.argtypes = [U32, I64, V, V]
         L.pqt_guard_band_probe.restype = I32
+        L.pqt_settle_threshold.argtypes = [V, I32, V, V]
+        L.pqt_settle_threshold.restype = I32
         _lib = L
     return _lib

@@ -75,6 +75,42 @@ def test_fast_launch_shapes_do_not_change_results(threads, rpc):
     _run_both(prob, 16, 7, np.linspace(3.0, 1e-8, 8), 0.05, 1, seed=3, threads=threads, rpc=rpc)
 
 
+_UP_DOWN = np.concatenate([np.linspace(3.0, 0.2, 14), np.linspace(0.3, 1.5, 6), np.linspace(1.5, 1e-8, 20)])
+
+
+@pytest.mark.parametrize("P,sched,mcsteps,global_moves,threads,rpc", [
+    (20, np.linspace(3.0, 1e-8, 40), 1, 0, 32, 1),
+    (20, np.linspace(3.0, 1e-8, 40), 1, 0, 64, 2),
+    (16, np.linspace(3.0, 1e-8, 40), 2, 1, 32, 1),
+    (32, _UP_DOWN, 1, 0, 32, 1),
+    (20, _UP_DOWN, 2, 1, 64, 2),
+    (64, np.linspace(3.0, 1e-8, 30), 1, 1, 64, 2),
+])
+def test_fast_staged_phases_bit_exact(P, sched, mcsteps, global_moves, threads, rpc):
+    """Staged phases (scan, then visits of the queued sites) on a lattice large enough
+    for them, long enough that most sites are quiet (skipped: both slice classes
+    certain to reject) in the later sweeps.  A schedule whose J-perp goes down and up
+    again makes the kernel rewrite every quiet bit; world-line moves clear the bits
+    around a flipped world-line."""
+    from piqmc import fast, tools
+    g = np.random.default_rng(P + len(sched))
+    J = lattice(32, True, g, dist=lambda r: r.normal(), fields=lambda r: r.normal(0, 0.2))
+    prob = fast.Problem(tools.GenerateNeighbors(1024, J, 5))
+    assert rpc * prob.class_stride >= 2 * threads     # the staged variant runs
+    _run_both(prob, P, 4, sched, 0.05, mcsteps, seed=31 + P, global_moves=global_moves, threads=threads, rpc=rpc)
+
+
+def test_fast_staged_phases_with_rising_temperature():
+    """Per-step betas that fall mid-schedule: quiet bits are rewritten at that step."""
+    from piqmc import fast, tools
+    g = np.random.default_rng(12)
+    J = lattice(32, True, g, dist=lambda r: r.normal())
+    prob = fast.Problem(tools.GenerateNeighbors(1024, J, 4))
+    temps = np.concatenate([np.linspace(0.5, 0.02, 15), np.full(5, 0.3), np.linspace(0.3, 0.02, 15)])
+    betas = (np.float32(1.0) / temps.astype(np.float32)).astype(np.float32)
+    _run_both(prob, 20, 3, np.linspace(2.0, 1e-8, len(temps)), 0.05, 1, seed=6, betas=betas, threads=32, rpc=1)
+
+
 def test_fast_sa_betas():
     """P = 1 with a per-step inverse temperature: the packed classical annealer."""
     from piqmc import fast, tools
