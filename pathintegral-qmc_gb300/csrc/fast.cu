@@ -195,17 +195,15 @@ int launch_fast_t(void* words, const int32_t* nbr, const float* cpl, const float
 }
 
 template <typename W, int MAXDEG, int NQC>
-const void* fast_kernel_for(const FastArgs& a, int threads) {
-    if constexpr (NQC > 0)
-        if (staged_phase(NQC, a.rpc, a.stride, threads)) return (const void*)fast_kernel<W, MAXDEG, NQC, true>();
-    return (const void*)fast_kernel<W, MAXDEG, NQC, false>();
+const void* fast_kernel_for() {
+    return (const void*)fast_kernel<W, MAXDEG, NQC, staged_phase(NQC)>();
 }
 
 // Waves of CTAs a launch of `threads`-thread CTAs takes on this device (resident
 // CTAs per SM from the runtime's occupancy of the variant that would run).
 template <typename W, int MAXDEG, int NQC>
 int fast_waves(const FastArgs& a, int threads, int64_t* waves) {
-    const void* k = fast_kernel_for<W, MAXDEG, NQC>(a, threads);
+    const void* k = fast_kernel_for<W, MAXDEG, NQC>();
     PQ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
     int dev = 0, nsm = 0, per_sm = 0;
     PQ_CUDA_TRY(cudaGetDevice(&dev));
@@ -218,10 +216,9 @@ int fast_waves(const FastArgs& a, int threads, int64_t* waves) {
     return PQ_OK;
 }
 
-// Compile-time P: staged phases when a thread walks at least two sites per phase
-// (staged_phase).  With the thread count chosen automatically, CTAs of half the
-// size are taken when that runs the replicas in fewer waves (more CTAs resident
-// per SM): the last wave of a launch leaves SMs idle.
+// Compile-time P: staged phases (staged_phase).  With the thread count chosen
+// automatically, CTAs of half the size are taken when that runs the replicas in
+// fewer waves (more CTAs resident per SM): the last wave of a launch leaves SMs idle.
 template <typename W, int MAXDEG, int NQC>
 int launch_fast(void* words, const int32_t* nbr, const float* cpl, const float* field, const float* jperp,
                 const float* betas, const FastArgs& a, int threads, bool auto_threads, unsigned long long* accepts,
@@ -236,13 +233,8 @@ int launch_fast(void* words, const int32_t* nbr, const float* cpl, const float* 
         if (rc != PQ_OK) return rc;
         if (w_half < w_full) threads = half;
     }
-    if constexpr (NQC > 0) {
-        if (staged_phase(NQC, a.rpc, a.stride, threads))
-            return launch_fast_t<W, MAXDEG, NQC, true>(words, nbr, cpl, field, jperp, betas, a, threads, accepts,
-                                                       status, stream);
-    }
-    return launch_fast_t<W, MAXDEG, NQC, false>(words, nbr, cpl, field, jperp, betas, a, threads, accepts, status,
-                                                stream);
+    return launch_fast_t<W, MAXDEG, NQC, staged_phase(NQC)>(words, nbr, cpl, field, jperp, betas, a, threads,
+                                                            accepts, status, stream);
 }
 
 template <typename W>

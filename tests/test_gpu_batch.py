@@ -80,7 +80,8 @@ def test_batch_chunks_and_graph_replay():
 
 def test_batch_equals_the_oracle_directly():
     """Every instance of a batch against the packed sweep's CPU restatement, bit for bit
-    (not only through the single-instance kernel): staged and per-site items, P = 1..64."""
+    (not only through the single-instance kernel): staged items (compile-time P) and per-site
+    items (run-time P), P = 1..64."""
     import oracle
     from piqmc import batch, fast
     nbs, R, P, g = _instances(2)

@@ -40,8 +40,8 @@ def test_settle_threshold_is_exact():
                                                     _device.ptr(out), _device.stream_handle()), "probe")
     smin = out.cpu().numpy()
     X = np.array([0xc1851592], np.uint32).view(np.float32)[0]
-    m2b = (np.float32(-2.0) * betas).astype(np.float32)
     with np.errstate(over="ignore", invalid="ignore"):   # -2 beta overflows for beta = 3e38; 0 * -inf
+        m2b = (np.float32(-2.0) * betas).astype(np.float32)
         for b, m, s in zip(betas, m2b, smin):
             if not m < 0:
                 assert np.isinf(s) and s > 0, (b, s)
