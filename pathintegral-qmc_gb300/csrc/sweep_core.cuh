@@ -231,6 +231,58 @@ __device__ __forceinline__ W update_fixed(W wi, const W (&d)[DEG], const float (
     return flips << q;
 }
 
+// The share of lane t of L lanes (L a power of two) in update_fixed's work on slice
+// class q: the Philox blocks b = t, t + L, ... of the class (4 slices each), with the
+// same uniforms and arithmetic; the L lanes' flips together are update_fixed's.  Each
+// block's words are shifted once so that its slices sit at fixed bit positions.  One
+// block per loop pass: smaller code than update_fixed's unrolled classes (what the
+// batched kernel, with a variant per instance shape, wants).
+template <int NQ, int DEG, typename W, typename KS>
+__device__ __forceinline__ W update_part(W wi, const W (&d)[DEG], const float (&J)[DEG], float h, float jp, int q,
+                                         uint32_t i, uint32_t sweep, uint32_t rep, const KS& ks, float m2beta,
+                                         float m2blog2e, float smin, bool& calm, int t, int L) {
+    constexpr int P = 2 * NQ;
+    constexpr int NB = (NQ + 3) / 4;
+    constexpr int BITS = 8 * sizeof(W);
+    constexpr W MASK = P >= BITS ? ~(W)0 : (((W)1 << P) - 1);
+    const W up = ((wi << 1) | (wi >> (P - 1))) & MASK;
+    const W dn = ((wi >> 1) | (wi << (P - 1))) & MASK;
+    const W dlw = wi ^ up, drw = wi ^ dn;
+    W cm = 0;
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) cm |= (W)1 << (2 * k);
+    calm = calm && (dlw & drw & (cm << q)) == 0;
+    W flips = 0;
+#pragma unroll 1
+    for (int b = t; b < NB; b += L) {
+        const int sh = 8 * b + q;   // bit of the block's first slice
+        const uint32_t wq = (uint32_t)(wi >> sh), dl = (uint32_t)(dlw >> sh), dr = (uint32_t)(drw >> sh);
+        uint32_t dq[DEG];
+#pragma unroll
+        for (int m = 0; m < DEG; ++m) dq[m] = (uint32_t)(d[m] >> sh);
+        const int nv = NQ - 4 * b;   // slices of this block (4, or fewer in the last)
+        const pq_u32x4 rnd = pq_philox_ks(pq_u32x4{i, sweep, rep, (uint32_t)((q << 16) | b)}, ks);
+        const uint32_t rw4[4] = {rnd.x, rnd.y, rnd.z, rnd.w};
+        uint32_t f = 0;
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+            if (jj < nv) {
+                const int s2 = 31 - 2 * jj;  // bit 2 jj -> sign bit
+                float e = flip_sign(h, (wq << s2) & 0x80000000u);
+#pragma unroll
+                for (int m = 0; m < DEG; ++m) e = __fadd_rn(e, flip_sign(J[m], (dq[m] << s2) & 0x80000000u));
+                const float tt =
+                    __fadd_rn(flip_sign(jp, (dl << s2) & 0x80000000u), flip_sign(jp, (dr << s2) & 0x80000000u));
+                const float sum = __fadd_rn(e, tt);
+                calm = calm && sum >= smin;
+                if (decide(sum, pq_u01(rw4[jj]), m2beta, m2blog2e)) f |= 1u << (2 * jj);
+            }
+        }
+        flips |= (W)f << sh;
+    }
+    return flips;
+}
+
 // One 32-bit half (bits 32*half .. 32*half+31) of update_fixed<32, DEG, uint64_t>:
 // the same updates, uniforms and arithmetic for the slices of that half, so two
 // lanes that take one half each and combine their flips reproduce it exactly.
@@ -297,10 +349,14 @@ enum SiteVisit { kVisitKept = 0, kVisitQuiet = 1, kVisitChanged = 2 };
 // changed, J-perp has not decreased and beta has not decreased (each s only grows
 // with J-perp, and fl(s * -2 beta) only falls as s and beta grow).  kVisitChanged
 // when the site's word changed.
-template <typename W, int MAXDEG, int NQC, typename KS, bool SPLIT>
+//
+// Lanes: `part` of the `nparts` lanes of part_mask that visit the site together
+// (SPLIT: the lane pair, one 32-bit half each; COMPACT: a group of adjacent lanes
+// that share its Philox blocks, update_part); otherwise one lane (part 0).
+template <typename W, int MAXDEG, int NQC, typename KS, bool SPLIT, bool COMPACT>
 __device__ __forceinline__ int site_visit(const Item& it, const KS& ks, W* rw, int i, uint32_t rep, uint32_t first,
-                                          float jp, uint32_t sweep, float m2beta, float m2blog2e, float smin, int half,
-                                          unsigned pair_mask, bool& bad, unsigned long long& nacc) {
+                                          float jp, uint32_t sweep, float m2beta, float m2blog2e, float smin, int part,
+                                          int nparts, unsigned part_mask, bool& bad, unsigned long long& nacc) {
     static_assert(NQC > 0, "staged phases need a compile-time slice count");
     using CMk = ClassMasks<W, NQC>;
     constexpr int P = 2 * NQC;
@@ -338,7 +394,7 @@ __device__ __forceinline__ int site_visit(const Item& it, const KS& ks, W* rw, i
                 wi ^= fl | fl2;
 #pragma unroll
                 for (int m = 0; m < MAXDEG; ++m) d[m] ^= fl | fl2;
-                if (!SPLIT || half == 0)
+                if (part == 0)
                     nacc += sizeof(W) == 8 ? __popcll((unsigned long long)(fl | fl2)) : __popc((uint32_t)(fl | fl2));
             }
         } else {
@@ -363,7 +419,7 @@ __device__ __forceinline__ int site_visit(const Item& it, const KS& ks, W* rw, i
                 wi ^= fl;
 #pragma unroll
                 for (int m = 0; m < MAXDEG; ++m) d[m] ^= fl;
-                if (!SPLIT || half == 0)
+                if (part == 0)
                     nacc += sizeof(W) == 8 ? __popcll((unsigned long long)fl) : __popc((uint32_t)fl);
             }
         }
@@ -374,10 +430,15 @@ __device__ __forceinline__ int site_visit(const Item& it, const KS& ks, W* rw, i
         const int q = qq ^ (int)first;
         W fl;
         if constexpr (SPLIT) {
-            const W own = update_fixed_half64<MAXDEG, KS>(wi, d, J, h, jp, q, half, (uint32_t)i, sweep, rep, ks,
+            const W own = update_fixed_half64<MAXDEG, KS>(wi, d, J, h, jp, q, part, (uint32_t)i, sweep, rep, ks,
                                                          m2beta, m2blog2e, smin, calm);
             nacc += __popcll((unsigned long long)own);
-            fl = own | (W)__shfl_xor_sync(pair_mask, (unsigned long long)own, 1);
+            fl = own | (W)__shfl_xor_sync(part_mask, (unsigned long long)own, 1);
+        } else if constexpr (COMPACT) {
+            fl = update_part<NQC, MAXDEG, W, KS>(wi, d, J, h, jp, q, (uint32_t)i, sweep, rep, ks, m2beta, m2blog2e,
+                                                 smin, calm, part, nparts);
+            nacc += sizeof(W) == 8 ? __popcll((unsigned long long)fl) : __popc((uint32_t)fl);
+            for (int off = 1; off < nparts; off <<= 1) fl |= (W)__shfl_xor_sync(part_mask, fl, off);
         } else {
             fl = update_fixed<NQC, MAXDEG, W, KS>(wi, d, J, h, jp, q, (uint32_t)i, sweep, rep, ks, m2beta, m2blog2e,
                                                   smin, calm);
@@ -388,9 +449,9 @@ __device__ __forceinline__ int site_visit(const Item& it, const KS& ks, W* rw, i
 #pragma unroll
         for (int m = 0; m < MAXDEG; ++m) d[m] ^= fl;
     }
-    if constexpr (SPLIT) calm = __shfl_xor_sync(pair_mask, (int)calm, 1) != 0 && calm;
+    if (nparts > 1) calm = __all_sync(part_mask, calm);
     if (wi == w0) return calm ? kVisitQuiet : kVisitKept;
-    if (!SPLIT || half == 0) rw[i] = wi;
+    if (part == 0) rw[i] = wi;
     return kVisitChanged;
 }
 
@@ -494,18 +555,19 @@ __device__ __forceinline__ void site_update(const Item& it, const KS& ks, W* rw,
     if (half == 0) rw[i] = wi;
 }
 
-// One queued site of replica r in phase p: visit it, then record what the visit
-// showed in the quiet bits.  fresh: the sweep visits every site and rewrites its
+// One queued site of replica r in phase p: visit it (lane `part` of the `nparts`
+// lanes of part_mask that visit it, site_visit), then record what the visit showed
+// in the quiet bits.  fresh: the sweep visits every site and rewrites its
 // bit (the bits read before it are not trusted); otherwise the site's bit is clear.
-template <typename W, int MAXDEG, int NQC, typename KS, bool SPLIT>
+template <typename W, int MAXDEG, int NQC, typename KS, bool SPLIT, bool COMPACT>
 __device__ __forceinline__ void visit_queued(const Item& it, const KS& ks, W* sw, uint32_t* quiet, int nwq,
                                              const uint32_t* parity, int p, int i, int r, bool fresh, float jp,
-                                             uint32_t sweep, float m2beta, float m2blog2e, float smin, int half,
-                                             unsigned pair_mask, bool& bad, unsigned long long& nacc) {
-    const int v = site_visit<W, MAXDEG, NQC, KS, SPLIT>(it, ks, sw + r * it.n, i, it.replica0 + r,
-                                                        (parity[r] >> p) & 1u, jp, sweep, m2beta, m2blog2e, smin,
-                                                        half, pair_mask, bad, nacc);
-    if (SPLIT && half != 0) return;
+                                             uint32_t sweep, float m2beta, float m2blog2e, float smin, int part,
+                                             int nparts, unsigned part_mask, bool& bad, unsigned long long& nacc) {
+    const int v = site_visit<W, MAXDEG, NQC, KS, SPLIT, COMPACT>(it, ks, sw + r * it.n, i, it.replica0 + r,
+                                                                 (parity[r] >> p) & 1u, jp, sweep, m2beta, m2blog2e,
+                                                                 smin, part, nparts, part_mask, bad, nacc);
+    if (part != 0) return;
     uint32_t* qr = quiet + r * nwq;
     if (v == kVisitQuiet) {
         quiet_set(qr, i);
@@ -513,6 +575,13 @@ __device__ __forceinline__ void visit_queued(const Item& it, const KS& ks, W* sw
         if (fresh) quiet_clear(qr, i);
         if (v == kVisitChanged) quiet_clear_neighbours<MAXDEG>(it, qr, i);
     }
+}
+
+// Lanes that may share one visited site: the Philox blocks of a slice class (4
+// slices each), rounded up to a power of two, at most 4.
+template <int NQC>
+__host__ __device__ constexpr int kVisitLanes() {
+    return (NQC + 3) / 4 >= 3 ? 4 : ((NQC + 3) / 4 >= 2 ? 2 : 1);
 }
 
 // Queue of the sites a phase visits, per group: kQueuePerThread entries per thread
@@ -559,8 +628,12 @@ __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* s
 // per-site phases.
 __host__ __device__ constexpr bool staged_phase(int nqc) { return nqc > 0; }
 
-// The single-instance kernel inlines the item loop; the batched kernel calls one
-// out-of-line copy per variant, so each variant keeps its own register budget.
+// The single-instance kernel inlines the item loop (INLINE: visits with the
+// unrolled update_fixed); the batched kernel calls one out-of-line copy per variant,
+// so each variant keeps its own register budget, and visits with the compact
+// update_part (its many variants share the instruction cache; measured on GB300 the
+// 256-instance workload ran 4.0-4.3e11 updates/s with it against 3.5e11, while the
+// single-instance 80x80 kernel ran 202 ms per anneal unrolled against 228-370 ms).
 template <typename W, int MAXDEG, int NQC, bool STAGED>
 __device__ __forceinline__ void run_item(const Item& it, const PhiloxKeyTable& keys, W* sw, uint8_t* order,
                                          uint32_t* parity, const SiteQueue& q, const Group& g, bool& bad,
@@ -584,6 +657,8 @@ __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* s
     const W mask = full_mask<W>(P);
     const int nclass_q = P == 1 ? 1 : ((P & 1) ? 3 : 2);
     static_assert(!SPLIT || (sizeof(W) == 8 && NQC == 32), "lane pairs split 64-slice world-lines only");
+    // the batched kernel's out-of-line copies visit with update_part (compact code, lanes shared)
+    constexpr bool COMPACT = !INLINE && !SPLIT;
     // site walk of the local updates: one lane per site, or a lane pair per site
     const int site_tid = SPLIT ? g.tid >> 1 : g.tid;
     const int site_nthr = SPLIT ? g.nthr >> 1 : g.nthr;
@@ -667,10 +742,10 @@ __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* s
                                 if (slot < qcap) {
                                     if (half == 0) q.slots[slot] = entry;
                                 } else {   // queue full: visit the site now
-                                    visit_queued<W, MAXDEG, NQC, KS, SPLIT>(it, ks, sw, quiet, nwq, parity, p,
-                                                                            site_i, site_r, fresh, jp, sweep, m2beta,
-                                                                            m2blog2e, smin, half, pair_mask, bad,
-                                                                            nacc);
+                                    visit_queued<W, MAXDEG, NQC, KS, SPLIT, COMPACT>(
+                                        it, ks, sw, quiet, nwq, parity, p, site_i, site_r, fresh, jp, sweep, m2beta,
+                                        m2blog2e, smin, half, SPLIT ? 2 : 1, SPLIT ? pair_mask : (1u << lane), bad,
+                                        nacc);
                                 }
                             }
                         }
@@ -678,14 +753,23 @@ __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* s
                     // the other counter's last reader finished before this phase began
                     if (g.tid == 0) q.count[(phase + 1u) & 1u] = 0;
                     group_sync(g);
-                    // visits of the queued sites, one per thread (lane pair)
+                    // visits of the queued sites, one per thread (lane pair); with COMPACT
+                    // visits a short queue gives each site up to kVisitLanes adjacent lanes,
+                    // which share its Philox blocks
                     const int nq = min(*cnt, qcap);
-                    for (int e = site_tid; e < nq; e += site_nthr) {
+                    int nparts = 1;
+                    if constexpr (COMPACT) {
+                        while (nparts < kVisitLanes<NQC>() && nq * 2 * nparts <= site_nthr) nparts <<= 1;
+                    }
+                    const int part = SPLIT ? half : (site_tid & (nparts - 1));
+                    const unsigned part_mask =
+                        SPLIT ? pair_mask : ((0xFFFFFFFFu >> (32 - nparts)) << ((int)lane & ~(nparts - 1)));
+                    const int groups = site_nthr / nparts;
+                    for (int e = site_tid / nparts; e < nq; e += groups) {
                         const uint32_t en = q.slots[e];
-                        visit_queued<W, MAXDEG, NQC, KS, SPLIT>(it, ks, sw, quiet, nwq, parity, p,
-                                                                (int)(en & 0x3FFFFFu), (int)((en >> 22) & 0xFFu),
-                                                                fresh, jp, sweep, m2beta, m2blog2e, smin, half,
-                                                                pair_mask, bad, nacc);
+                        visit_queued<W, MAXDEG, NQC, KS, SPLIT, COMPACT>(
+                            it, ks, sw, quiet, nwq, parity, p, (int)(en & 0x3FFFFFu), (int)((en >> 22) & 0xFFu), fresh,
+                            jp, sweep, m2beta, m2blog2e, smin, part, SPLIT ? 2 : nparts, part_mask, bad, nacc);
                     }
                     ++phase;
                 } else {
