@@ -68,7 +68,9 @@ __global__ void __launch_bounds__(256, 2) batch_kernel(const pq_batch_task* __re
             const Group g{(int)threadIdx.x - gi * gthr, gthr,
                           (task.nitems == 1 && gthr == (int)blockDim.x) ? 0 : 1 + gi};
             run_task_item(bi, in, run, nbr_pool, cpl_pool, field_pool, csize_pool, jperp_pool, words_pool, smem,
-                          SiteQueue{queue_slots + kQueuePerThread * gi * gthr, queue_count + 2 * gi}, g,
+                          SiteQueue{queue_slots + kQueuePerThread * gi * gthr, queue_count + 2 * gi,
+                                    kQueuePerThread * gthr},
+                          g,
                           task.lanes_per_site, bad, nacc);
         }
         __syncthreads();

@@ -18,8 +18,25 @@ struct FastArgs {
     int64_t sweep_base;
     int replica_base;
     int rpc;  // replicas per CTA
+    int qcap; // site-queue entries per CTA (fast_queue_cap)
     PhiloxKeyTable keys;  // round keys of (key0, key1), read as constant operands
 };
+
+// Shared-memory budget of one CTA of the packed sweep.
+constexpr size_t kSmemBudget = 200 * 1024;
+
+// Site-queue entries of a CTA: a whole phase when the budget allows (the word scan
+// then runs each phase in one chunk), else kQueuePerThread per thread.
+inline int fast_queue_cap(int rpc, int n, int P, int stride, int threads) {
+    const int whole = whole_phase_queue(threads, rpc, stride);
+    if (item_smem_bytes(rpc, n, P) + (size_t)whole * 4 + 16 <= kSmemBudget) return whole;
+    return kQueuePerThread * threads;
+}
+
+// Dynamic shared memory of one CTA: the item, the site queue, its two counters.
+inline size_t fast_smem_bytes(int rpc, int n, int P, int stride, int threads) {
+    return item_smem_bytes(rpc, n, P) + (size_t)fast_queue_cap(rpc, n, P, stride, threads) * 4 + 16;
+}
 
 // One CTA's replicas through the schedule (the body of both kernels below).
 template <typename W, int MAXDEG, int NQC, bool STAGED>
@@ -30,9 +47,10 @@ __device__ __forceinline__ void fast_cta(W* __restrict__ words, const int32_t* _
                                          int32_t* __restrict__ status) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int csize[kMaxClasses];
-    // the sites a phase visits: kQueuePerThread slots per thread and two counters, after the item
+    // the sites a phase visits (fast_queue_cap entries) and two counters, after the item
+    const int qcap = a.qcap;
     uint32_t* queue_slots = reinterpret_cast<uint32_t*>(smem_raw + item_smem_bytes(a.rpc, a.n, a.P));
-    int* queue_count = reinterpret_cast<int*>(queue_slots + kQueuePerThread * blockDim.x);
+    int* queue_count = reinterpret_cast<int*>(queue_slots + qcap);
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int c = 0; c < kMaxClasses; ++c) csize[c] = a.class_size[c];
@@ -55,7 +73,7 @@ __device__ __forceinline__ void fast_cta(W* __restrict__ words, const int32_t* _
     bool bad = false;
     unsigned long long nacc = 0;
     stage_in<W>(it, sw, g);   // also publishes csize
-    run_item<W, MAXDEG, NQC, STAGED>(it, a.keys, sw, order, parity, SiteQueue{queue_slots, queue_count}, g, bad,
+    run_item<W, MAXDEG, NQC, STAGED>(it, a.keys, sw, order, parity, SiteQueue{queue_slots, queue_count, qcap}, g, bad,
                                      nacc);
     stage_out<W>(it, sw, g);
     if (bad) pq_set_status(status, PQ_ERR_BAD_INDEX);
@@ -184,13 +202,15 @@ template <typename W, int MAXDEG, int NQC, bool STAGED>
 int launch_fast_t(void* words, const int32_t* nbr, const float* cpl, const float* field, const float* jperp,
                   const float* betas, const FastArgs& a, int threads, unsigned long long* accepts, int32_t* status,
                   cudaStream_t stream) {
-    const size_t smem = item_smem_bytes(a.rpc, a.n, a.P) + (size_t)kQueuePerThread * threads * 4 + 16;
+    const size_t smem = fast_smem_bytes(a.rpc, a.n, a.P, a.stride, threads);
     static PqSmemAttr attr;
     const auto kernel = fast_kernel<W, MAXDEG, NQC, STAGED>();
     const int rc = pq_set_smem_limit(attr, (const void*)kernel, 220 * 1024);
     if (rc != PQ_OK) return rc;
     const int grid = (a.R + a.rpc - 1) / a.rpc;
-    kernel<<<grid, threads, smem, stream>>>((W*)words, nbr, cpl, field, jperp, betas, a, accepts, status);
+    FastArgs la = a;
+    la.qcap = fast_queue_cap(a.rpc, a.n, a.P, a.stride, threads);
+    kernel<<<grid, threads, smem, stream>>>((W*)words, nbr, cpl, field, jperp, betas, la, accepts, status);
     return pq_launch_status();
 }
 
@@ -208,7 +228,7 @@ int fast_waves(const FastArgs& a, int threads, int64_t* waves) {
     int dev = 0, nsm = 0, per_sm = 0;
     PQ_CUDA_TRY(cudaGetDevice(&dev));
     PQ_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    const size_t smem = item_smem_bytes(a.rpc, a.n, a.P) + (size_t)kQueuePerThread * threads * 4 + 16;
+    const size_t smem = fast_smem_bytes(a.rpc, a.n, a.P, a.stride, threads);
     PQ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem));
     const int64_t slots = (int64_t)nsm * (per_sm > 0 ? per_sm : 1);
     const int64_t grid = (a.R + a.rpc - 1) / a.rpc;
@@ -264,9 +284,6 @@ int dispatch_deg(void* words, const int32_t* nbr, const float* cpl, const float*
 
 extern "C" {
 
-// Shared-memory budget of one CTA of the packed sweep.
-static const size_t kSmemBudget = 200 * 1024;
-
 int pq_qa_fast_ex(void* words, const int32_t* nbr, const float* cpl, const float* field, const float* jperp,
                   const float* betas, const pq_fast_params* prm, unsigned long long* accepts, int32_t* status,
                   void* stream) {
@@ -315,7 +332,7 @@ int pq_qa_fast_ex(void* words, const int32_t* nbr, const float* cpl, const float
         if (!threads) threads = items >= 256 ? 256 : ((items + 31) / 32) * 32;
     }
     if (threads % 32 || threads > 512 || threads < rpc) return PQ_ERR_INVALID_ARG;
-    if (item_smem_bytes(rpc, p.n, p.P) + (size_t)kQueuePerThread * threads * 4 + 16 > kSmemBudget)
+    if (fast_smem_bytes(rpc, p.n, p.P, p.class_stride, threads) > kSmemBudget)
         return PQ_ERR_TOO_LARGE;
     a.rpc = rpc;
     cudaStream_t st = (cudaStream_t)stream;

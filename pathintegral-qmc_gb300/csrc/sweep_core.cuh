@@ -589,9 +589,19 @@ __host__ __device__ constexpr int kVisitLanes() {
 constexpr int kQueuePerThread = 2;
 
 struct SiteQueue {
-    uint32_t* slots;   // kQueuePerThread * group threads entries
+    uint32_t* slots;   // cap entries
     int* count;        // [2]
+    int cap;           // entries of slots
 };
+
+// Queue entries that hold every site of a phase (rounded up to whole 32-site words per
+// replica), at least kQueuePerThread per thread: what the single-instance kernel
+// takes when its shared memory allows, so that its word scan runs a phase in one chunk.
+__host__ __device__ inline int whole_phase_queue(int threads, int rpc, int stride) {
+    const int64_t phase = (int64_t)rpc * (((int64_t)stride + 31) / 32 + 1) * 32;
+    const int64_t per_thread = (int64_t)kQueuePerThread * threads;
+    return (int)(phase > per_thread ? phase : per_thread);
+}
 
 // The quiet bits of an item: after its parity words (item_smem_bytes).
 __device__ __forceinline__ uint32_t* item_quiet(uint32_t* parity, int nrep) {
@@ -667,7 +677,7 @@ __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* s
     const uint32_t lane = (uint32_t)(g.tid & 31);
     // queue rank below this site: lanes below this lane (below the pair's first lane for SPLIT)
     const uint32_t lanes_below = (1u << (SPLIT ? (lane & ~1u) : lane)) - 1u;
-    const int qcap = kQueuePerThread * g.nthr;
+    const int qcap = q.cap;
     uint32_t phase = 0;   // running phase count: picks the phase's queue counter
     uint32_t* const quiet = item_quiet(parity, nrep);
     const int nwq = quiet_words(n);
@@ -709,7 +719,93 @@ __device__ __forceinline__ void run_item_body(const Item& it, const KS& ks, W* s
                     cls = order[rl * kMaxClasses + p];
                     cs = it.csize[cls];
                 }
-                if constexpr (NQC > 0 && STAGED) {
+                if constexpr (NQC > 0 && STAGED && INLINE) {
+                    // scan by words (single-instance kernel): each lane takes one 32-site
+                    // word of a replica's class range, and the warp queues the word's sites
+                    // whose quiet bit is clear.  The phase's words go in chunks the queue
+                    // can hold whole (one chunk when it holds every site of a phase), each
+                    // chunk scanned, then visited: sites of one phase are independent.
+                    int nwords = 0;
+                    for (int r = 0; r < nrep; ++r) {
+                        const int c2 = order[r * kMaxClasses + p], b2 = c2 * S, n2 = it.csize[c2];
+                        nwords += n2 > 0 ? ((b2 + n2 - 1) >> 5) - (b2 >> 5) + 1 : 0;
+                    }
+                    const int chunk = qcap >> 5;
+                    for (int c0 = 0; c0 < nwords; c0 += chunk) {
+                        int* cnt = q.count + (phase & 1u);
+                        const int c1 = min(nwords, c0 + chunk);
+                        // this thread's first word of the chunk: replica wr, word wo of its range
+                        int wr = 0, wo = c0 + site_tid;
+                        int wb = order[p] * S, wcs = it.csize[order[p]];
+                        int wn = wcs > 0 ? ((wb + wcs - 1) >> 5) - (wb >> 5) + 1 : 0;
+                        int wi = c0 + site_tid;   // flattened word index
+                        while (wo >= wn) {
+                            wo -= wn;
+                            if (++wr == nrep) break;
+                            const int c2 = order[wr * kMaxClasses + p];
+                            wb = c2 * S;
+                            wcs = it.csize[c2];
+                            wn = wcs > 0 ? ((wb + wcs - 1) >> 5) - (wb >> 5) + 1 : 0;
+                        }
+                        for (;;) {
+                            const bool active = wi < c1;
+                            if (!__any_sync(0xffffffffu, active)) break;
+                            uint32_t bits = 0;
+                            int w = 0;
+                            if (active) {
+                                w = (wb >> 5) + wo;
+                                const int lo = wb - 32 * w;          // > 0 only in the range's first word
+                                const int hi = wb + wcs - 32 * w;    // < 32 only in its last word (>= 1)
+                                uint32_t m = lo > 0 ? (0xFFFFFFFFu << lo) : 0xFFFFFFFFu;
+                                if (hi < 32) m &= (1u << hi) - 1u;
+                                bits = (fresh ? 0xFFFFFFFFu : ~quiet[wr * nwq + w]) & m;
+                            }
+                            const int c = __popc(bits);
+                            int incl = c;
+#pragma unroll
+                            for (int off = 1; off < 32; off <<= 1) {
+                                const int t = __shfl_up_sync(0xffffffffu, incl, off);
+                                if ((int)lane >= off) incl += t;
+                            }
+                            const int tot = __shfl_sync(0xffffffffu, incl, 31);
+                            int base = 0;
+                            if (lane == 31 && tot) base = atomicAdd(cnt, tot);
+                            base = __shfl_sync(0xffffffffu, base, 31);
+                            int pos = base + incl - c;   // < qcap: a chunk holds at most qcap sites
+                            const uint32_t rtag = (uint32_t)wr << 22;
+                            while (bits) {
+                                const int bpos = __ffs(bits) - 1;
+                                bits &= bits - 1u;
+                                q.slots[pos++] = (uint32_t)(32 * w + bpos) | rtag;
+                            }
+                            if (active) {
+                                wi += site_nthr;
+                                wo += site_nthr;
+                                while (wo >= wn) {
+                                    wo -= wn;
+                                    if (++wr == nrep) break;
+                                    const int c2 = order[wr * kMaxClasses + p];
+                                    wb = c2 * S;
+                                    wcs = it.csize[c2];
+                                    wn = wcs > 0 ? ((wb + wcs - 1) >> 5) - (wb >> 5) + 1 : 0;
+                                }
+                            }
+                        }
+                        // the other counter's last reader finished before this chunk began
+                        if (g.tid == 0) q.count[(phase + 1u) & 1u] = 0;
+                        group_sync(g);
+                        // visits of the queued sites, one per thread
+                        const int nq = *cnt;
+                        for (int e = site_tid; e < nq; e += site_nthr) {
+                            const uint32_t en = q.slots[e];
+                            visit_queued<W, MAXDEG, NQC, KS, SPLIT, false>(
+                                it, ks, sw, quiet, nwq, parity, p, (int)(en & 0x3FFFFFu), (int)((en >> 22) & 0xFFu),
+                                fresh, jp, sweep, m2beta, m2blog2e, smin, 0, 1, 1u << lane, bad, nacc);
+                        }
+                        ++phase;
+                        if (c1 < nwords) group_sync(g);   // the next chunk reuses the queue
+                    }
+                } else if constexpr (NQC > 0 && STAGED) {
                     int* cnt = q.count + (phase & 1u);
                     // scan: queue the sites whose quiet bit is clear
                     for (;;) {

@@ -100,6 +100,21 @@ def test_fast_staged_phases_bit_exact(P, sched, mcsteps, global_moves, threads, 
     _run_both(prob, P, 4, sched, 0.05, mcsteps, seed=31 + P, global_moves=global_moves, threads=threads, rpc=rpc)
 
 
+def test_fast_staged_phases_in_chunks():
+    """A 220 x 220 lattice with 128-thread CTAs: a queue that holds a whole phase would pass
+    the shared-memory budget, so the scan goes through each phase in chunks of words the
+    smaller queue holds (about twelve per phase), each scanned and then visited."""
+    from piqmc import fast, tools
+    g = np.random.default_rng(220)
+    L = 220
+    J = lattice(L, True, g, dist=lambda r: r.normal(), fields=lambda r: r.normal(0, 0.2))
+    prob = fast.Problem(tools.GenerateNeighbors(L * L, J, 5))
+    assert prob.maxdeg == 4
+    words_kb = prob.nslots * 4 / 1024
+    assert words_kb + ((prob.class_stride + 31) // 32 + 1) * 32 * 4 / 1024 > 200 > words_kb + 2   # chunked
+    _run_both(prob, 16, 2, np.linspace(3.0, 1e-8, 6), 0.05, 1, seed=220, threads=128, rpc=1)
+
+
 def test_fast_staged_phases_with_rising_temperature():
     """Per-step betas that fall mid-schedule: quiet bits are rewritten at that step."""
     from piqmc import fast, tools

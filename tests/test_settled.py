@@ -1,4 +1,4 @@
-"""The settled-decision rule of the packed sweeps (csrc/sweep_core.cuh, site_settle).
+"""The settled-decision rule of the packed sweeps (csrc/sweep_core.cuh, site_visit and the quiet sites).
 
 The packed sweep settles an update without its uniform when sum < 0 (flip) or when
 fl(sum * -2 beta) <= -16.63553237915039 (reject).  The second rule is exact only
