@@ -613,16 +613,20 @@ __device__ __forceinline__ uint32_t* item_quiet(uint32_t* parity, int nrep) {
 // parity: nrep words, followed by the quiet bits; q: the group's queue.  Counts
 // accepted local flips into nacc and out-of-range indices into bad.
 //
-// Compile-time P (NQC > 0): each phase runs in two stages.  The scan walks the
-// phase's sites and appends (warp-aggregated) those whose quiet bit is clear to
-// the group's queue as (slot, replica); after a group barrier, the visit stage
-// runs site_visit on the queued sites, one per thread (lane pair), so the
-// per-slice work fills whole warps.  A quiet site is skipped: site_visit would
-// reject both of its classes without drawing a uniform, so skipping it changes no
-// result.  The first sweep of the item, and of a schedule step whose J-perp or beta
-// is below the previous step's, visits every site and rewrites its bit.  Sites of one
-// phase share no coupling, so which thread takes a site does not change any
-// result; a site that finds the queue full is visited at once by its own thread.
+// Compile-time P (NQC > 0): each phase runs in two stages.  The scan appends
+// (warp-aggregated) the phase's sites whose quiet bit is clear to the group's queue
+// as (slot, replica); after a group barrier, the visit stage runs site_visit on the
+// queued sites, one per thread (lane pair), so the per-slice work fills whole warps.
+// A quiet site is skipped: site_visit would reject both of its classes without
+// drawing a uniform, so skipping it changes no result.  The first sweep of the item,
+// and of a schedule step whose J-perp or beta is below the previous step's, visits
+// every site and rewrites its bit.  Sites of one phase share no coupling, so which
+// thread takes a site, and in which chunk, does not change any result.
+//
+// The single-instance kernel (INLINE) scans a 32-site word of quiet bits per lane
+// into a queue that holds a whole phase (in chunks of words when it cannot); the
+// batched kernel's items walk their sites one per lane, and a site that finds the
+// small per-group queue full is visited at once by its own thread.
 //
 // SPLIT (64-bit words with P = 64 only): two adjacent lanes share each site, one
 // 32-bit half of the world-line each, and exchange their flips after every slice
