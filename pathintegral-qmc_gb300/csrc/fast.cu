@@ -261,14 +261,25 @@ template <typename W>
 int dispatch_deg(void* words, const int32_t* nbr, const float* cpl, const float* field, const float* jperp,
                  const float* betas, const FastArgs& a, int threads, bool auto_threads, unsigned long long* accepts,
                  int32_t* status, cudaStream_t stream) {
-    // compile-time slice counts for the common even P with exactly four couplings
-    if (a.maxdeg == 4) {
+    // compile-time slice counts (staged phases, quiet sites) for the common even P and up
+    // to eight couplings; a degree below the variant's adds +0 terms, which can change
+    // only the sign of a zero sum and no decision
+    if (a.maxdeg <= 8) {
+        const bool four = a.maxdeg <= 4;
         if constexpr (sizeof(W) == 4) {
-            if (a.P == 20) return launch_fast<W, 4, 10>(words, nbr, cpl, field, jperp, betas, a, threads, auto_threads, accepts, status, stream);
-            if (a.P == 16) return launch_fast<W, 4, 8>(words, nbr, cpl, field, jperp, betas, a, threads, auto_threads, accepts, status, stream);
-            if (a.P == 32) return launch_fast<W, 4, 16>(words, nbr, cpl, field, jperp, betas, a, threads, auto_threads, accepts, status, stream);
+            if (a.P == 20)
+                return four ? launch_fast<W, 4, 10>(words, nbr, cpl, field, jperp, betas, a, threads, auto_threads, accepts, status, stream)
+                            : launch_fast<W, 8, 10>(words, nbr, cpl, field, jperp, betas, a, threads, auto_threads, accepts, status, stream);
+            if (a.P == 16)
+                return four ? launch_fast<W, 4, 8>(words, nbr, cpl, field, jperp, betas, a, threads, auto_threads, accepts, status, stream)
+                            : launch_fast<W, 8, 8>(words, nbr, cpl, field, jperp, betas, a, threads, auto_threads, accepts, status, stream);
+            if (a.P == 32)
+                return four ? launch_fast<W, 4, 16>(words, nbr, cpl, field, jperp, betas, a, threads, auto_threads, accepts, status, stream)
+                            : launch_fast<W, 8, 16>(words, nbr, cpl, field, jperp, betas, a, threads, auto_threads, accepts, status, stream);
         } else {
-            if (a.P == 64) return launch_fast<W, 4, 32>(words, nbr, cpl, field, jperp, betas, a, threads, auto_threads, accepts, status, stream);
+            if (a.P == 64)
+                return four ? launch_fast<W, 4, 32>(words, nbr, cpl, field, jperp, betas, a, threads, auto_threads, accepts, status, stream)
+                            : launch_fast<W, 8, 32>(words, nbr, cpl, field, jperp, betas, a, threads, auto_threads, accepts, status, stream);
         }
     }
     if (a.maxdeg <= 4)

@@ -100,6 +100,57 @@ def test_fast_staged_phases_bit_exact(P, sched, mcsteps, global_moves, threads, 
     _run_both(prob, P, 4, sched, 0.05, mcsteps, seed=31 + P, global_moves=global_moves, threads=threads, rpc=rpc)
 
 
+def _graph(kind, g):
+    """Coupling graphs of other degrees: a ring, random graphs, a periodic King's graph (8)."""
+    import scipy.sparse as sps
+    if kind == "ring":
+        n = 300
+        J = sps.dok_matrix((n, n))
+        for i in range(n):
+            J[i, (i + 1) % n] = g.normal()
+    elif kind.startswith("random"):
+        dmax = int(kind[6:])
+        n = 400
+        J = sps.dok_matrix((n, n))
+        deg = np.zeros(n, int)
+        for _ in range(n * dmax // 2):
+            a, b = sorted(g.choice(n - 1, 2, replace=False))     # spin n - 1 stays isolated
+            if deg[a] < dmax and deg[b] < dmax and (a, b) not in J:
+                J[int(a), int(b)] = g.normal()
+                deg[a] += 1
+                deg[b] += 1
+    else:   # King's graph, 20 x 20 torus
+        L = 20
+        n = L * L
+        J = sps.dok_matrix((n, n))
+        for y in range(L):
+            for x in range(L):
+                i = y * L + x
+                for dx, dy in ((1, 0), (0, 1), (1, 1), (1, -1)):
+                    j = ((y + dy) % L) * L + (x + dx) % L
+                    a, b = min(i, j), max(i, j)
+                    J[a, b] = g.normal()
+    for i in range(n):                                  # fields, a third of them zero
+        if g.random() < 2 / 3:
+            J[i, i] = g.normal(0, 0.3)
+    return J
+
+
+@pytest.mark.parametrize("kind,P", [("ring", 20), ("random3", 16), ("random6", 20), ("random6", 64),
+                                    ("random8", 32), ("kings", 20), ("kings", 64)])
+def test_fast_staged_phases_other_degrees(kind, P):
+    """Degrees up to four take the four-coupling variants, five to eight the eight-coupling
+    ones: the padded terms add +0, which changes no decision (an isolated spin with no field
+    has a zero energy sum)."""
+    from piqmc import fast, tools
+    g = np.random.default_rng(len(kind) * 100 + P)
+    J = _graph(kind, g)
+    n = J.shape[0]
+    prob = fast.Problem(tools.GenerateNeighbors(n, J, 9))
+    assert prob.maxdeg <= 8
+    _run_both(prob, P, 3, np.linspace(3.0, 1e-8, 30), 0.05, 1, seed=P + n, global_moves=1, threads=64, rpc=1)
+
+
 def test_fast_staged_phases_in_chunks():
     """A 220 x 220 lattice with 128-thread CTAs: a queue that holds a whole phase would pass
     the shared-memory budget, so the scan goes through each phase in chunks of words the
