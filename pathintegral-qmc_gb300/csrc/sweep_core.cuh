@@ -962,7 +962,8 @@ __device__ __forceinline__ void run_item_pick(const Item& it, W* sw, uint8_t* or
         run_item_call<W, MAXDEG, NQC, SPLIT, false>(it, sw, order, parity, q, g, bad, nacc);
 }
 
-// Word type / degree / compile-time P dispatch of one item.
+// Word type / degree / compile-time P dispatch of one item (any degree up to four takes
+// the four-coupling variants: the padded terms add +0 and change no decision).
 __device__ inline void run_item_any(const Item& it, unsigned char* smem, const SiteQueue& q, const Group& g, bool& bad,
                                     unsigned long long& nacc, int lanes_per_site = 1) {
     // layout of the item's shared memory: words, then order bytes, then parity words
@@ -973,18 +974,18 @@ __device__ inline void run_item_any(const Item& it, unsigned char* smem, const S
     if (it.P <= 32) {
         uint32_t* sw = reinterpret_cast<uint32_t*>(smem);
         stage_in<uint32_t>(it, sw, g);
-        if (it.maxdeg == 4 && it.P == 20) run_item_pick<uint32_t, 4, 10>(it, sw, order, parity, q, g, bad, nacc);
-        else if (it.maxdeg == 4 && it.P == 16) run_item_pick<uint32_t, 4, 8>(it, sw, order, parity, q, g, bad, nacc);
-        else if (it.maxdeg == 4 && it.P == 32) run_item_pick<uint32_t, 4, 16>(it, sw, order, parity, q, g, bad, nacc);
+        if (it.maxdeg <= 4 && it.P == 20) run_item_pick<uint32_t, 4, 10>(it, sw, order, parity, q, g, bad, nacc);
+        else if (it.maxdeg <= 4 && it.P == 16) run_item_pick<uint32_t, 4, 8>(it, sw, order, parity, q, g, bad, nacc);
+        else if (it.maxdeg <= 4 && it.P == 32) run_item_pick<uint32_t, 4, 16>(it, sw, order, parity, q, g, bad, nacc);
         else if (it.maxdeg <= 4) run_item_call<uint32_t, 4, 0>(it, sw, order, parity, q, g, bad, nacc);
         else run_item_call<uint32_t, 8, 0>(it, sw, order, parity, q, g, bad, nacc);
         stage_out<uint32_t>(it, sw, g);
     } else {
         uint64_t* sw = reinterpret_cast<uint64_t*>(smem);
         stage_in<uint64_t>(it, sw, g);
-        if (it.maxdeg == 4 && it.P == 64 && lanes_per_site == 2)
+        if (it.maxdeg <= 4 && it.P == 64 && lanes_per_site == 2)
             run_item_pick<uint64_t, 4, 32, true>(it, sw, order, parity, q, g, bad, nacc);
-        else if (it.maxdeg == 4 && it.P == 64) run_item_pick<uint64_t, 4, 32>(it, sw, order, parity, q, g, bad, nacc);
+        else if (it.maxdeg <= 4 && it.P == 64) run_item_pick<uint64_t, 4, 32>(it, sw, order, parity, q, g, bad, nacc);
         else if (it.maxdeg <= 4) run_item_call<uint64_t, 4, 0>(it, sw, order, parity, q, g, bad, nacc);
         else run_item_call<uint64_t, 8, 0>(it, sw, order, parity, q, g, bad, nacc);
         stage_out<uint64_t>(it, sw, g);

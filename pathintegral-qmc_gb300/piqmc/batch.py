@@ -58,8 +58,8 @@ def heuristic_tile(nslots, P, R):
 
 
 def lane_pairs_supported(problem, P):
-    """Items of this instance can give each site a lane pair (64-slice world-lines, 4 couplings)."""
-    return P == 64 and problem.maxdeg == 4
+    """Items of this instance can give each site a lane pair (64-slice world-lines, up to 4 couplings)."""
+    return P == 64 and problem.maxdeg <= 4
 
 
 def normalise_tile(tile, problem, P):

@@ -19,6 +19,14 @@ def _instances(seed=0):
         nbs.append(tools.GenerateNeighbors(L * L, J, 5 if L % 2 else 4))
         R.append(r)
         P.append(p)
+    import scipy.sparse as sps
+    for n, p, r in ((60, 20, 3), (40, 64, 2)):      # rings: two couplings per spin
+        J = sps.dok_matrix((n, n))
+        for i in range(n):
+            J[i, (i + 1) % n] = g.normal()
+        nbs.append(tools.GenerateNeighbors(n, J, 2))
+        R.append(r)
+        P.append(p)
     return nbs, R, P, g
 
 
@@ -41,11 +49,11 @@ def test_batch_equals_single(tiles):
     spins = [np.where(g.random((r, nb.shape[0], p)) < 0.5, -1, 1).astype(np.int8) for nb, r, p in zip(nbs, R, P)]
     t = None
     if tiles == "mixed":
-        t = [(1, 1), (2, 2), (1, 8), (4, 1), (1, 3), (2, 1), (8, 1), (1, 2), (1, 4), (2, 2)]
+        t = [(1, 1), (2, 2), (1, 8), (4, 1), (1, 3), (2, 1), (8, 1), (1, 2), (1, 4), (2, 2), (1, 3), (2, 2)]
     elif tiles == "lane_pairs":
-        # the two 64-slice instances take lane pairs (the others fall back to one lane per site)
+        # the 64-slice instances take lane pairs (the others fall back to one lane per site)
         t = [(1, 1, 2), (2, 2, 2), (1, 8, 2), (4, 1, 2), (1, 3, 2), (1, 1, 2), (8, 1, 2), (1, 2, 2), (1, 4, 2),
-             (2, 2, 2)]
+             (2, 2, 2), (1, 3, 2), (1, 2, 2)]
     B = batch.Batch(nbs, R, P, tiles=t)
     if tiles == "lane_pairs":
         assert [tl[2] for tl in B.tiles] == [2 if p == 64 else 1 for p in P]
