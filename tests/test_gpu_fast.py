@@ -151,6 +151,34 @@ def test_fast_staged_phases_other_degrees(kind, P):
     _run_both(prob, P, 3, np.linspace(3.0, 1e-8, 30), 0.05, 1, seed=P + n, global_moves=1, threads=64, rpc=1)
 
 
+def test_benchmark_workload_bit_exact_at_full_length():
+    """The benchmark's own workload -- its seeded 80 x 80 instance, straight starts, key and
+    the whole 2000-step schedule, P = 20, 1024 replicas in one launch -- equals the
+    oracle bit for bit on the first and the last replica (about 15 s of oracle each)."""
+    import bench
+    from piqmc import fast, tools
+    import scipy.sparse as sps
+    n, P, R = bench.L_SIDE * bench.L_SIDE, bench.P_SLICES, bench.REPLICAS
+    rows, cols, vals = bench.instance_arrays()
+    J = sps.dok_matrix((n, n))
+    for a, b, v in zip(rows, cols, vals):
+        J[int(a), int(b)] = v
+    prob = fast.Problem(tools.GenerateNeighbors(n, J, 4))
+    sched = bench.schedule(bench.NSCHED)
+    jp = fast.jperp_schedule(sched, P, bench.TEMP)
+    spins = np.ascontiguousarray(np.repeat(bench.initial_spins(0, R, n)[:, :, None], P, axis=2))
+    words = prob.pack(torch.from_numpy(spins))
+    w0 = _words_u64(words)
+    seed = bench.BENCH_SEED
+    fast.anneal(prob, words, sched, P, bench.TEMP, seed=seed, jperp=torch.from_numpy(jp).cuda())
+    got = _words_u64(words)
+    for r in (0, R - 1):
+        w = w0[r].copy()
+        oracle.fast_anneal(prob.nbr_host, prob.cpl_host, prob.field_host, prob.class_size, prob.class_stride, w, P,
+                           jp, 1, np.float32(1.0) / np.float32(bench.TEMP), seed, replica=r)
+        np.testing.assert_array_equal(got[r], w, err_msg="replica %d" % r)
+
+
 def test_fast_staged_phases_in_chunks():
     """A 220 x 220 lattice with 128-thread CTAs: a queue that holds a whole phase would pass
     the shared-memory budget, so the scan goes through each phase in chunks of words the
