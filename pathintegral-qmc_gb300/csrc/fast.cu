@@ -118,29 +118,54 @@ auto fast_kernel() {
     else return qa_fast_kernel<W, MAXDEG, NQC, STAGED>;
 }
 
-// FP64 energy of one (replica, slice) per warp from the CSR of the coupling matrix.
+// FP64 energy of (replica, slice) from the CSR of the coupling matrix.  A warp takes
+// kEnergySlices slices of one replica, so each CSR entry it loads serves all of them;
+// every slice's operations and their order are those of one warp per slice (per row
+// rowsum += val * s_j in CSR order, acc += s_i * rowsum over the lane's rows, then the
+// warp's shuffle reduction).  A product with s = +-1 is exactly the value with its sign
+// bit flipped, so it is formed on the bits: one FP64 add per entry and slice.
+constexpr int kEnergySlices = 8;
+
+__device__ __forceinline__ double signed_by_bit(double v, uint64_t bit) {
+    return __longlong_as_double(__double_as_longlong(v) ^ (long long)(bit << 63));
+}
+
 template <typename W>
 __global__ void energy_packed_kernel(const W* __restrict__ words, int n, int P, int R,
                                      const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
                                      const double* __restrict__ val, double* __restrict__ out) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (warp >= R * P) return;
-    const int r = warp / P, k = warp % P;
+    const int chunks = (P + kEnergySlices - 1) / kEnergySlices;
+    if (warp >= R * chunks) return;
+    const int r = warp / chunks, k0 = (warp % chunks) * kEnergySlices;
     const W* w = words + (int64_t)r * n;
-    double acc = 0.0;
+    double acc[kEnergySlices];
+#pragma unroll
+    for (int c = 0; c < kEnergySlices; ++c) acc[c] = 0.0;
     for (int i = lane; i < n; i += 32) {
-        const double si = ((w[i] >> k) & 1) ? -1.0 : 1.0;
-        double rowsum = 0.0;
+        const W wi = w[i] >> k0;
+        double rowsum[kEnergySlices];
+#pragma unroll
+        for (int c = 0; c < kEnergySlices; ++c) rowsum[c] = 0.0;
         for (int64_t e = row_ptr[i]; e < row_ptr[i + 1]; ++e) {
             const int j = col[e];
-            const double sj = (j == i) ? 1.0 : ((((unsigned)j < (unsigned)n) && ((w[j] >> k) & 1)) ? -1.0 : 1.0);
-            rowsum += val[e] * sj;
+            const double v = val[e];
+            const W wj = j == i ? (W)0 : (((unsigned)j < (unsigned)n) ? (W)(w[j] >> k0) : (W)0);
+#pragma unroll
+            for (int c = 0; c < kEnergySlices; ++c) rowsum[c] += signed_by_bit(v, (uint64_t)((wj >> c) & 1));
         }
-        acc += si * rowsum;
+#pragma unroll
+        for (int c = 0; c < kEnergySlices; ++c) acc[c] += signed_by_bit(rowsum[c], (uint64_t)((wi >> c) & 1));
     }
-    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
-    if (lane == 0) out[warp] = -acc;
+#pragma unroll
+    for (int c = 0; c < kEnergySlices; ++c)
+        for (int off = 16; off > 0; off >>= 1) acc[c] += __shfl_down_sync(0xffffffffu, acc[c], off);
+    if (lane == 0) {
+#pragma unroll
+        for (int c = 0; c < kEnergySlices; ++c)
+            if (k0 + c < P) out[(int64_t)r * P + k0 + c] = -acc[c];
+    }
 }
 
 // Configuration streaming between the int8 layout [R][n][P] and packed words.
@@ -363,7 +388,7 @@ int pq_energy_packed(const void* words, int word_bits, int n, int P, int R, cons
     if (!words || !row_ptr || !out || n <= 0 || P < 1 || R < 0) return PQ_ERR_INVALID_ARG;
     if (!((word_bits == 32 && P <= 32) || (word_bits == 64 && P <= 64))) return PQ_ERR_INVALID_ARG;
     if (R == 0) return PQ_OK;
-    const int64_t warps = (int64_t)R * P;
+    const int64_t warps = (int64_t)R * ((P + kEnergySlices - 1) / kEnergySlices);
     const unsigned blocks = (unsigned)((warps * 32 + 255) / 256);
     cudaStream_t st = (cudaStream_t)stream;
     if (word_bits == 32)
