@@ -48,9 +48,26 @@ def _p(a):
     return a.ctypes.data_as(ctypes.c_void_p)
 
 
+def _kings(L, g):
+    """A periodic King's graph (eight couplings per spin), fields on every spin."""
+    import scipy.sparse as sps
+    n = L * L
+    J = sps.dok_matrix((n, n))
+    for y in range(L):
+        for x in range(L):
+            i = y * L + x
+            for dx, dy in ((1, 0), (0, 1), (1, 1), (1, -1)):
+                j = ((y + dy) % L) * L + (x + dx) % L
+                J[min(i, j), max(i, j)] = g.normal()
+            J[i, i] = g.normal(0, 0.3)
+    return J
+
+
 def _problem(L, periodic, seed, fields):
     from piqmc import fast, tools
     g = np.random.default_rng(seed)
+    if fields == "kings":
+        return fast.Problem(tools.GenerateNeighbors(L * L, _kings(L, g), 9), on_device=False)
     J = lattice(L, periodic, g, dist=lambda r: r.normal(),
                 fields=(lambda r: r.normal(0, 0.3)) if fields else None)
     return fast.Problem(tools.GenerateNeighbors(L * L, J, 5), on_device=False)
@@ -88,7 +105,8 @@ def _run(prob, P, sched, T, mcsteps=1, global_moves=0, betas=None, seed=5, break
 _UP_DOWN = np.concatenate([np.linspace(3.0, 0.2, 30), np.linspace(0.3, 1.5, 10), np.linspace(1.5, 1e-8, 40)])
 
 CASES = [
-    # (lattice side, periodic, fields, P, schedule, T, mcsteps, global moves, betas, straight start)
+    # (lattice side, periodic, fields (or "kings" for a King's graph), P, schedule, T, mcsteps,
+    #  global moves, betas, straight start)
     (12, True, True, 20, np.linspace(3.0, 1e-8, 120), 0.05, 1, 0, None, True),
     (12, True, False, 16, np.linspace(3.0, 1e-8, 120), 0.05, 2, 1, None, True),
     (11, True, True, 8, _UP_DOWN, 0.05, 1, 0, None, True),            # odd torus: three colours
@@ -97,6 +115,7 @@ CASES = [
      (1.0 / np.concatenate([np.linspace(1.0, 0.05, 30), np.full(6, 0.4), np.linspace(0.4, 0.05, 24)])), True),
     (9, True, False, 64, np.linspace(3.0, 1e-8, 60), 0.05, 1, 1, None, True),
     (12, True, True, 20, np.linspace(3.0, 1e-8, 300), 0.05, 1, 0, None, False),   # kinked start
+    (12, True, "kings", 20, np.linspace(3.0, 1e-8, 120), 0.05, 1, 1, None, True),  # eight couplings
 ]
 
 
